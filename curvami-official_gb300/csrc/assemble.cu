@@ -1,0 +1,812 @@
+// assemble.cu — stage B on sm_103a: the Kirchhoff-Love residual and tangent of every
+// face Gauss point, the elastic hinge, and their scatter into the block-upper CSC K.
+//
+// Reference: NonLinearAssembler::updateStiffness (plate/Assembly.h:158-345),
+// Kinematics::compute (plate/Kinematics.h:61-120), Constitutive::evaluate
+// (plate/Constitutive.h:57-70), Constraints::evaluateElasticFold / foldAngleAndGrad
+// (plate/Constraints.h:54-119, 341-436), Meshless::assembleSystem* (plate/Meshless.h:102-127)
+// and the energies (plate/Meshless.h:197-220, Constraints.h:310-339).
+//
+// One warp per Gauss point. Lanes first reduce the kinematic sums (r0,a and r0,ab over
+// the neighbours) with shuffles, every lane then holds the point's frame a1, a2, b,
+// C0^-1 and the resultants N, M. Per neighbour (lane-strided) the FP64 residual
+// contribution is formed and scattered, and a record of the neighbour's factors is
+// staged in shared memory. The pair loop then spreads the n(n+1)/2 blocks over the
+// lanes. Each block is written in the rank-3 form
+//     K_IJ = a1 (x) Y1 + a2 (x) Y2 + b (x) Y3 + geo I,
+// which follows from Bm_I = a1 (x) (dx, 0, dy) + a2 (x) (0, dy, dx) in strain space,
+// Bb_I = beta_I (x) b, Db_J = -(a1 c_J0 + a2 c_J1) (x) b with c_J = C0^-1 grad Phi_J:
+//     Y1 = dx_I P_J0 + dy_I P_J2 - Tu_I c_J0 b
+//     Y2 = dy_I P_J1 + dx_I P_J2 - Tu_I c_J1 b
+//     Y3 = beta_I . Q_J - Tu_J (a1 c_I0 + a2 c_I1) + bv (dPhi_I . c_J) b
+//     geo = dPhi_I . N dPhi_J,
+// the same terms as K_mat + K_geo_m + T12 + T3 of Assembly.h:290-300 (70 FMA per block
+// against the reference's ~90), with the Gauss weight folded into the J-side factors.
+//
+// Precision modes: FP64 throughout, or "mixed" (FP64 kinematics, resultants and
+// residual; the per-neighbour factors and the pair loop in FP32, accumulated into an
+// FP32 block array that is widened to FP64 on output).
+// Scatter modes: atomics into a block array (BSR, one 3x3 block per pattern slot), or
+// deterministic: every block value goes to a contribution array and a second kernel
+// sums each block's contributions in ascending Gauss-point order.
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "cgb_device.cuh"
+#include "cgb_internal.h"
+
+namespace cgb {
+namespace {
+
+constexpr int kFaceWarps = 4;
+constexpr int kRecI = 9;   // dx dy beta0 beta1 beta2 Tu g0 g1 g2
+constexpr int kRecJ = 23;  // P(9) Q(9) cW0 cW1 nW0 nW1 TuW
+constexpr int kRec = kRecI + kRecJ;
+
+struct Material { double A[9], B[9], D[9]; };
+
+struct FaceArgs {
+  int n_gp;
+  int nmax;
+  const int64_t* ptr;
+  const int32_t* idx;
+  const double* dpsi;
+  const double* ddpsi;
+  const double* weight;
+  const double* x;
+  const int64_t* map_ptr;
+  const int32_t* map_slot;
+  Material mat;
+  double* F;         // atomic F (3 n_nodes)
+  double* Fc;        // deterministic F contributions (3 per entry)
+  void* Kacc;        // atomic block accumulator
+  void* Kc;          // deterministic contributions (9 per pair)
+};
+
+// Per-point kinematics and resultants (Kinematics.h:61-120, Constitutive.h:57-70).
+struct PointState {
+  double a1[3], a2[3], rxx[3], ryy[3], rxy[3], b[3];
+  double Ci[4];   // C0^-1 row-major
+  double N[3], M[3];
+  double pXY[2];
+  double bv;
+  double e0[3], e1[3];
+};
+
+__device__ __forceinline__ void point_state(const double s[15], const Material& m, PointState& P) {
+  P.a1[0] = 1.0 + s[0]; P.a1[1] = s[1]; P.a1[2] = s[2];
+  P.a2[0] = s[3]; P.a2[1] = 1.0 + s[4]; P.a2[2] = s[5];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { P.rxx[c] = s[6 + c]; P.ryy[c] = s[9 + c]; P.rxy[c] = s[12 + c]; }
+  const double C00 = P.a1[0] * P.a1[0] + P.a1[1] * P.a1[1] + P.a1[2] * P.a1[2];
+  const double C11 = P.a2[0] * P.a2[0] + P.a2[1] * P.a2[1] + P.a2[2] * P.a2[2];
+  const double C01 = P.a1[0] * P.a2[0] + P.a1[1] * P.a2[1] + P.a1[2] * P.a2[2];
+  const double det = C00 * C11 - C01 * C01;
+  const double id = 1.0 / det;
+  P.Ci[0] = C11 * id; P.Ci[1] = -C01 * id; P.Ci[2] = -C01 * id; P.Ci[3] = C00 * id;
+  double n[3] = {P.a1[1] * P.a2[2] - P.a1[2] * P.a2[1], P.a1[2] * P.a2[0] - P.a1[0] * P.a2[2],
+                 P.a1[0] * P.a2[1] - P.a1[1] * P.a2[0]};
+  const double area = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) P.b[c] = n[c] / area;
+  P.e0[0] = 0.5 * (C00 - 1.0);
+  P.e0[1] = 0.5 * (C11 - 1.0);
+  P.e0[2] = 2.0 * (0.5 * C01);
+  P.e1[0] = -(P.rxx[0] * P.b[0] + P.rxx[1] * P.b[1] + P.rxx[2] * P.b[2]);
+  P.e1[1] = -(P.ryy[0] * P.b[0] + P.ryy[1] * P.b[1] + P.ryy[2] * P.b[2]);
+  P.e1[2] = 2.0 * -(P.rxy[0] * P.b[0] + P.rxy[1] * P.b[1] + P.rxy[2] * P.b[2]);
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    P.N[r] = m.A[3 * r] * P.e0[0] + m.A[3 * r + 1] * P.e0[1] + m.A[3 * r + 2] * P.e0[2] +
+             (m.B[3 * r] * P.e1[0] + m.B[3 * r + 1] * P.e1[1] + m.B[3 * r + 2] * P.e1[2]);
+    P.M[r] = m.B[r] * P.e0[0] + m.B[3 + r] * P.e0[1] + m.B[6 + r] * P.e0[2] +
+             (m.D[3 * r] * P.e1[0] + m.D[3 * r + 1] * P.e1[1] + m.D[3 * r + 2] * P.e1[2]);
+  }
+  double vc[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) vc[c] = P.rxx[c] * P.M[0] + 2.0 * P.rxy[c] * P.M[2] + P.ryy[c] * P.M[1];
+  P.bv = P.b[0] * vc[0] + P.b[1] * vc[1] + P.b[2] * vc[2];
+  const double fa = P.a1[0] * vc[0] + P.a1[1] * vc[1] + P.a1[2] * vc[2];
+  const double fb = P.a2[0] * vc[0] + P.a2[1] * vc[1] + P.a2[2] * vc[2];
+  P.pXY[0] = P.Ci[0] * fa + P.Ci[1] * fb;
+  P.pXY[1] = P.Ci[2] * fa + P.Ci[3] * fb;
+}
+
+// Kinematic sums over the neighbours, lane-strided, reduced across the warp.
+__device__ __forceinline__ void kin_sums(int lane, int64_t p0, int n, const int32_t* idx, const double* dpsi,
+                                         const double* ddpsi, const double* x, double s[15]) {
+#pragma unroll
+  for (int k = 0; k < 15; ++k) s[k] = 0.0;
+  for (int a = lane; a < n; a += 32) {
+    const int64_t e = p0 + a;
+    const int64_t j = idx[e];
+    const double u0 = x[3 * j], u1 = x[3 * j + 1], u2 = x[3 * j + 2];
+    const double2 d = reinterpret_cast<const double2*>(dpsi)[e];
+    const double dxx = ddpsi[3 * e], dyy = ddpsi[3 * e + 1], dxy = ddpsi[3 * e + 2];
+    s[0] += u0 * d.x; s[1] += u1 * d.x; s[2] += u2 * d.x;
+    s[3] += u0 * d.y; s[4] += u1 * d.y; s[5] += u2 * d.y;
+    s[6] += u0 * dxx; s[7] += u1 * dxx; s[8] += u2 * dxx;
+    s[9] += u0 * dyy; s[10] += u1 * dyy; s[11] += u2 * dyy;
+    s[12] += u0 * dxy; s[13] += u1 * dxy; s[14] += u2 * dxy;
+  }
+#pragma unroll
+  for (int k = 0; k < 15; ++k) s[k] = warp_sum(s[k]);
+}
+
+// Scatter of one block into the accumulators. v is row-major in the local (I, J)
+// orientation; the stored block is (min node, max node), transposed when flipped.
+template <typename TK>
+__device__ __forceinline__ void scatter_atomic(void* acc, int32_t slot, bool flip, const TK v[9]);
+
+template <>
+__device__ __forceinline__ void scatter_atomic<double>(void* acc, int32_t slot, bool flip, const double v[9]) {
+  double* d = static_cast<double*>(acc) + 9 * static_cast<int64_t>(slot);
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) atomicAdd(d + 3 * r + c, flip ? v[3 * c + r] : v[3 * r + c]);
+}
+
+template <>
+__device__ __forceinline__ void scatter_atomic<float>(void* acc, int32_t slot, bool flip, const float v[9]) {
+  // 12 floats per block: three 16-byte vector atomics.
+  float4* d = reinterpret_cast<float4*>(static_cast<float*>(acc) + 12 * static_cast<int64_t>(slot));
+  float t[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) t[3 * r + c] = flip ? v[3 * c + r] : v[3 * r + c];
+  atomicAdd(d, make_float4(t[0], t[1], t[2], t[3]));
+  atomicAdd(d + 1, make_float4(t[4], t[5], t[6], t[7]));
+  atomicAdd(d + 2, make_float4(t[8], 0.0f, 0.0f, 0.0f));
+}
+
+template <typename TK>
+__device__ __forceinline__ void store_contrib(void* cbuf, int64_t q, bool flip, const TK v[9]) {
+  TK* d = static_cast<TK*>(cbuf) + 9 * q;
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) d[3 * r + c] = flip ? v[3 * c + r] : v[3 * r + c];
+}
+
+template <typename TK, bool DET, bool WANT_K>
+__global__ void __launch_bounds__(32 * kFaceWarps) face_kernel(FaceArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nmax = a.nmax;
+  TK* rec = reinterpret_cast<TK*>(smem_raw) + static_cast<size_t>(w) * kRec * nmax;
+  int* nid = reinterpret_cast<int*>(reinterpret_cast<TK*>(smem_raw) + static_cast<size_t>(kFaceWarps) * kRec * nmax) +
+             w * nmax;
+  const Material& m = a.mat;
+  TK At[9], Bt[9], Dt[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { At[k] = static_cast<TK>(m.A[k]); Bt[k] = static_cast<TK>(m.B[k]); Dt[k] = static_cast<TK>(m.D[k]); }
+
+  for (int g = blockIdx.x * kFaceWarps + w; g < a.n_gp; g += gridDim.x * kFaceWarps) {
+    const int64_t p0 = a.ptr[g];
+    const int n = static_cast<int>(a.ptr[g + 1] - p0);
+    if (n == 0) continue;  // Assembly.h:208
+    double s[15];
+    kin_sums(lane, p0, n, a.idx, a.dpsi, a.ddpsi, a.x, s);
+    PointState P;
+    point_state(s, m, P);
+    const double W = a.weight[g];
+
+    // ---- per neighbour: residual (FP64) and the pair-loop record ----
+    for (int i = lane; i < n; i += 32) {
+      const int64_t e = p0 + i;
+      const int node = a.idx[e];
+      const double2 d = reinterpret_cast<const double2*>(a.dpsi)[e];
+      const double dxx = a.ddpsi[3 * e], dyy = a.ddpsi[3 * e + 1], dxy = a.ddpsi[3 * e + 2];
+      const double c0 = P.Ci[0] * d.x + P.Ci[1] * d.y;
+      const double c1 = P.Ci[2] * d.x + P.Ci[3] * d.y;
+      double gI[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) gI[r] = P.a1[r] * c0 + P.a2[r] * c1;
+      const double SXX = P.rxx[0] * gI[0] + P.rxx[1] * gI[1] + P.rxx[2] * gI[2];
+      const double SYY = P.ryy[0] * gI[0] + P.ryy[1] * gI[1] + P.ryy[2] * gI[2];
+      const double SXY = P.rxy[0] * gI[0] + P.rxy[1] * gI[1] + P.rxy[2] * gI[2];
+      const double be0 = -dxx + SXX, be1 = -dyy + SYY, be2 = 2.0 * (-dxy + SXY);
+      // f = (Bm^T N + Bb^T M) W (Assembly.h:249-250).
+      const double fm1 = d.x * P.N[0] + d.y * P.N[2];
+      const double fm2 = d.y * P.N[1] + d.x * P.N[2];
+      const double fbm = be0 * P.M[0] + be1 * P.M[1] + be2 * P.M[2];
+      double f[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] = (P.a1[c] * fm1 + P.a2[c] * fm2 + P.b[c] * fbm) * W;
+      if (DET) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) a.Fc[3 * e + c] = f[c];
+      } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) atomicAdd(a.F + 3 * static_cast<int64_t>(node) + c, f[c]);
+      }
+      if (!WANT_K) continue;
+      // Record in the tangent's precision.
+      const TK dx = static_cast<TK>(d.x), dy = static_cast<TK>(d.y);
+      const TK b0 = static_cast<TK>(be0), b1 = static_cast<TK>(be1), b2 = static_cast<TK>(be2);
+      const TK Tu = static_cast<TK>(d.x * P.pXY[0] + d.y * P.pXY[1] -
+                                    (dxx * P.M[0] + 2.0 * dxy * P.M[2] + dyy * P.M[1]));
+      const TK Wt = static_cast<TK>(W);
+      TK* R = rec + i;
+      R[0 * nmax] = dx; R[1 * nmax] = dy;
+      R[2 * nmax] = b0; R[3 * nmax] = b1; R[4 * nmax] = b2;
+      R[5 * nmax] = Tu;
+#pragma unroll
+      for (int r = 0; r < 3; ++r) R[(6 + r) * nmax] = static_cast<TK>(gI[r]);
+      // P = A Bm + B Bb, Q = B Bm + D Bb (Assembly.h:255-256), times W:
+      //   P(r,c) = a1_c pa_r + a2_c pb_r + b_c pc_r.
+      TK a1t[3], a2t[3], bt[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) { a1t[c] = static_cast<TK>(P.a1[c]); a2t[c] = static_cast<TK>(P.a2[c]); bt[c] = static_cast<TK>(P.b[c]); }
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const TK pa = (At[3 * r] * dx + At[3 * r + 2] * dy) * Wt;
+        const TK pb = (At[3 * r + 1] * dy + At[3 * r + 2] * dx) * Wt;
+        const TK pc = (Bt[3 * r] * b0 + Bt[3 * r + 1] * b1 + Bt[3 * r + 2] * b2) * Wt;
+        const TK qa = (Bt[3 * r] * dx + Bt[3 * r + 2] * dy) * Wt;
+        const TK qb = (Bt[3 * r + 1] * dy + Bt[3 * r + 2] * dx) * Wt;
+        const TK qc = (Dt[3 * r] * b0 + Dt[3 * r + 1] * b1 + Dt[3 * r + 2] * b2) * Wt;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          R[(kRecI + 3 * r + c) * nmax] = a1t[c] * pa + a2t[c] * pb + bt[c] * pc;
+          R[(kRecI + 9 + 3 * r + c) * nmax] = a1t[c] * qa + a2t[c] * qb + bt[c] * qc;
+        }
+      }
+      R[(kRecI + 18) * nmax] = static_cast<TK>(c0 * W);
+      R[(kRecI + 19) * nmax] = static_cast<TK>(c1 * W);
+      R[(kRecI + 20) * nmax] = static_cast<TK>((P.N[0] * d.x + P.N[2] * d.y) * W);
+      R[(kRecI + 21) * nmax] = static_cast<TK>((P.N[2] * d.x + P.N[1] * d.y) * W);
+      R[(kRecI + 22) * nmax] = Tu * Wt;
+      nid[i] = node;
+    }
+    if (!WANT_K) continue;
+    __syncwarp();
+
+    // ---- pair loop ----
+    TK a1t[3], a2t[3], bt[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { a1t[c] = static_cast<TK>(P.a1[c]); a2t[c] = static_cast<TK>(P.a2[c]); bt[c] = static_cast<TK>(P.b[c]); }
+    const TK bv = static_cast<TK>(P.bv);
+    const int64_t np = static_cast<int64_t>(n) * (n + 1) / 2;
+    const int64_t m0 = a.map_ptr[g];
+    int i = 0, off = lane;
+    while (i < n && off >= n - i) { off -= n - i; ++i; }
+    for (int64_t p = lane; p < np; p += 32) {
+      const int j = i + off;
+      const TK* RI = rec + i;
+      const TK* RJ = rec + j;
+      const TK dxi = RI[0], dyi = RI[nmax], be0 = RI[2 * nmax], be1 = RI[3 * nmax], be2 = RI[4 * nmax];
+      const TK Tui = RI[5 * nmax], gi0 = RI[6 * nmax], gi1 = RI[7 * nmax], gi2 = RI[8 * nmax];
+      const TK cj0 = RJ[(kRecI + 18) * nmax], cj1 = RJ[(kRecI + 19) * nmax];
+      const TK nj0 = RJ[(kRecI + 20) * nmax], nj1 = RJ[(kRecI + 21) * nmax];
+      const TK TuWj = RJ[(kRecI + 22) * nmax];
+      const TK s1 = Tui * cj0, s2 = Tui * cj1;
+      const TK t3 = bv * (dxi * cj0 + dyi * cj1);
+      const TK geo = dxi * nj0 + dyi * nj1;
+      TK Y1[3], Y2[3], Y3[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const TK P0 = RJ[(kRecI + c) * nmax], P1 = RJ[(kRecI + 3 + c) * nmax], P2 = RJ[(kRecI + 6 + c) * nmax];
+        const TK Q0 = RJ[(kRecI + 9 + c) * nmax], Q1 = RJ[(kRecI + 12 + c) * nmax], Q2 = RJ[(kRecI + 15 + c) * nmax];
+        const TK gic = c == 0 ? gi0 : (c == 1 ? gi1 : gi2);
+        Y1[c] = dxi * P0 + dyi * P2 - s1 * bt[c];
+        Y2[c] = dyi * P1 + dxi * P2 - s2 * bt[c];
+        Y3[c] = be0 * Q0 + be1 * Q1 + be2 * Q2 + t3 * bt[c] - TuWj * gic;
+      }
+      TK v[9];
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          v[3 * r + c] = a1t[r] * Y1[c] + a2t[r] * Y2[c] + bt[r] * Y3[c] + (r == c ? geo : TK(0));
+      const bool flip = nid[i] > nid[j];
+      if (DET) {
+        store_contrib<TK>(a.Kc, m0 + p, flip, v);
+      } else {
+        scatter_atomic<TK>(a.Kacc, a.map_slot[m0 + p], flip, v);
+      }
+      off += 32;
+      while (i < n && off >= n - i) { off -= n - i; ++i; }
+    }
+    __syncwarp();
+  }
+}
+
+// ---- hinge (FP64) -----------------------------------------------------------------
+
+struct HingeArgs {
+  int n_gp;
+  int max_u;
+  const int64_t* lptr; const int32_t* lidx; const double* ldpsi;
+  const int64_t* rptr; const int32_t* ridx; const double* rdpsi;
+  const double* weight; const double* tangent;
+  double Kt, theta0;
+  const double* theta0_gp; const int8_t* active;
+  const int64_t* u_ptr; const int32_t* u_node; const int32_t* l_pos; const int32_t* r_pos;
+  const int64_t* pair_ptr; const int32_t* pair_slot;
+  const double* x;
+  int exact;
+  int want_K;
+  int tk_float;      // accumulator type
+  double* F; void* Kacc;              // atomic mode
+  double* Fc; void* Kc;               // deterministic mode
+  int64_t f_base, k_base;             // contribution id offsets of this fold
+};
+
+__device__ __forceinline__ void cross(const double* a, const double* b, double* c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+__device__ __forceinline__ double dot(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// Constraints::foldAngleAndGrad (plate/Constraints.h:54-119).
+__device__ double fold_angle(const double* F, double tx, double ty, double* grad) {
+  const double *a1L = F, *a2L = F + 3, *a1R = F + 6, *a2R = F + 9;
+  double nL[3], nR[3];
+  cross(a1L, a2L, nL); cross(a1R, a2R, nR);
+  const double normL = sqrt(dot(nL, nL)), normR = sqrt(dot(nR, nR));
+  double bL[3], bR[3], aT[3], t[3];
+  for (int c = 0; c < 3; ++c) { bL[c] = nL[c] / normL; bR[c] = nR[c] / normR; aT[c] = a1L[c] * tx + a2L[c] * ty; }
+  const double naT = sqrt(dot(aT, aT));
+  for (int c = 0; c < 3; ++c) t[c] = aT[c] / naT;
+  const double cth = dot(bL, bR);
+  double bxb[3];
+  cross(bL, bR, bxb);
+  const double sth = dot(bxb, t);
+  const double theta = atan2(-sth, cth);
+  if (grad) {
+    double dbL[3][6], dbR[3][6];
+    for (int side = 0; side < 2; ++side) {
+      const double* a1 = side ? a1R : a1L;
+      const double* a2 = side ? a2R : a2L;
+      const double* b = side ? bR : bL;
+      const double nn = side ? normR : normL;
+      double (*out)[6] = side ? dbR : dbL;
+      double dn[3][6];
+      for (int i = 0; i < 3; ++i) {
+        double e[3] = {0, 0, 0};
+        e[i] = 1.0;
+        double c1[3], c2[3];
+        cross(e, a2, c1); cross(a1, e, c2);
+        for (int r = 0; r < 3; ++r) { dn[r][i] = c1[r]; dn[r][i + 3] = c2[r]; }
+      }
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 6; ++c) {
+          double acc = 0.0;
+          for (int k = 0; k < 3; ++k) acc += (((r == k) ? 1.0 : 0.0) - b[r] * b[k]) / nn * dn[k][c];
+          out[r][c] = acc;
+        }
+    }
+    double dt[3][6];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 6; ++c) {
+        double acc = 0.0;
+        for (int k = 0; k < 3; ++k) {
+          const double daT = (c < 3) ? ((c == k) ? tx : 0.0) : ((c - 3 == k) ? ty : 0.0);
+          acc += (((r == k) ? 1.0 : 0.0) - t[r] * t[k]) / naT * daT;
+        }
+        dt[r][c] = acc;
+      }
+    double bRxt[3], txbL[3];
+    cross(bR, t, bRxt); cross(t, bL, txbL);
+    const double denom = cth * cth + sth * sth;
+    const double inv = (denom > 1e-14) ? 1.0 / denom : 0.0;
+    for (int c = 0; c < 6; ++c) {
+      const double dcL = bR[0] * dbL[0][c] + bR[1] * dbL[1][c] + bR[2] * dbL[2][c];
+      const double dcR = bL[0] * dbR[0][c] + bL[1] * dbR[1][c] + bL[2] * dbR[2][c];
+      const double dsL = (bRxt[0] * dbL[0][c] + bRxt[1] * dbL[1][c] + bRxt[2] * dbL[2][c]) +
+                         (bxb[0] * dt[0][c] + bxb[1] * dt[1][c] + bxb[2] * dt[2][c]);
+      const double dsR = txbL[0] * dbR[0][c] + txbL[1] * dbR[1][c] + txbL[2] * dbR[2][c];
+      grad[c] = -(cth * dsL - sth * dcL) * inv;
+      grad[6 + c] = -(cth * dsR - sth * dcR) * inv;
+    }
+  }
+  return theta;
+}
+
+constexpr int kHingeWarps = 2;
+
+// One warp per crease Gauss point (Constraints.h:349-435). The left and right
+// entries are merged per node: with G_u = sum of the dof gradients of node u over both
+// sides, the reference's triplets (all k, m with node_k <= node_m) sum to
+// W Kt G_P (x) G_Q (+ W moment B_P^T H B_Q) on block (P, Q) of the merged list.
+__global__ void __launch_bounds__(32 * kHingeWarps) hinge_kernel(HingeArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // Per warp: G[3*max_u], Bsum[4*max_u], H[144] (+16 spare).
+  double* base = reinterpret_cast<double*>(smem_raw) + static_cast<size_t>(w) * (7 * a.max_u + 144 + 16);
+  double* G = base;
+  double* Bs = base + 3 * a.max_u;
+  double* H = base + 7 * a.max_u;
+  for (int g = blockIdx.x * kHingeWarps + w; g < a.n_gp; g += gridDim.x * kHingeWarps) {
+    if (a.active && a.active[g] == 0) continue;  // Constraints.h:350
+    double sL[6] = {0, 0, 0, 0, 0, 0}, sR[6] = {0, 0, 0, 0, 0, 0};
+    for (int64_t e = a.lptr[g] + lane; e < a.lptr[g + 1]; e += 32) {
+      const int64_t j = a.lidx[e];
+      const double dX = a.ldpsi[2 * e], dY = a.ldpsi[2 * e + 1];
+      for (int c = 0; c < 3; ++c) { sL[c] += a.x[3 * j + c] * dX; sL[3 + c] += a.x[3 * j + c] * dY; }
+    }
+    for (int64_t e = a.rptr[g] + lane; e < a.rptr[g + 1]; e += 32) {
+      const int64_t j = a.ridx[e];
+      const double dX = a.rdpsi[2 * e], dY = a.rdpsi[2 * e + 1];
+      for (int c = 0; c < 3; ++c) { sR[c] += a.x[3 * j + c] * dX; sR[3 + c] += a.x[3 * j + c] * dY; }
+    }
+    double F12[12];
+    for (int k = 0; k < 6; ++k) { F12[k] = warp_sum(sL[k]); F12[6 + k] = warp_sum(sR[k]); }
+    F12[0] += 1.0; F12[4] += 1.0; F12[6] += 1.0; F12[10] += 1.0;
+    const double tx = a.tangent[2 * g], ty = a.tangent[2 * g + 1];
+    double grad[12];
+    const double theta = fold_angle(F12, tx, ty, grad);
+    const double th0 = a.theta0_gp ? a.theta0_gp[g] : a.theta0;
+    const double W = a.weight[g];
+    const double Wm = W * (a.Kt * (theta - th0));
+    const double WK = W * a.Kt;
+    const bool use_hess = a.exact && a.want_K && fabs(Wm) > 0.0;
+    if (use_hess) {
+      // Central differences of the analytic gradient (Constraints.h:402-413), one
+      // perturbed evaluation per lane (24 lanes), then symmetrised.
+      double mx = 0.0;
+      for (int k = 0; k < 12; ++k) mx = fmax(mx, fabs(F12[k]));
+      const double hs = 1e-6 * fmax(1.0, mx);
+      if (lane < 24) {
+        const int k = lane >> 1;
+        double Fp[12];
+        for (int q = 0; q < 12; ++q) Fp[q] = F12[q];
+        Fp[k] += (lane & 1) ? -hs : hs;
+        double gp[12];
+        fold_angle(Fp, tx, ty, gp);
+        // H[r][k] = (g+ - g-)/(2h): the '+' lane stores g+, the '-' lane subtracts it.
+        if ((lane & 1) == 0) for (int r = 0; r < 12; ++r) H[r * 12 + k] = gp[r];
+        __syncwarp(0x00ffffffu);
+        if (lane & 1) for (int r = 0; r < 12; ++r) H[r * 12 + k] = (H[r * 12 + k] - gp[r]) / (2.0 * hs);
+      }
+      __syncwarp();
+      if (lane < 12) {
+        double row[12];
+        for (int c = 0; c < 12; ++c) row[c] = 0.5 * (H[lane * 12 + c] + H[c * 12 + lane]);
+        __syncwarp(0x00000fffu);
+        for (int c = 0; c < 12; ++c) H[lane * 12 + c] = row[c];
+      }
+      __syncwarp();
+    }
+    // Per merged node: G_u (3) and the summed (dX, dY) of each side (4).
+    const int64_t u0 = a.u_ptr[g];
+    const int mu = static_cast<int>(a.u_ptr[g + 1] - u0);
+    for (int u = lane; u < mu; u += 32) {
+      G[3 * u] = 0.0; G[3 * u + 1] = 0.0; G[3 * u + 2] = 0.0;
+      Bs[4 * u] = 0.0; Bs[4 * u + 1] = 0.0; Bs[4 * u + 2] = 0.0; Bs[4 * u + 3] = 0.0;
+    }
+    __syncwarp();
+    // Left then right: within a side every node occurs once, so no two lanes collide.
+    for (int64_t e = a.lptr[g] + lane; e < a.lptr[g + 1]; e += 32) {
+      const int u = a.l_pos[e];
+      const double dX = a.ldpsi[2 * e], dY = a.ldpsi[2 * e + 1];
+      for (int d = 0; d < 3; ++d) G[3 * u + d] += grad[d] * dX + grad[d + 3] * dY;
+      Bs[4 * u] += dX; Bs[4 * u + 1] += dY;
+    }
+    __syncwarp();
+    for (int64_t e = a.rptr[g] + lane; e < a.rptr[g + 1]; e += 32) {
+      const int u = a.r_pos[e];
+      const double dX = a.rdpsi[2 * e], dY = a.rdpsi[2 * e + 1];
+      for (int d = 0; d < 3; ++d) G[3 * u + d] += grad[6 + d] * dX + grad[9 + d] * dY;
+      Bs[4 * u + 2] += dX; Bs[4 * u + 3] += dY;
+    }
+    __syncwarp();
+    for (int u = lane; u < mu; u += 32) {
+      const int node = a.u_node[u0 + u];
+      for (int d = 0; d < 3; ++d) {
+        const double f = G[3 * u + d] * Wm;
+        if (a.Fc) a.Fc[3 * (a.f_base + u0 + u) + d] = f;
+        else atomicAdd(a.F + 3 * static_cast<int64_t>(node) + d, f);
+      }
+    }
+    if (a.want_K) {
+      const int64_t np = static_cast<int64_t>(mu) * (mu + 1) / 2;
+      const int64_t q0 = a.pair_ptr[g];
+      int P = 0, off = lane;
+      while (P < mu && off >= mu - P) { off -= mu - P; ++P; }
+      for (int64_t p = lane; p < np; p += 32) {
+        const int Q = P + off;
+        double v[9];
+        for (int dk = 0; dk < 3; ++dk)
+          for (int dm = 0; dm < 3; ++dm) {
+            double val = WK * (G[3 * P + dk] * G[3 * Q + dm]);
+            if (use_hess) {
+              // B_P(dk) has dX_L at dk, dY_L at dk+3, dX_R at 6+dk, dY_R at 9+dk.
+              const int ik[4] = {dk, dk + 3, 6 + dk, 9 + dk};
+              const int im[4] = {dm, dm + 3, 6 + dm, 9 + dm};
+              double hb = 0.0;
+              for (int s1 = 0; s1 < 4; ++s1) {
+                double row = 0.0;
+                for (int s2 = 0; s2 < 4; ++s2) row += H[ik[s1] * 12 + im[s2]] * Bs[4 * Q + s2];
+                hb += Bs[4 * P + s1] * row;
+              }
+              val += Wm * hb;
+            }
+            v[3 * dk + dm] = val;
+          }
+        if (a.Kc) {
+          if (a.tk_float) { float t[9]; for (int k = 0; k < 9; ++k) t[k] = static_cast<float>(v[k]); store_contrib<float>(a.Kc, a.k_base + q0 + p, false, t); }
+          else store_contrib<double>(a.Kc, a.k_base + q0 + p, false, v);
+        } else {
+          const int32_t slot = a.pair_slot[q0 + p];
+          if (a.tk_float) { float t[9]; for (int k = 0; k < 9; ++k) t[k] = static_cast<float>(v[k]); scatter_atomic<float>(a.Kacc, slot, false, t); }
+          else scatter_atomic<double>(a.Kacc, slot, false, v);
+        }
+        off += 32;
+        while (P < mu && off >= mu - P) { off -= mu - P; ++P; }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---- output: blocks -> the reference's CSC -------------------------------------------
+// Column node j holds len_j block rows; scalar column 3j+c starts at 9 col_ptr[j] +
+// 3 c len_j and lists rows 3i+r for the block rows i ascending (Assembly.h:103-107).
+template <typename TA, int STRIDE>
+__global__ void blocks_to_csc(int n_nodes, const int64_t* __restrict__ col_ptr, const TA* __restrict__ acc,
+                              double* __restrict__ K) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t j = warp; j < n_nodes; j += nw) {
+    const int64_t b0 = col_ptr[j];
+    const int len = static_cast<int>(col_ptr[j + 1] - b0);
+    double* col = K + 9 * b0;
+    for (int t = lane; t < 9 * len; t += 32) {
+      // t enumerates the column's output in storage order: c major, then (pos, r).
+      const int c = t / (3 * len), rem = t - c * 3 * len, pos = rem / 3, r = rem - 3 * pos;
+      col[t] = static_cast<double>(acc[(b0 + pos) * STRIDE + 3 * r + c]);
+    }
+  }
+}
+
+// Deterministic: each block sums its contributions in ascending id order.
+template <typename TC>
+__global__ void det_reduce_blocks(int n_nodes, const int64_t* __restrict__ col_ptr,
+                                  const int64_t* __restrict__ lptr, const int64_t* __restrict__ list,
+                                  const TC* __restrict__ contrib, double* __restrict__ K) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t j = warp; j < n_nodes; j += nw) {
+    const int64_t b0 = col_ptr[j];
+    const int len = static_cast<int>(col_ptr[j + 1] - b0);
+    double* col = K + 9 * b0;
+    for (int pos = lane; pos < len; pos += 32) {
+      TC s[9];
+      for (int k = 0; k < 9; ++k) s[k] = TC(0);
+      for (int64_t q = lptr[b0 + pos]; q < lptr[b0 + pos + 1]; ++q) {
+        const TC* v = contrib + 9 * list[q];
+        for (int k = 0; k < 9; ++k) s[k] += v[k];
+      }
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) col[3 * c * len + 3 * pos + r] = static_cast<double>(s[3 * r + c]);
+    }
+  }
+}
+
+__global__ void det_reduce_F(int n_nodes, const int64_t* __restrict__ lptr, const int64_t* __restrict__ list,
+                             const double* __restrict__ fc, double* __restrict__ F) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_nodes) return;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int64_t q = lptr[j]; q < lptr[j + 1]; ++q) {
+    const double* v = fc + 3 * list[q];
+    s0 += v[0]; s1 += v[1]; s2 += v[2];
+  }
+  F[3 * j] = s0; F[3 * j + 1] = s1; F[3 * j + 2] = s2;
+}
+
+// ---- energies -----------------------------------------------------------------------
+__global__ void __launch_bounds__(128) face_energy_kernel(int n_gp, const int64_t* ptr, const int32_t* idx,
+                                                          const double* dpsi, const double* ddpsi,
+                                                          const double* weight, const double* x, Material m,
+                                                          double* out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  double em = 0.0, eb = 0.0;
+  for (int64_t g = warp; g < n_gp; g += nw) {
+    const int64_t p0 = ptr[g];
+    const int n = static_cast<int>(ptr[g + 1] - p0);
+    double s[15];
+    kin_sums(lane, p0, n, idx, dpsi, ddpsi, x, s);
+    PointState P;
+    point_state(s, m, P);
+    if (lane == 0) {
+      em += 0.5 * weight[g] * (P.e0[0] * P.N[0] + P.e0[1] * P.N[1] + P.e0[2] * P.N[2]);
+      eb += 0.5 * weight[g] * (P.e1[0] * P.M[0] + P.e1[1] * P.M[1] + P.e1[2] * P.M[2]);
+    }
+  }
+  if (lane == 0) { atomicAdd(out, em); atomicAdd(out + 1, eb); }
+}
+
+__global__ void hinge_energy_kernel(HingeArgs a, double* out) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= a.n_gp) return;
+  if (a.active && a.active[g] == 0) return;
+  double F12[12] = {1, 0, 0, 0, 1, 0, 1, 0, 0, 0, 1, 0};
+  for (int64_t e = a.lptr[g]; e < a.lptr[g + 1]; ++e) {
+    const int64_t j = a.lidx[e];
+    for (int c = 0; c < 3; ++c) { F12[c] += a.x[3 * j + c] * a.ldpsi[2 * e]; F12[3 + c] += a.x[3 * j + c] * a.ldpsi[2 * e + 1]; }
+  }
+  for (int64_t e = a.rptr[g]; e < a.rptr[g + 1]; ++e) {
+    const int64_t j = a.ridx[e];
+    for (int c = 0; c < 3; ++c) { F12[6 + c] += a.x[3 * j + c] * a.rdpsi[2 * e]; F12[9 + c] += a.x[3 * j + c] * a.rdpsi[2 * e + 1]; }
+  }
+  const double theta = fold_angle(F12, a.tangent[2 * g], a.tangent[2 * g + 1], nullptr);
+  const double th0 = a.theta0_gp ? a.theta0_gp[g] : a.theta0;
+  const double d = theta - th0;
+  atomicAdd(out, a.weight[g] * (0.5 * a.Kt * (d * d)));
+}
+
+inline unsigned nb(int64_t n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
+
+int sm_count(int device) {
+  static int cached = -1;
+  if (cached < 0) {
+    int v = 0;
+    CGB_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device));
+    cached = v;
+  }
+  return cached;
+}
+
+HingeArgs hinge_args(cgb_assembler* a, cgb_fold_dev& f, const double* d_x, int flags) {
+  HingeArgs h{};
+  h.n_gp = f.n_gp;
+  h.max_u = std::max(f.max_u, 1);
+  h.lptr = f.left->nbr_ptr.p; h.lidx = f.left->nbr_idx.p; h.ldpsi = f.left->dpsi.p;
+  h.rptr = f.right->nbr_ptr.p; h.ridx = f.right->nbr_idx.p; h.rdpsi = f.right->dpsi.p;
+  h.weight = f.weight.p; h.tangent = f.tangent.p;
+  h.Kt = f.Kt; h.theta0 = f.theta0;
+  h.theta0_gp = f.has_theta0_gp ? f.theta0_gp.p : nullptr;
+  h.active = f.has_active ? f.active.p : nullptr;
+  h.u_ptr = f.u_ptr.p; h.u_node = f.u_node.p; h.l_pos = f.l_pos.p; h.r_pos = f.r_pos.p;
+  h.pair_ptr = f.pair_ptr.p; h.pair_slot = f.pair_slot.p;
+  h.x = d_x;
+  h.exact = (flags & CGB_HINGE_EXACT) ? 1 : 0;
+  h.want_K = (flags & CGB_TANGENT) ? 1 : 0;
+  h.tk_float = (flags & CGB_MIXED) ? 1 : 0;
+  (void)a;
+  return h;
+}
+
+}  // namespace
+
+void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags) {
+  cgb_context* ctx = a->ctx;
+  cudaStream_t st = ctx->stream;
+  const cgb_shape* S = a->faces;
+  const bool want_K = (flags & CGB_TANGENT) != 0;
+  const bool mixed = (flags & CGB_MIXED) != 0;
+  const bool det = (flags & CGB_DETERMINISTIC) != 0;
+  const bool hinge = (flags & CGB_HINGE) != 0;
+  if (!a->have_material) throw Error(CGB_ERR_INVALID, "assemble: material not set (cgb_set_material)");
+  if (want_K && !d_K) throw Error(CGB_ERR_INVALID, "assemble: K output missing with CGB_TANGENT");
+  if (det) deterministic_prepare(a);
+
+  const int64_t ndof = 3 * static_cast<int64_t>(a->n_nodes);
+  // Accumulators.
+  if (!det) CGB_CUDA(cudaMemsetAsync(d_F, 0, ndof * sizeof(double), st));
+  if (want_K && !det) {
+    if (mixed) {
+      a->kacc32.ensure(12 * a->n_blocks);
+      CGB_CUDA(cudaMemsetAsync(a->kacc32.p, 0, 12 * a->n_blocks * sizeof(float), st));
+    } else {
+      a->kacc64.ensure(9 * a->n_blocks);
+      CGB_CUDA(cudaMemsetAsync(a->kacc64.p, 0, 9 * a->n_blocks * sizeof(double), st));
+    }
+  }
+  const int64_t n_contrib = a->n_pairs + [&] { int64_t s = 0; for (auto& f : a->folds) s += f.n_pairs; return s; }();
+  if (det) {
+    a->fcontrib.ensure(3 * std::max<int64_t>(a->n_fcontrib, 1));
+    if (want_K) {
+      if (mixed) a->contrib32.ensure(9 * std::max<int64_t>(n_contrib, 1));
+      else a->contrib64.ensure(9 * std::max<int64_t>(n_contrib, 1));
+    }
+    // Hinge entries of inactive crease points contribute zero.
+    if (a->n_fcontrib > S->nnz)
+      CGB_CUDA(cudaMemsetAsync(a->fcontrib.p + 3 * S->nnz, 0, 3 * (a->n_fcontrib - S->nnz) * sizeof(double), st));
+    if (want_K && n_contrib > a->n_pairs) {
+      if (mixed) CGB_CUDA(cudaMemsetAsync(a->contrib32.p + 9 * a->n_pairs, 0, 9 * (n_contrib - a->n_pairs) * sizeof(float), st));
+      else CGB_CUDA(cudaMemsetAsync(a->contrib64.p + 9 * a->n_pairs, 0, 9 * (n_contrib - a->n_pairs) * sizeof(double), st));
+    }
+  }
+
+  // Face kernel.
+  FaceArgs fa{};
+  fa.n_gp = S->n_gp;
+  fa.nmax = std::max(S->max_n, 1);
+  fa.ptr = S->nbr_ptr.p; fa.idx = S->nbr_idx.p; fa.dpsi = S->dpsi.p; fa.ddpsi = S->ddpsi.p;
+  fa.weight = a->weight.p; fa.x = d_x;
+  fa.map_ptr = a->map_ptr.p; fa.map_slot = a->map_slot.p;
+  std::memcpy(fa.mat.A, a->A, sizeof a->A); std::memcpy(fa.mat.B, a->B, sizeof a->B); std::memcpy(fa.mat.D, a->D, sizeof a->D);
+  fa.F = d_F;
+  fa.Fc = a->fcontrib.p;
+  fa.Kacc = mixed ? static_cast<void*>(a->kacc32.p) : static_cast<void*>(a->kacc64.p);
+  fa.Kc = mixed ? static_cast<void*>(a->contrib32.p) : static_cast<void*>(a->contrib64.p);
+  const size_t tk = mixed ? sizeof(float) : sizeof(double);
+  const size_t smem = want_K ? static_cast<size_t>(kFaceWarps) * fa.nmax * (kRec * tk + sizeof(int)) : 0;
+  if (smem > 200 * 1024)
+    throw Error(CGB_ERR_CAPACITY, "assemble: " + std::to_string(S->max_n) + " neighbours per Gauss point exceed the shared-memory staging");
+  const int sms = sm_count(ctx->device);
+  const unsigned grid = std::max(1u, std::min(nb(S->n_gp, kFaceWarps), static_cast<unsigned>(sms * 16)));
+  auto launch = [&](auto kern) {
+    if (smem > 48 * 1024) CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    if (S->n_gp) kern<<<grid, 32 * kFaceWarps, smem, st>>>(fa);
+  };
+  if (mixed) {
+    if (det) { if (want_K) launch(face_kernel<float, true, true>); else launch(face_kernel<float, true, false>); }
+    else { if (want_K) launch(face_kernel<float, false, true>); else launch(face_kernel<float, false, false>); }
+  } else {
+    if (det) { if (want_K) launch(face_kernel<double, true, true>); else launch(face_kernel<double, true, false>); }
+    else { if (want_K) launch(face_kernel<double, false, true>); else launch(face_kernel<double, false, false>); }
+  }
+  CGB_CUDA(cudaGetLastError());
+
+  // Hinge.
+  if (hinge) {
+    int64_t kb = a->hinge_pair_base, fb = a->hinge_f_base;
+    for (auto& f : a->folds) {
+      if (f.n_gp == 0) continue;
+      HingeArgs h = hinge_args(a, f, d_x, flags);
+      h.F = d_F;
+      h.Kacc = mixed ? static_cast<void*>(a->kacc32.p) : static_cast<void*>(a->kacc64.p);
+      if (det) {
+        h.Fc = a->fcontrib.p;
+        h.Kc = mixed ? static_cast<void*>(a->contrib32.p) : static_cast<void*>(a->contrib64.p);
+        h.f_base = fb; h.k_base = kb;
+      }
+      const size_t hs = static_cast<size_t>(kHingeWarps) * (7 * h.max_u + 144 + 16) * sizeof(double);
+      if (hs > 48 * 1024) CGB_CUDA(cudaFuncSetAttribute(hinge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(hs)));
+      hinge_kernel<<<nb(f.n_gp, kHingeWarps), 32 * kHingeWarps, hs, st>>>(h);
+      CGB_CUDA(cudaGetLastError());
+      kb += f.n_pairs;
+      fb += f.n_u;
+    }
+  }
+
+  // Reductions / output.
+  const unsigned cg = std::max(1u, std::min(nb(a->n_nodes, 4), static_cast<unsigned>(sms * 32)));
+  if (det) {
+    det_reduce_F<<<nb(a->n_nodes, 128), 128, 0, st>>>(a->n_nodes, a->node_list_ptr.p, a->node_list.p, a->fcontrib.p, d_F);
+    if (want_K) {
+      if (mixed) det_reduce_blocks<float><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->blk_list_ptr.p, a->blk_list.p, a->contrib32.p, d_K);
+      else det_reduce_blocks<double><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->blk_list_ptr.p, a->blk_list.p, a->contrib64.p, d_K);
+    }
+  } else if (want_K) {
+    if (mixed) blocks_to_csc<float, 12><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->kacc32.p, d_K);
+    else blocks_to_csc<double, 9><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->kacc64.p, d_K);
+  }
+  CGB_CUDA(cudaGetLastError());
+}
+
+void energies_device(cgb_assembler* a, const double* d_x, double* out3) {
+  cgb_context* ctx = a->ctx;
+  cudaStream_t st = ctx->stream;
+  a->energy.ensure(3);
+  CGB_CUDA(cudaMemsetAsync(a->energy.p, 0, 3 * sizeof(double), st));
+  Material m;
+  std::memcpy(m.A, a->A, sizeof m.A); std::memcpy(m.B, a->B, sizeof m.B); std::memcpy(m.D, a->D, sizeof m.D);
+  const cgb_shape* S = a->faces;
+  if (S->n_gp)
+    face_energy_kernel<<<std::max(1u, std::min(nb(S->n_gp, 4), 152u * 32u)), 128, 0, st>>>(
+        S->n_gp, S->nbr_ptr.p, S->nbr_idx.p, S->dpsi.p, S->ddpsi.p, a->weight.p, d_x, m, a->energy.p);
+  for (auto& f : a->folds) {
+    if (!f.n_gp) continue;
+    HingeArgs h = hinge_args(a, f, d_x, 0);
+    hinge_energy_kernel<<<nb(f.n_gp, 128), 128, 0, st>>>(h, a->energy.p + 2);
+  }
+  CGB_CUDA(cudaGetLastError());
+  CGB_CUDA(cudaMemcpyAsync(out3, a->energy.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CGB_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace cgb

@@ -1,0 +1,174 @@
+// cgb_internal.h — host-side internals shared by the CUDA translation units of the
+// GB300 Gauss-point library (context, shape sets, assembler, device buffers).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/curvami_gb300.h"
+
+namespace cgb {
+
+// A failure inside the library: carries the C-ABI status code and the message that
+// cgb_last_error() returns (the reference's exception text where one exists).
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+inline void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess)
+    throw Error(CGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CGB_CUDA(call) ::cgb::cuda_check((call), #call)
+
+// Owning device buffer (cudaMalloc'd, freed on destruction or reset).
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t count) { alloc(count); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) { reset(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevBuf() { reset(); }
+  void alloc(size_t count) {
+    reset();
+    if (count == 0) count = 1;  // keep a valid pointer for empty sets
+    CGB_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void ensure(size_t count) { if (n < count || !p) alloc(count); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+template <class T>
+void upload(DevBuf<T>& d, const T* h, size_t count, cudaStream_t s) {
+  d.alloc(count);
+  if (count) CGB_CUDA(cudaMemcpyAsync(d.p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+struct Crease {
+  std::vector<double> xy;
+  int extend_start = 0, extend_end = 0, is_closed = 0;
+};
+
+}  // namespace cgb
+
+// Opaque handles of the C ABI.
+struct cgb_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string last_error;
+  // Nodes (Meshless::nodes X_ref), interleaved x y.
+  int n_nodes = 0;
+  std::vector<double> h_node_xy;
+  cgb::DevBuf<double> node_xy;
+  // Device-side error word written by kernels (bounds checks, capacity).
+  cgb::DevBuf<int> dev_err;
+  int* h_err = nullptr;  // pinned mirror
+};
+
+struct cgb_shape {
+  cgb_context* ctx = nullptr;
+  int n_gp = 0;
+  int64_t nnz = 0;
+  int max_n = 0;  // largest neighbour count of the set
+  cgb::DevBuf<double> gp_xy;      // 2 per point
+  cgb::DevBuf<int64_t> nbr_ptr;   // n_gp + 1
+  cgb::DevBuf<int32_t> nbr_idx;   // nnz
+  cgb::DevBuf<double> s;          // nnz (normalised distance), may be empty
+  cgb::DevBuf<double> psi;        // nnz
+  cgb::DevBuf<double> dpsi;       // 2 * nnz (x, y)
+  cgb::DevBuf<double> ddpsi;      // 3 * nnz (xx, yy, xy)
+};
+
+// Per-fold data kept by the assembler (plate/PlateData.h: Fold; Constraints.h:341).
+struct cgb_fold_dev {
+  int n_gp = 0;
+  double Kt = 0.0, theta0 = 0.0;
+  const cgb_shape* left = nullptr;
+  const cgb_shape* right = nullptr;
+  cgb::DevBuf<double> weight, tangent, theta0_gp;
+  cgb::DevBuf<int8_t> active;
+  bool has_theta0_gp = false, has_active = false;
+  // Merged node list of left U right per crease point (sorted unique nodes),
+  // and for every left/right entry its position in that list.
+  cgb::DevBuf<int64_t> u_ptr;       // n_gp + 1
+  cgb::DevBuf<int32_t> u_node;      // merged nodes
+  cgb::DevBuf<int32_t> l_pos, r_pos;
+  cgb::DevBuf<int64_t> pair_ptr;    // n_gp + 1, pairs P <= Q over the merged list
+  cgb::DevBuf<int32_t> pair_slot;   // block slot of each pair in the union pattern
+  int max_u = 0;
+  int64_t n_u = 0;      // merged-node entries over all crease points (u_ptr[n_gp])
+  int64_t n_pairs = 0;
+};
+
+struct cgb_assembler {
+  cgb_context* ctx = nullptr;
+  const cgb_shape* faces = nullptr;
+  int n_nodes = 0;
+  int64_t n_blocks = 0;  // 3x3 blocks of the union pattern; nnz = 9 * n_blocks
+  cgb::DevBuf<double> weight;       // face Gauss-point weights
+  // Union pattern (face blocks U hinge blocks), block-column CSC:
+  cgb::DevBuf<int64_t> col_ptr;     // n_nodes + 1 (block offsets)
+  cgb::DevBuf<int32_t> col_nodes;   // n_blocks (block rows, ascending per column)
+  cgb::DevBuf<int32_t> outer;       // 3 n_nodes + 1 (scalar CSC, the reference's K layout)
+  // Face Gauss point -> block slot of each local pair (i <= j) in loop order.
+  cgb::DevBuf<int64_t> map_ptr;     // n_gp + 1
+  cgb::DevBuf<int32_t> map_slot;    // total pairs
+  int64_t n_pairs = 0;
+  std::vector<cgb_fold_dev> folds;
+  double A[9] = {0}, B[9] = {0}, D[9] = {0};
+  bool have_material = false;
+  // Accumulators.
+  cgb::DevBuf<double> kacc64;       // 9 * n_blocks
+  cgb::DevBuf<float> kacc32;        // 12 * n_blocks (padded for 16-byte vector atomics)
+  cgb::DevBuf<double> F;            // 3 n_nodes (device scratch for host-buffer calls)
+  cgb::DevBuf<double> K;            // 9 n_blocks (device scratch for host-buffer calls)
+  cgb::DevBuf<double> x;            // 3 n_nodes
+  // Deterministic scatter: per pair contributions and per-block ordered lists.
+  bool det_ready = false;
+  cgb::DevBuf<int64_t> blk_list_ptr;  // n_blocks + 1
+  cgb::DevBuf<int64_t> blk_list;      // global contribution ids, ascending
+  cgb::DevBuf<int64_t> node_list_ptr; // n_nodes + 1
+  cgb::DevBuf<int64_t> node_list;     // F contribution ids, ascending
+  cgb::DevBuf<double> contrib64;      // 9 per contribution
+  cgb::DevBuf<float> contrib32;
+  cgb::DevBuf<double> fcontrib;       // 3 per F contribution
+  int64_t n_fcontrib = 0;
+  int64_t hinge_pair_base = 0;        // first contribution id of hinge pairs
+  int64_t hinge_f_base = 0;
+  // Energies.
+  cgb::DevBuf<double> energy;       // 3
+  // Pinned staging for the host-buffer entry point.
+  double* h_stage = nullptr;
+  size_t h_stage_bytes = 0;
+};
+
+namespace cgb {
+// shape.cu
+void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shape_params& prm,
+                 const std::vector<Crease>& creases, cgb_shape* out);
+// pattern.cu
+void pattern_build(cgb_assembler* a);
+void deterministic_prepare(cgb_assembler* a);
+// assemble.cu
+void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags);
+void energies_device(cgb_assembler* a, const double* d_x, double* out3);
+}  // namespace cgb

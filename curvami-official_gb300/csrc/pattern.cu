@@ -1,0 +1,421 @@
+// pattern.cu — symbolic phase on sm_103a: the block-upper sparsity pattern of K, the
+// Gauss-point -> block-slot map, and the ordered contribution lists of the
+// deterministic scatter.
+//
+// Reference: NonLinearAssembler::initSparsityPattern (plate/Assembly.h:59-153) and the
+// pattern growth of K += K_fold (plate/Meshless.h:113-127, Constraints.h:420-433).
+//
+// Column j of the block pattern is the sorted set of nodes i <= j that share a
+// neighbour list with j. "Neighbour lists" are the face Gauss points' lists plus, for
+// the hinge, each crease point's merged left/right node list (the hinge couples every
+// node pair of that merged list). One warp builds one column: it walks the lists that
+// contain j (node -> list inverse index), inserts every i <= j into a shared-memory hash
+// set, then sorts the set by ranks. The result is the same sorted unique set the
+// reference builds with sort + unique, so the pattern is bit-exact.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <string>
+
+#include "cgb_device.cuh"
+#include "cgb_internal.h"
+
+namespace cgb {
+namespace {
+
+constexpr int kWarps = 2;
+constexpr int kCap = 2048;        // hash slots per warp (8 KB)
+constexpr int kMaxColumn = 1536;  // largest column the hash set accepts (75 % load)
+
+enum : int { kErrCapacity = CGB_ERR_CAPACITY, kErrMapping = CGB_ERR_MAPPING };
+
+// A set of lists in CSR form (face Gauss points, then crease points).
+struct Lists {
+  int n;
+  const int64_t* ptr;
+  const int32_t* idx;
+};
+
+__global__ void count_per_node(int64_t n, const int32_t* __restrict__ idx, int32_t* __restrict__ cnt) {
+  const int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (e < n) atomicAdd(&cnt[idx[e]], 1);
+}
+
+// inv[cursor[node]++] = list id (+ base), one thread per list.
+__global__ void fill_inverse(Lists L, int base, int64_t* __restrict__ cursor, int32_t* __restrict__ inv) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= L.n) return;
+  for (int64_t e = L.ptr[g]; e < L.ptr[g + 1]; ++e) {
+    const int64_t at = atomicAdd(reinterpret_cast<unsigned long long*>(&cursor[L.idx[e]]), 1ULL);
+    inv[at] = base + g;
+  }
+}
+
+__device__ __forceinline__ unsigned hash32(unsigned x) {
+  x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+  return x;
+}
+
+// Column sets. Phase 0 counts, phase 1 writes the sorted column into col_nodes.
+__global__ void __launch_bounds__(32 * kWarps) column_kernel(int n_nodes, Lists A, Lists B,
+                                                              const int64_t* __restrict__ inv_ptr,
+                                                              const int32_t* __restrict__ inv,
+                                                              int phase, int32_t* __restrict__ col_len,
+                                                              const int64_t* __restrict__ col_ptr,
+                                                              int32_t* __restrict__ col_nodes, int* err) {
+  __shared__ int table[kWarps][kCap];
+  __shared__ int keys[kWarps][kMaxColumn];
+  __shared__ int count[kWarps];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int* T = table[w];
+  for (int j = blockIdx.x * kWarps + w; j < n_nodes; j += gridDim.x * kWarps) {
+    for (int s = lane; s < kCap; s += 32) T[s] = -1;
+    if (lane == 0) count[w] = 0;
+    __syncwarp();
+    bool overflow = false;
+    for (int64_t q = inv_ptr[j]; q < inv_ptr[j + 1]; ++q) {
+      const int lid = inv[q];
+      const Lists& L = lid < A.n ? A : B;
+      const int li = lid < A.n ? lid : lid - A.n;
+      const int64_t e0 = L.ptr[li], e1 = L.ptr[li + 1];
+      for (int64_t e = e0 + lane; e < e1; e += 32) {
+        const int i = L.idx[e];
+        if (i > j) continue;
+        unsigned h = hash32(static_cast<unsigned>(i)) & (kCap - 1);
+        for (int probe = 0; probe < kCap; ++probe) {
+          const int prev = atomicCAS(&T[h], -1, i);
+          if (prev == -1) {
+            const int at = atomicAdd(&count[w], 1);
+            if (at < kMaxColumn) keys[w][at] = i; else overflow = true;
+            break;
+          }
+          if (prev == i) break;
+          h = (h + 1) & (kCap - 1);
+        }
+      }
+    }
+    __syncwarp();
+    const int m = count[w];
+    if (__any_sync(0xffffffffu, overflow) || m > kMaxColumn) {
+      if (lane == 0) dev_fail(err, kErrCapacity);
+      continue;
+    }
+    if (phase == 0) {
+      if (lane == 0) col_len[j] = m;
+    } else {
+      const int64_t base = col_ptr[j];
+      for (int a = lane; a < m; a += 32) {
+        const int v = keys[w][a];
+        int rank = 0;
+        for (int b = 0; b < m; ++b) rank += (keys[w][b] < v);
+        col_nodes[base + rank] = v;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Face Gauss point -> block slot of each local pair (i <= j), in the reference's loop
+// order (plate/Assembly.h:128-143). One warp per Gauss point.
+__global__ void slot_map_kernel(int n_gp, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                const int64_t* __restrict__ map_ptr, const int64_t* __restrict__ col_ptr,
+                                const int32_t* __restrict__ col_nodes, int32_t* __restrict__ slot, int* err) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t g = warp; g < n_gp; g += nwarps) {
+    const int64_t p0 = ptr[g];
+    const int n = static_cast<int>(ptr[g + 1] - p0);
+    const int64_t np = static_cast<int64_t>(n) * (n + 1) / 2;
+    const int64_t m0 = map_ptr[g];
+    // pair p -> (i, j): walk rows of length n - i.
+    int i = 0, off = lane;
+    while (i < n && off >= n - i) { off -= n - i; ++i; }
+    for (int64_t p = lane; p < np; p += 32) {
+      const int j = i + off;
+      const int ni = idx[p0 + i], nj = idx[p0 + j];
+      const int lo = ni < nj ? ni : nj, hi = ni < nj ? nj : ni;
+      int64_t a = col_ptr[hi], b = col_ptr[hi + 1];
+      while (a < b) {
+        const int64_t mid = (a + b) >> 1;
+        if (col_nodes[mid] < lo) a = mid + 1; else b = mid;
+      }
+      int32_t s = -1;
+      if (a < col_ptr[hi + 1] && col_nodes[a] == lo) s = static_cast<int32_t>(a);
+      else dev_fail(err, kErrMapping);
+      slot[m0 + p] = s;
+      off += 32;
+      while (i < n && off >= n - i) { off -= n - i; ++i; }
+    }
+  }
+}
+
+// CSR fill of the deterministic lists: one thread per contribution id.
+__global__ void count_slots(int64_t n, const int32_t* __restrict__ key, int64_t* __restrict__ cnt) {
+  const int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (q < n) atomicAdd(reinterpret_cast<unsigned long long*>(&cnt[key[q]]), 1ULL);
+}
+__global__ void fill_slots(int64_t n, int64_t base, const int32_t* __restrict__ key, int64_t* __restrict__ cursor,
+                           int64_t* __restrict__ list) {
+  const int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (q < n) {
+    const int64_t at = atomicAdd(reinterpret_cast<unsigned long long*>(&cursor[key[q]]), 1ULL);
+    list[at] = base + q;
+  }
+}
+// Sort each list ascending (insertion sort: lists are short and this runs once).
+__global__ void sort_lists(int64_t n, const int64_t* __restrict__ lptr, int64_t* __restrict__ list) {
+  const int64_t b = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (b >= n) return;
+  const int64_t s = lptr[b], e = lptr[b + 1];
+  for (int64_t k = s + 1; k < e; ++k) {
+    const int64_t v = list[k];
+    int64_t m = k - 1;
+    while (m >= s && list[m] > v) { list[m + 1] = list[m]; --m; }
+    list[m + 1] = v;
+  }
+}
+
+inline unsigned nb(int64_t n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
+
+int read_err(cgb_context* ctx) {
+  int e = 0;
+  CGB_CUDA(cudaMemcpyAsync(&e, ctx->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CGB_CUDA(cudaStreamSynchronize(ctx->stream));
+  return e;
+}
+
+}  // namespace
+
+void pattern_build(cgb_assembler* a) {
+  cgb_context* ctx = a->ctx;
+  cudaStream_t st = ctx->stream;
+  const cgb_shape* F = a->faces;
+  const int n_nodes = a->n_nodes;
+  CGB_CUDA(cudaMemsetAsync(ctx->dev_err.p, 0, sizeof(int), st));
+
+  // ---- hinge lists: merged sorted node lists of every crease point (host) ----
+  std::vector<int64_t> hptr(1, 0);
+  std::vector<int32_t> hidx;
+  for (auto& f : a->folds) {
+    std::vector<int64_t> lp(f.n_gp + 1), rp(f.n_gp + 1);
+    CGB_CUDA(cudaMemcpyAsync(lp.data(), f.left->nbr_ptr.p, lp.size() * 8, cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaMemcpyAsync(rp.data(), f.right->nbr_ptr.p, rp.size() * 8, cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+    std::vector<int32_t> li(std::max<int64_t>(lp.back(), 1)), ri(std::max<int64_t>(rp.back(), 1));
+    if (lp.back()) CGB_CUDA(cudaMemcpyAsync(li.data(), f.left->nbr_idx.p, lp.back() * 4, cudaMemcpyDeviceToHost, st));
+    if (rp.back()) CGB_CUDA(cudaMemcpyAsync(ri.data(), f.right->nbr_idx.p, rp.back() * 4, cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+    std::vector<int64_t> uptr(f.n_gp + 1, 0);
+    std::vector<int32_t> unode, lpos(std::max<int64_t>(lp.back(), 1)), rpos(std::max<int64_t>(rp.back(), 1));
+    std::vector<int32_t> tmp;
+    f.max_u = 0;
+    for (int g = 0; g < f.n_gp; ++g) {
+      tmp.clear();
+      for (int64_t e = lp[g]; e < lp[g + 1]; ++e) tmp.push_back(li[e]);
+      for (int64_t e = rp[g]; e < rp[g + 1]; ++e) tmp.push_back(ri[e]);
+      std::sort(tmp.begin(), tmp.end());
+      tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+      for (int64_t e = lp[g]; e < lp[g + 1]; ++e)
+        lpos[e] = static_cast<int32_t>(std::lower_bound(tmp.begin(), tmp.end(), li[e]) - tmp.begin());
+      for (int64_t e = rp[g]; e < rp[g + 1]; ++e)
+        rpos[e] = static_cast<int32_t>(std::lower_bound(tmp.begin(), tmp.end(), ri[e]) - tmp.begin());
+      unode.insert(unode.end(), tmp.begin(), tmp.end());
+      uptr[g + 1] = uptr[g] + static_cast<int64_t>(tmp.size());
+      f.max_u = std::max<int>(f.max_u, static_cast<int>(tmp.size()));
+      hidx.insert(hidx.end(), tmp.begin(), tmp.end());
+      hptr.push_back(hptr.back() + static_cast<int64_t>(tmp.size()));
+    }
+    f.n_u = uptr[f.n_gp];
+    upload(f.u_ptr, uptr.data(), uptr.size(), st);
+    upload(f.u_node, unode.data(), unode.size(), st);
+    upload(f.l_pos, lpos.data(), lpos.size(), st);
+    upload(f.r_pos, rpos.data(), rpos.size(), st);
+    CGB_CUDA(cudaStreamSynchronize(st));
+  }
+  const int n_hl = static_cast<int>(hptr.size() - 1);
+  DevBuf<int64_t> d_hptr;
+  DevBuf<int32_t> d_hidx;
+  upload(d_hptr, hptr.data(), hptr.size(), st);
+  upload(d_hidx, hidx.data(), std::max<size_t>(hidx.size(), 1), st);
+
+  // ---- node -> list inverse index ----
+  DevBuf<int32_t> cnt(n_nodes);
+  CGB_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes(), st));
+  if (F->nnz) count_per_node<<<nb(F->nnz, 256), 256, 0, st>>>(F->nnz, F->nbr_idx.p, cnt.p);
+  if (!hidx.empty()) count_per_node<<<nb(hidx.size(), 256), 256, 0, st>>>(hidx.size(), d_hidx.p, cnt.p);
+  CGB_CUDA(cudaGetLastError());
+  std::vector<int32_t> hc(n_nodes);
+  CGB_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, cnt.bytes(), cudaMemcpyDeviceToHost, st));
+  CGB_CUDA(cudaStreamSynchronize(st));
+  std::vector<int64_t> inv_ptr(n_nodes + 1, 0);
+  for (int j = 0; j < n_nodes; ++j) inv_ptr[j + 1] = inv_ptr[j] + hc[j];
+  DevBuf<int64_t> d_inv_ptr, cursor;
+  upload(d_inv_ptr, inv_ptr.data(), inv_ptr.size(), st);
+  upload(cursor, inv_ptr.data(), n_nodes, st);
+  DevBuf<int32_t> inv(inv_ptr.back());
+  Lists LA{F->n_gp, F->nbr_ptr.p, F->nbr_idx.p};
+  Lists LB{n_hl, d_hptr.p, d_hidx.p};
+  if (LA.n) fill_inverse<<<nb(LA.n, 128), 128, 0, st>>>(LA, 0, cursor.p, inv.p);
+  if (LB.n) fill_inverse<<<nb(LB.n, 128), 128, 0, st>>>(LB, LA.n, cursor.p, inv.p);
+  CGB_CUDA(cudaGetLastError());
+
+  // ---- columns: count, scan, fill ----
+  DevBuf<int32_t> col_len(n_nodes);
+  const unsigned cgrid = std::max(1u, std::min(nb(n_nodes, kWarps), 152u * 16u));
+  column_kernel<<<cgrid, 32 * kWarps, 0, st>>>(n_nodes, LA, LB, d_inv_ptr.p, inv.p, 0, col_len.p, nullptr,
+                                              nullptr, ctx->dev_err.p);
+  CGB_CUDA(cudaGetLastError());
+  if (int e = read_err(ctx))
+    throw Error(e, "initSparsityPattern: a column of the node pattern has more than 1536 block rows");
+  std::vector<int32_t> hl(n_nodes);
+  CGB_CUDA(cudaMemcpyAsync(hl.data(), col_len.p, col_len.bytes(), cudaMemcpyDeviceToHost, st));
+  CGB_CUDA(cudaStreamSynchronize(st));
+  std::vector<int64_t> cptr(n_nodes + 1, 0);
+  for (int j = 0; j < n_nodes; ++j) cptr[j + 1] = cptr[j] + hl[j];
+  a->n_blocks = cptr[n_nodes];
+  if (9 * a->n_blocks >= (1LL << 31))
+    throw Error(CGB_ERR_CAPACITY, "initSparsityPattern: nnz(K) exceeds the int32 index range of the reference's K");
+  upload(a->col_ptr, cptr.data(), cptr.size(), st);
+  a->col_nodes.alloc(a->n_blocks);
+  column_kernel<<<cgrid, 32 * kWarps, 0, st>>>(n_nodes, LA, LB, d_inv_ptr.p, inv.p, 1, col_len.p, a->col_ptr.p,
+                                              a->col_nodes.p, ctx->dev_err.p);
+  CGB_CUDA(cudaGetLastError());
+  // Scalar CSC outer index (Assembly.h:103-107): column 3j+c starts at
+  // 9 col_ptr[j] + 3 c len_j.
+  std::vector<int32_t> outer(3 * static_cast<size_t>(n_nodes) + 1);
+  for (int j = 0; j < n_nodes; ++j)
+    for (int c = 0; c < 3; ++c) outer[3 * j + c] = static_cast<int32_t>(9 * cptr[j] + 3 * c * hl[j]);
+  outer[3 * n_nodes] = static_cast<int32_t>(9 * cptr[n_nodes]);
+  upload(a->outer, outer.data(), outer.size(), st);
+
+  // ---- face slot map ----
+  std::vector<int64_t> fptr(F->n_gp + 1);
+  CGB_CUDA(cudaMemcpyAsync(fptr.data(), F->nbr_ptr.p, fptr.size() * 8, cudaMemcpyDeviceToHost, st));
+  CGB_CUDA(cudaStreamSynchronize(st));
+  std::vector<int64_t> mptr(F->n_gp + 1, 0);
+  for (int g = 0; g < F->n_gp; ++g) {
+    const int64_t n = fptr[g + 1] - fptr[g];
+    mptr[g + 1] = mptr[g] + n * (n + 1) / 2;
+  }
+  a->n_pairs = mptr[F->n_gp];
+  upload(a->map_ptr, mptr.data(), mptr.size(), st);
+  a->map_slot.alloc(a->n_pairs);
+  if (F->n_gp)
+    slot_map_kernel<<<std::min<int64_t>(nb(F->n_gp, 8), 152 * 64), 256, 0, st>>>(
+        F->n_gp, F->nbr_ptr.p, F->nbr_idx.p, a->map_ptr.p, a->col_ptr.p, a->col_nodes.p, a->map_slot.p,
+        ctx->dev_err.p);
+  CGB_CUDA(cudaGetLastError());
+  if (int e = read_err(ctx)) {
+    if (e == CGB_ERR_MAPPING)
+      throw Error(e, "Assembly: Gauss-point neighbour missing from the sparsity pattern; "
+                     "CSR mapping is inconsistent.");
+    throw Error(e, "initSparsityPattern: device check failed");
+  }
+
+  // ---- hinge pair slots (host: crease points are few) ----
+  if (!a->folds.empty()) {
+    std::vector<int32_t> hcn(a->n_blocks);
+    CGB_CUDA(cudaMemcpyAsync(hcn.data(), a->col_nodes.p, hcn.size() * 4, cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+    int64_t hoff = 0;
+    for (auto& f : a->folds) {
+      std::vector<int64_t> pp(f.n_gp + 1, 0);
+      std::vector<int32_t> ps;
+      for (int g = 0; g < f.n_gp; ++g) {
+        const int64_t u0 = hptr[hoff + g], u1 = hptr[hoff + g + 1];
+        for (int64_t P = u0; P < u1; ++P)
+          for (int64_t Q = P; Q < u1; ++Q) {
+            const int lo = hidx[P], hi = hidx[Q];
+            auto b0 = hcn.begin() + cptr[hi], b1 = hcn.begin() + cptr[hi + 1];
+            auto it = std::lower_bound(b0, b1, lo);
+            if (it == b1 || *it != lo)
+              throw Error(CGB_ERR_MAPPING, "Assembly: hinge block missing from the sparsity pattern");
+            ps.push_back(static_cast<int32_t>(it - hcn.begin()));
+          }
+        pp[g + 1] = static_cast<int64_t>(ps.size());
+      }
+      hoff += f.n_gp;
+      f.n_pairs = static_cast<int64_t>(ps.size());
+      upload(f.pair_ptr, pp.data(), pp.size(), st);
+      upload(f.pair_slot, ps.data(), std::max<size_t>(ps.size(), 1), st);
+      CGB_CUDA(cudaStreamSynchronize(st));
+    }
+  }
+  CGB_CUDA(cudaStreamSynchronize(st));
+}
+
+// Ordered lists for the deterministic scatter. Contribution ids: face pairs
+// [0, n_pairs), then hinge pairs fold by fold. F contribution ids: face entries
+// [0, nnz_face), then hinge merged-node entries fold by fold. Each K block and each
+// node sums its contributions in ascending id order, i.e. Gauss point by Gauss point
+// in the reference's loop order.
+void deterministic_prepare(cgb_assembler* a) {
+  if (a->det_ready) return;
+  cgb_context* ctx = a->ctx;
+  cudaStream_t st = ctx->stream;
+  int64_t n_hp = 0, n_hf = 0;
+  std::vector<int64_t> fnum;  // merged-node entries per fold
+  for (auto& f : a->folds) {
+    n_hp += f.n_pairs;
+    fnum.push_back(f.n_u);
+    n_hf += f.n_u;
+  }
+  const int64_t nq = a->n_pairs + n_hp;
+  a->hinge_pair_base = a->n_pairs;
+  a->hinge_f_base = a->faces->nnz;
+  a->n_fcontrib = a->faces->nnz + n_hf;
+
+  // K lists.
+  DevBuf<int64_t> cnt(a->n_blocks + 1);
+  CGB_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes(), st));
+  if (a->n_pairs) count_slots<<<nb(a->n_pairs, 256), 256, 0, st>>>(a->n_pairs, a->map_slot.p, cnt.p);
+  for (auto& f : a->folds)
+    if (f.n_pairs) count_slots<<<nb(f.n_pairs, 256), 256, 0, st>>>(f.n_pairs, f.pair_slot.p, cnt.p);
+  std::vector<int64_t> hc(a->n_blocks);
+  CGB_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, hc.size() * 8, cudaMemcpyDeviceToHost, st));
+  CGB_CUDA(cudaStreamSynchronize(st));
+  std::vector<int64_t> lp(a->n_blocks + 1, 0);
+  for (int64_t b = 0; b < a->n_blocks; ++b) lp[b + 1] = lp[b] + hc[b];
+  upload(a->blk_list_ptr, lp.data(), lp.size(), st);
+  DevBuf<int64_t> cur;
+  upload(cur, lp.data(), a->n_blocks, st);
+  a->blk_list.alloc(nq);
+  if (a->n_pairs) fill_slots<<<nb(a->n_pairs, 256), 256, 0, st>>>(a->n_pairs, 0, a->map_slot.p, cur.p, a->blk_list.p);
+  int64_t base = a->n_pairs;
+  for (auto& f : a->folds) {
+    if (f.n_pairs) fill_slots<<<nb(f.n_pairs, 256), 256, 0, st>>>(f.n_pairs, base, f.pair_slot.p, cur.p, a->blk_list.p);
+    base += f.n_pairs;
+  }
+  sort_lists<<<nb(a->n_blocks, 128), 128, 0, st>>>(a->n_blocks, a->blk_list_ptr.p, a->blk_list.p);
+  CGB_CUDA(cudaGetLastError());
+
+  // F lists (node of each contribution: face entries then hinge merged nodes).
+  DevBuf<int64_t> fc(a->n_nodes + 1);
+  CGB_CUDA(cudaMemsetAsync(fc.p, 0, fc.bytes(), st));
+  if (a->faces->nnz) count_slots<<<nb(a->faces->nnz, 256), 256, 0, st>>>(a->faces->nnz, a->faces->nbr_idx.p, fc.p);
+  for (size_t k = 0; k < a->folds.size(); ++k)
+    if (fnum[k]) count_slots<<<nb(fnum[k], 256), 256, 0, st>>>(fnum[k], a->folds[k].u_node.p, fc.p);
+  std::vector<int64_t> hf(a->n_nodes);
+  CGB_CUDA(cudaMemcpyAsync(hf.data(), fc.p, hf.size() * 8, cudaMemcpyDeviceToHost, st));
+  CGB_CUDA(cudaStreamSynchronize(st));
+  std::vector<int64_t> np(a->n_nodes + 1, 0);
+  for (int j = 0; j < a->n_nodes; ++j) np[j + 1] = np[j] + hf[j];
+  upload(a->node_list_ptr, np.data(), np.size(), st);
+  DevBuf<int64_t> fcur;
+  upload(fcur, np.data(), a->n_nodes, st);
+  a->node_list.alloc(a->n_fcontrib);
+  if (a->faces->nnz)
+    fill_slots<<<nb(a->faces->nnz, 256), 256, 0, st>>>(a->faces->nnz, 0, a->faces->nbr_idx.p, fcur.p, a->node_list.p);
+  base = a->faces->nnz;
+  for (size_t k = 0; k < a->folds.size(); ++k) {
+    if (fnum[k]) fill_slots<<<nb(fnum[k], 256), 256, 0, st>>>(fnum[k], base, a->folds[k].u_node.p, fcur.p, a->node_list.p);
+    base += fnum[k];
+  }
+  sort_lists<<<nb(a->n_nodes, 128), 128, 0, st>>>(a->n_nodes, a->node_list_ptr.p, a->node_list.p);
+  CGB_CUDA(cudaGetLastError());
+  CGB_CUDA(cudaStreamSynchronize(st));
+  a->det_ready = true;
+}
+
+}  // namespace cgb

@@ -1,0 +1,657 @@
+// shape.cu — stage A on sm_103a: neighbour gather (GlobalFRNN) and RKPM shape
+// functions with crease visibility (GlobalRKPM), FP64.
+//
+// Reference: core/include/curvami/FRNN.h:23-78, core/include/curvami/Enrichment.h:23-92,
+// core/include/curvami/GlobalRKPM.h:15-397.
+//
+// Design: the node cell grid is a dense array over the reference's flattened cell key
+// (y * cols + x, so keys that wrap across a row resolve to the same cells as the
+// reference's hash map). One thread per Gauss point gathers its neighbours in the
+// reference's order (dx outer, dy inner, node index ascending in a cell) with an FP64
+// distance test written without FMA contraction, so the neighbour sets and their order
+// are bit-exact. The RKPM solve is FP64-pipe bound on GB300 (the FP64 rate is 1/62 of
+// the FP32 rate), so it also runs one Gauss point per thread: two passes over the
+// neighbours (moments, then shape functions) recompute the per-neighbour jets instead
+// of storing them, and per-node crease sides are hoisted into a per-node array.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+
+#include "cgb_device.cuh"
+#include "cgb_internal.h"
+
+namespace cgb {
+namespace {
+
+constexpr int kThreads = 128;
+
+struct GridDev {
+  double minx, miny, cell;
+  int cols;
+  long long ncells;
+  const int32_t* cell_start;  // ncells + 1
+  const int32_t* cell_nodes;
+};
+
+// Thread per Gauss point: count (out_idx == nullptr) or fill the neighbour list.
+__global__ void frnn_kernel(int n_gp, const double* __restrict__ gp_xy,
+                            const double* __restrict__ node_xy, const double* __restrict__ rho_node,
+                            double rho, double rho2, GridDev G, const int64_t* __restrict__ ptr,
+                            int32_t* __restrict__ count, int32_t* __restrict__ out_idx,
+                            double* __restrict__ out_s) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_gp) return;
+  const double gx = gp_xy[2 * g], gy = gp_xy[2 * g + 1];
+  const int qx = static_cast<int>(floor(__ddiv_rn(__dsub_rn(gx, G.minx), G.cell)));
+  const int qy = static_cast<int>(floor(__ddiv_rn(__dsub_rn(gy, G.miny), G.cell)));
+  int64_t pos = out_idx ? ptr[g] : 0;
+  int cnt = 0;
+  for (int dx = -1; dx <= 1; ++dx) {
+    for (int dy = -1; dy <= 1; ++dy) {
+      const long long key = static_cast<long long>(qy + dy) * G.cols + (qx + dx);
+      if (key < 0 || key >= G.ncells) continue;
+      const int k0 = G.cell_start[key], k1 = G.cell_start[key + 1];
+      for (int k = k0; k < k1; ++k) {
+        const int j = G.cell_nodes[k];
+        const double ddx = __dsub_rn(node_xy[2 * j], gx);
+        const double ddy = __dsub_rn(node_xy[2 * j + 1], gy);
+        const double dist2 = __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy));
+        double r = rho, r2 = rho2;
+        if (rho_node) { r = rho_node[j]; r2 = __dmul_rn(r, r); }
+        if (dist2 <= r2) {
+          if (out_idx) {
+            out_idx[pos] = j;
+            out_s[pos] = __ddiv_rn(__dsqrt_rn(dist2), r);
+            ++pos;
+          }
+          ++cnt;
+        }
+      }
+    }
+  }
+  if (!out_idx) count[g] = cnt;
+}
+
+// Per-node crease side sn = (f >= 0 ? +1 : -1) (GlobalRKPM.h:92-93).
+__global__ void node_side_kernel(int n_nodes, const double* __restrict__ node_xy, DevCrease cr,
+                                 int8_t* __restrict__ side) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_nodes) return;
+  const DevIndicator I = eval_indicator(node_xy[2 * j], node_xy[2 * j + 1], cr);
+  side[j] = (I.f >= 0.0) ? 1 : -1;
+}
+
+// Gauss-point indicators, 6 doubles per point per crease.
+__global__ void gp_indicator_kernel(int n_gp, const double* __restrict__ gp_xy, DevCrease cr,
+                                    double* __restrict__ out) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_gp) return;
+  const DevIndicator I = eval_indicator(gp_xy[2 * g], gp_xy[2 * g + 1], cr);
+  double* o = out + 6 * static_cast<int64_t>(g);
+  o[0] = I.f; o[1] = I.gx; o[2] = I.gy; o[3] = I.hxx; o[4] = I.hyy; o[5] = I.hxy;
+}
+
+__device__ __forceinline__ void window(int kernel, double s, double& w, double& dw, double& d2w) {
+  if (kernel == 0) {  // quartic spline, GlobalRKPM.h:15-17
+    if (s >= 1.0) { w = 0.0; } else { const double s2 = s * s; w = 1.0 - 6.0 * s2 + 8.0 * s2 * s - 3.0 * s2 * s2; }
+    dw = (s >= 1.0 || s < 1e-14) ? 0.0 : -12.0 * s + 24.0 * s * s - 12.0 * s * s * s;
+    d2w = (s >= 1.0) ? 0.0 : -12.0 + 48.0 * s - 36.0 * s * s;
+  } else {  // cubic B-spline (extension), same cut-offs
+    if (s >= 1.0) { w = 0.0; dw = 0.0; d2w = 0.0; return; }
+    if (s <= 0.5) {
+      w = 2.0 / 3.0 - 4.0 * s * s + 4.0 * s * s * s;
+      dw = (s < 1e-14) ? 0.0 : -8.0 * s + 12.0 * s * s;
+      d2w = -8.0 + 24.0 * s;
+    } else {
+      const double r = 1.0 - s;
+      w = 4.0 / 3.0 * r * r * r;
+      dw = -4.0 * r * r;
+      d2w = 8.0 * r;
+    }
+  }
+}
+
+struct Jets { double w, x, y, xx, yy, xy; };
+
+// Weight jets with crease visibility for one (Gauss point, neighbour) entry:
+// GlobalRKPM.h:59-84 (including the reference's d2x = xi^2/s^3, d2y = eta^2/s^3) and
+// the visibility product of GlobalRKPM.h:87-112.
+__device__ __forceinline__ Jets weight_jets(int kernel, double xi, double eta, double si, double fac,
+                                            int n_creases, const double* gind,
+                                            const int8_t* node_side, int n_nodes, int j,
+                                            double rho) {
+  const double zx = xi * fac, zy = eta * fac;
+  double wi, d, dd;
+  window(kernel, si, wi, d, dd);
+  const double dx = (si == 0.0) ? 0.0 : zx / si;
+  const double dy = (si == 0.0) ? 0.0 : zy / si;
+  Jets J;
+  J.w = wi;
+  J.x = d * dx;
+  J.y = d * dy;
+  const double si3 = si * si * si;
+  const double d2x = (si == 0.0) ? dd : (zx * zx) / si3;
+  const double d2y = (si == 0.0) ? dd : (zy * zy) / si3;
+  J.xx = dd * dx * dx + d * d2x;
+  J.yy = dd * dy * dy + d * d2y;
+  J.xy = (si == 0.0) ? 0.0 : dd * dx * dy + d * (-(zx * zy) / si3);
+  if (fac != 1.0) {
+    const double f2 = fac * fac;
+    J.x *= fac; J.y *= fac; J.xx *= f2; J.yy *= f2; J.xy *= f2;
+  }
+  for (int c = 0; c < n_creases; ++c) {
+    const double* I = gind + 6 * c;
+    const double sn = static_cast<double>(node_side[static_cast<int64_t>(c) * n_nodes + j]);
+    const double W = 0.5 * (1.0 + sn * I[0]);
+    const double dWx = 0.5 * sn * I[1] * rho, dWy = 0.5 * sn * I[2] * rho;
+    const double ddWxx = 0.5 * sn * I[3] * rho * rho;
+    const double ddWyy = 0.5 * sn * I[4] * rho * rho;
+    const double ddWxy = 0.5 * sn * I[5] * rho * rho;
+    const Jets o = J;
+    J.w = o.w * W;
+    J.x = o.x * W + o.w * dWx;
+    J.y = o.y * W + o.w * dWy;
+    J.xx = o.xx * W + 2.0 * o.x * dWx + o.w * ddWxx;
+    J.yy = o.yy * W + 2.0 * o.y * dWy + o.w * ddWyy;
+    J.xy = o.xy * W + o.x * dWy + o.y * dWx + o.w * ddWxy;
+  }
+  return J;
+}
+
+// Monomial basis jets (GlobalRKPM.h:114-152): degree-major, p_y ascending.
+template <int ORDER>
+struct Basis {
+  static constexpr int NP = (ORDER + 1) * (ORDER + 2) / 2;
+  double p[NP], px[NP], py[NP], pxx[NP], pyy[NP], pxy[NP];
+  __device__ __forceinline__ explicit Basis(double x, double y) {
+    double xp[ORDER + 1], yp[ORDER + 1];
+    xp[0] = 1.0; yp[0] = 1.0;
+#pragma unroll
+    for (int q = 1; q <= ORDER; ++q) { xp[q] = xp[q - 1] * x; yp[q] = yp[q - 1] * y; }
+    int idx = 0;
+#pragma unroll
+    for (int d = 0; d <= ORDER; ++d) {
+#pragma unroll
+      for (int qy = 0; qy <= d; ++qy) {
+        const int qx = d - qy;
+        p[idx] = xp[qx] * yp[qy];
+        px[idx] = qx > 0 ? static_cast<double>(qx) * xp[qx > 0 ? qx - 1 : 0] * yp[qy] : 0.0;
+        py[idx] = qy > 0 ? static_cast<double>(qy) * xp[qx] * yp[qy > 0 ? qy - 1 : 0] : 0.0;
+        pxx[idx] = qx > 1 ? static_cast<double>(qx * (qx - 1)) * xp[qx > 1 ? qx - 2 : 0] * yp[qy] : 0.0;
+        pyy[idx] = qy > 1 ? static_cast<double>(qy * (qy - 1)) * xp[qx] * yp[qy > 1 ? qy - 2 : 0] : 0.0;
+        pxy[idx] = (qx > 0 && qy > 0)
+                       ? static_cast<double>(qx * qy) * xp[qx > 0 ? qx - 1 : 0] * yp[qy > 0 ? qy - 1 : 0]
+                       : 0.0;
+        ++idx;
+      }
+    }
+  }
+};
+
+template <int NP>
+struct PackedIdx {
+  // K[i][j] of GlobalRKPM.h:29-36, row-major over i <= j.
+  __device__ __forceinline__ static int k(int i, int j) {
+    const int a = i < j ? i : j, b = i < j ? j : i;
+    return a * NP - a * (a - 1) / 2 + (b - a);
+  }
+};
+
+__device__ __forceinline__ void inv3(const double m[3][3], double r[3][3]) {
+  const double c00 = m[1][1] * m[2][2] - m[1][2] * m[2][1];
+  const double c10 = m[1][2] * m[2][0] - m[1][0] * m[2][2];
+  const double c20 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
+  const double det = m[0][0] * c00 + m[0][1] * c10 + m[0][2] * c20;
+  const double id = 1.0 / det;
+  r[0][0] = c00 * id; r[1][0] = c10 * id; r[2][0] = c20 * id;
+  r[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) * id;
+  r[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
+  r[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) * id;
+  r[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) * id;
+  r[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) * id;
+  r[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) * id;
+}
+
+__device__ __forceinline__ void mm3(const double a[3][3], const double b[3][3], double c[3][3]) {
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) c[r][k] = a[r][0] * b[0][k] + a[r][1] * b[1][k] + a[r][2] * b[2][k];
+}
+
+struct RkpmArgs {
+  int n_gp, n_nodes, kernel, n_creases;
+  double rho;
+  const double* gp_xy;
+  const double* node_xy;
+  const double* rho_node;
+  const int64_t* ptr;
+  const int32_t* idx;
+  const double* s;
+  const double* gind;        // 6 * n_creases per Gauss point
+  const int8_t* node_side;   // n_creases * n_nodes
+  double* psi;
+  double* dpsi;
+  double* ddpsi;
+  int8_t* bad;
+};
+
+// One Gauss point per thread: GlobalRKPM.h:59-397 for that point.
+template <int ORDER>
+__global__ void __launch_bounds__(kThreads) rkpm_kernel(RkpmArgs a) {
+  constexpr int NP = (ORDER + 1) * (ORDER + 2) / 2;
+  constexpr int NM = NP * (NP + 1) / 2;
+  using PI = PackedIdx<NP>;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= a.n_gp) return;
+  const int64_t p0 = a.ptr[g], p1 = a.ptr[g + 1];
+  const double gx = a.gp_xy[2 * g], gy = a.gp_xy[2 * g + 1];
+  double gind[6 * 4];
+  const int nc = a.n_creases < 4 ? a.n_creases : 4;
+  for (int c = 0; c < 6 * nc; ++c) gind[c] = a.gind[static_cast<int64_t>(g) * 6 * a.n_creases + c];
+
+  // Moments (GlobalRKPM.h:161-189): M, dMx, dMy, d2Mxx, d2Myy, d2Mxy.
+  double M[NM], Mx[NM], My[NM], Mxx[NM], Myy[NM], Mxy[NM];
+#pragma unroll
+  for (int k = 0; k < NM; ++k) { M[k] = 0; Mx[k] = 0; My[k] = 0; Mxx[k] = 0; Myy[k] = 0; Mxy[k] = 0; }
+  for (int64_t e = p0; e < p1; ++e) {
+    const int j = a.idx[e];
+    const double xi = (gx - a.node_xy[2 * j]) / a.rho;
+    const double eta = (gy - a.node_xy[2 * j + 1]) / a.rho;
+    const double fac = a.rho_node ? a.rho / a.rho_node[j] : 1.0;
+    const Jets J = weight_jets(a.kernel, xi, eta, a.s[e], fac, nc, gind, a.node_side, a.n_nodes, j, a.rho);
+    const Basis<ORDER> B(xi, eta);
+#pragma unroll
+    for (int ip = 0; ip < NP; ++ip) {
+#pragma unroll
+      for (int jp = ip; jp < NP; ++jp) {
+        const int k = PI::k(ip, jp);
+        const double pi = B.p[ip], pj = B.p[jp];
+        const double dpix = B.px[ip], dpjx = B.px[jp], dpiy = B.py[ip], dpjy = B.py[jp];
+        const double pp = pi * pj;
+        const double sx = dpix * pj + pi * dpjx, sy = dpiy * pj + pi * dpjy;
+        M[k] += pp * J.w;
+        Mx[k] += pp * J.x + sx * J.w;
+        My[k] += pp * J.y + sy * J.w;
+        Mxx[k] += J.xx * pp + 2.0 * J.x * sx + J.w * (B.pxx[ip] * pj + 2.0 * dpix * dpjx + pi * B.pxx[jp]);
+        Myy[k] += J.yy * pp + 2.0 * J.y * sy + J.w * (B.pyy[ip] * pj + 2.0 * dpiy * dpjy + pi * B.pyy[jp]);
+        Mxy[k] += J.xy * pp + J.x * sy + J.y * sx +
+                  J.w * (B.pxy[ip] * pj + dpix * dpjy + dpiy * dpjx + pi * B.pxy[jp]);
+      }
+    }
+  }
+
+  // Leading 3x3 inverse with derivatives and the residual guard (GlobalRKPM.h:203-239).
+  double Iv[NM], Ix[NM], Iy[NM], Ixx[NM], Iyy[NM], Ixy[NM];
+#pragma unroll
+  for (int k = 0; k < NM; ++k) { Iv[k] = 0; Ix[k] = 0; Iy[k] = 0; Ixx[k] = 0; Iyy[k] = 0; Ixy[k] = 0; }
+  int bad = 0;
+  {
+    double m3[3][3], dx3[3][3], dy3[3][3], dxx3[3][3], dyy3[3][3], dxy3[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int k = PI::k(r, c);
+        m3[r][c] = M[k]; dx3[r][c] = Mx[k]; dy3[r][c] = My[k];
+        dxx3[r][c] = Mxx[k]; dyy3[r][c] = Myy[k]; dxy3[r][c] = Mxy[k];
+      }
+    double inv[3][3], chk[3][3];
+    inv3(m3, inv);
+    mm3(m3, inv, chk);
+    bool finite = true;
+    double res = 0.0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (!isfinite(inv[r][c])) finite = false;
+        res = fmax(res, fabs(chk[r][c] - (r == c ? 1.0 : 0.0)));
+      }
+    if (!finite || res > 1e-8) bad = 1;
+    double ninv[3][3], t1[3][3], t2[3][3], invx[3][3], invy[3][3], invxx[3][3], invyy[3][3], invxy[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) ninv[r][c] = -inv[r][c];
+    mm3(ninv, dx3, t1); mm3(t1, inv, invx);
+    mm3(ninv, dy3, t1); mm3(t1, inv, invy);
+    {
+      double a2[3][3], in[3][3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) a2[r][c] = 2.0 * dx3[r][c];
+      mm3(a2, inv, t1); mm3(t1, dx3, t2);
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) in[r][c] = t2[r][c] - dxx3[r][c];
+      mm3(inv, in, t1); mm3(t1, inv, invxx);
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) a2[r][c] = 2.0 * dy3[r][c];
+      mm3(a2, inv, t1); mm3(t1, dy3, t2);
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) in[r][c] = t2[r][c] - dyy3[r][c];
+      mm3(inv, in, t1); mm3(t1, inv, invyy);
+      double q1[3][3], q2[3][3];
+      mm3(dx3, inv, t1); mm3(t1, dy3, q1);
+      mm3(dy3, inv, t1); mm3(t1, dx3, q2);
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) in[r][c] = q1[r][c] + q2[r][c] - dxy3[r][c];
+      mm3(inv, in, t1); mm3(t1, inv, invxy);
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = r; c < 3; ++c) {
+        const int k = PI::k(r, c);
+        Iv[k] = inv[r][c]; Ix[k] = invx[r][c]; Iy[k] = invy[r][c];
+        Ixx[k] = invxx[r][c]; Iyy[k] = invyy[r][c]; Ixy[k] = invxy[r][c];
+      }
+  }
+
+  // Bordered (Schur) inversion for np > 3 (GlobalRKPM.h:259-345).
+#pragma unroll
+  for (int it = 3; it < NP; ++it) {
+    double b[NP], bx[NP], by[NP], bxx[NP], byy[NP], bxy[NP];
+    double v[NP], vx[NP], vy[NP], vxx[NP], vyy[NP], vxy[NP];
+#pragma unroll
+    for (int j = 0; j < it; ++j) {
+      const int k = PI::k(j, it);
+      b[j] = M[k]; bx[j] = Mx[k]; by[j] = My[k]; bxx[j] = Mxx[k]; byy[j] = Myy[k]; bxy[j] = Mxy[k];
+    }
+#pragma unroll
+    for (int r = 0; r < it; ++r) {
+      double aIb = 0, daxb = 0, aIdbx = 0, dayb = 0, aIdby = 0;
+      double d2xxb = 0, daxdbx = 0, aId2bxx = 0, d2yyb = 0, daydby = 0, aId2byy = 0;
+      double d2xyb = 0, daxdby = 0, daydbx = 0, aId2bxy = 0;
+#pragma unroll
+      for (int c = 0; c < it; ++c) {
+        const int k = PI::k(r, c);
+        aIb += Iv[k] * b[c];
+        daxb += Ix[k] * b[c]; aIdbx += Iv[k] * bx[c];
+        dayb += Iy[k] * b[c]; aIdby += Iv[k] * by[c];
+        d2xxb += Ixx[k] * b[c]; daxdbx += Ix[k] * bx[c]; aId2bxx += Iv[k] * bxx[c];
+        d2yyb += Iyy[k] * b[c]; daydby += Iy[k] * by[c]; aId2byy += Iv[k] * byy[c];
+        d2xyb += Ixy[k] * b[c]; daxdby += Ix[k] * by[c]; daydbx += Iy[k] * bx[c]; aId2bxy += Iv[k] * bxy[c];
+      }
+      v[r] = aIb;
+      vx[r] = daxb + aIdbx;
+      vy[r] = dayb + aIdby;
+      vxx[r] = d2xxb + 2.0 * daxdbx + aId2bxx;
+      vyy[r] = d2yyb + 2.0 * daydby + aId2byy;
+      vxy[r] = d2xyb + daxdby + daydbx + aId2bxy;
+    }
+    double d_bv = 0, d_bxv = 0, d_bvx = 0, d_byv = 0, d_bvy = 0;
+    double d_bxxv = 0, d_bxvx = 0, d_bvxx = 0, d_byyv = 0, d_byvy = 0, d_bvyy = 0;
+    double d_bxyv = 0, d_bxvy = 0, d_byvx = 0, d_bvxy = 0;
+#pragma unroll
+    for (int j = 0; j < it; ++j) {
+      d_bv += b[j] * v[j];
+      d_bxv += bx[j] * v[j]; d_bvx += b[j] * vx[j];
+      d_byv += by[j] * v[j]; d_bvy += b[j] * vy[j];
+      d_bxxv += bxx[j] * v[j]; d_bxvx += bx[j] * vx[j]; d_bvxx += b[j] * vxx[j];
+      d_byyv += byy[j] * v[j]; d_byvy += by[j] * vy[j]; d_bvyy += b[j] * vyy[j];
+      d_bxyv += bxy[j] * v[j]; d_bxvy += bx[j] * vy[j]; d_byvx += by[j] * vx[j]; d_bvxy += b[j] * vxy[j];
+    }
+    const int kii = PI::k(it, it);
+    const double q = M[kii] - d_bv;
+    const double qx = Mx[kii] - (d_bxv + d_bvx);
+    const double qy = My[kii] - (d_byv + d_bvy);
+    const double qxx = Mxx[kii] - (d_bxxv + 2.0 * d_bxvx + d_bvxx);
+    const double qyy = Myy[kii] - (d_byyv + 2.0 * d_byvy + d_bvyy);
+    const double qxy = Mxy[kii] - (d_bxyv + d_bxvy + d_byvx + d_bvxy);
+    // A point already flagged singular keeps that flag: the reference throws on the
+    // singular set before it reaches the bordering.
+    if (!(fabs(q) > 1e-12 * fmax(fabs(M[kii]), 1.0)) && bad == 0) bad = 2;
+    const double iQ = 1.0 / q, iQ2 = iQ * iQ, iQ3 = iQ2 * iQ;
+#pragma unroll
+    for (int r = 0; r < it; ++r) {
+#pragma unroll
+      for (int c = r; c < it; ++c) {
+        const int k = PI::k(r, c);
+        Iv[k] += v[r] * v[c] * iQ;
+        Ix[k] += (vx[r] * v[c] + v[r] * vx[c]) * iQ - v[r] * v[c] * qx * iQ2;
+        Iy[k] += (vy[r] * v[c] + v[r] * vy[c]) * iQ - v[r] * v[c] * qy * iQ2;
+        Ixx[k] += (vxx[r] * v[c] + 2.0 * vx[r] * vx[c] + v[r] * vxx[c]) * iQ -
+                  (vx[r] * v[c] + v[r] * vx[c]) * qx * iQ2 * 2.0 +
+                  v[r] * v[c] * (2.0 * qx * qx * iQ3 - qxx * iQ2);
+        Iyy[k] += (vyy[r] * v[c] + 2.0 * vy[r] * vy[c] + v[r] * vyy[c]) * iQ -
+                  (vy[r] * v[c] + v[r] * vy[c]) * qy * iQ2 * 2.0 +
+                  v[r] * v[c] * (2.0 * qy * qy * iQ3 - qyy * iQ2);
+        Ixy[k] += (vxy[r] * v[c] + vx[r] * vy[c] + vy[r] * vx[c] + v[r] * vxy[c]) * iQ -
+                  (vx[r] * v[c] + v[r] * vx[c]) * qy * iQ2 - (vy[r] * v[c] + v[r] * vy[c]) * qx * iQ2 +
+                  v[r] * v[c] * (2.0 * qx * qy * iQ3 - qxy * iQ2);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < it; ++j) {
+      const int k = PI::k(j, it);
+      Iv[k] = -v[j] * iQ;
+      Ix[k] = -vx[j] * iQ + v[j] * qx * iQ2;
+      Iy[k] = -vy[j] * iQ + v[j] * qy * iQ2;
+      Ixx[k] = -vxx[j] * iQ + 2.0 * vx[j] * qx * iQ2 + v[j] * (qxx * iQ2 - 2.0 * qx * qx * iQ3);
+      Iyy[k] = -vyy[j] * iQ + 2.0 * vy[j] * qy * iQ2 + v[j] * (qyy * iQ2 - 2.0 * qy * qy * iQ3);
+      Ixy[k] = -vxy[j] * iQ + vx[j] * qy * iQ2 + vy[j] * qx * iQ2 + v[j] * (qxy * iQ2 - 2.0 * qx * qy * iQ3);
+    }
+    Iv[kii] = iQ;
+    Ix[kii] = -qx * iQ2;
+    Iy[kii] = -qy * iQ2;
+    Ixx[kii] = 2.0 * qx * qx * iQ3 - qxx * iQ2;
+    Iyy[kii] = 2.0 * qy * qy * iQ3 - qyy * iQ2;
+    Ixy[kii] = 2.0 * qx * qy * iQ3 - qxy * iQ2;
+  }
+  a.bad[g] = static_cast<int8_t>(bad);
+
+  // Row 0 of the inverse and its jets (the only part the shape functions use).
+  double c0[NP], c0x[NP], c0y[NP], c0xx[NP], c0yy[NP], c0xy[NP];
+#pragma unroll
+  for (int jp = 0; jp < NP; ++jp) {
+    const int k = PI::k(0, jp);
+    c0[jp] = Iv[k]; c0x[jp] = Ix[k]; c0y[jp] = Iy[k]; c0xx[jp] = Ixx[k]; c0yy[jp] = Iyy[k]; c0xy[jp] = Ixy[k];
+  }
+  // Shape functions (GlobalRKPM.h:363-396).
+  const double rho2 = a.rho * a.rho;
+  for (int64_t e = p0; e < p1; ++e) {
+    const int j = a.idx[e];
+    const double xi = (gx - a.node_xy[2 * j]) / a.rho;
+    const double eta = (gy - a.node_xy[2 * j + 1]) / a.rho;
+    const double fac = a.rho_node ? a.rho / a.rho_node[j] : 1.0;
+    const Jets J = weight_jets(a.kernel, xi, eta, a.s[e], fac, nc, gind, a.node_side, a.n_nodes, j, a.rho);
+    const Basis<ORDER> B(xi, eta);
+    double C = 0.0, Cx = 0.0, Cy = 0.0, Cxx = 0.0, Cyy = 0.0, Cxy = 0.0;
+#pragma unroll
+    for (int jp = 0; jp < NP; ++jp) {
+      C += c0[jp] * B.p[jp];
+      Cx += c0x[jp] * B.p[jp] + c0[jp] * B.px[jp];
+      Cy += c0y[jp] * B.p[jp] + c0[jp] * B.py[jp];
+      Cxx += c0xx[jp] * B.p[jp] + 2.0 * c0x[jp] * B.px[jp] + c0[jp] * B.pxx[jp];
+      Cyy += c0yy[jp] * B.p[jp] + 2.0 * c0y[jp] * B.py[jp] + c0[jp] * B.pyy[jp];
+      Cxy += c0xy[jp] * B.p[jp] + c0x[jp] * B.py[jp] + c0y[jp] * B.px[jp] + c0[jp] * B.pxy[jp];
+    }
+    a.psi[e] = C * J.w;
+    a.dpsi[2 * e] = (Cx * J.w + C * J.x) / a.rho;
+    a.dpsi[2 * e + 1] = (Cy * J.w + C * J.y) / a.rho;
+    a.ddpsi[3 * e] = (Cxx * J.w + 2.0 * Cx * J.x + C * J.xx) / rho2;
+    a.ddpsi[3 * e + 1] = (Cyy * J.w + 2.0 * Cy * J.y + C * J.yy) / rho2;
+    a.ddpsi[3 * e + 2] = (Cxy * J.w + Cx * J.y + Cy * J.x + C * J.xy) / rho2;
+  }
+}
+
+inline unsigned blocks_for(int64_t n, int t = kThreads) { return static_cast<unsigned>((n + t - 1) / t); }
+
+}  // namespace
+
+void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shape_params& prm,
+                 const std::vector<Crease>& creases, cgb_shape* out) {
+  cudaStream_t st = ctx->stream;
+  const int n_nodes = ctx->n_nodes;
+  if (n_nodes <= 0) throw Error(CGB_ERR_INVALID, "cgb_shape_build: nodes not set (cgb_set_nodes)");
+  if (n_gp < 0) throw Error(CGB_ERR_INVALID, "cgb_shape_build: n_gp < 0");
+  if (prm.order < 1 || prm.order > 3)
+    throw Error(CGB_ERR_INVALID, "cgb_shape_build: order must be 1, 2 or 3");
+  if (!(prm.rho > 0.0)) throw Error(CGB_ERR_INVALID, "cgb_shape_build: rho must be > 0");
+  if (creases.size() > 4) throw Error(CGB_ERR_CAPACITY, "cgb_shape_build: at most 4 creases per call");
+  out->ctx = ctx;
+  out->n_gp = n_gp;
+
+  // ---- node cell grid (FRNN.h:33-44), host side, O(n_nodes) ----
+  const double* nxy = ctx->h_node_xy.data();
+  double cell = prm.rho;
+  std::vector<double> rn;
+  if (prm.rho_node) {
+    rn.assign(prm.rho_node, prm.rho_node + n_nodes);
+    cell = 0.0;
+    for (double r : rn) {
+      if (!(r > 0.0)) throw Error(CGB_ERR_INVALID, "cgb_shape_build: rho_node must be > 0");
+      cell = std::max(cell, r);
+    }
+  }
+  double minx = nxy[0], miny = nxy[1], maxx = nxy[0];
+  for (int i = 0; i < n_nodes; ++i) {
+    minx = std::min(minx, nxy[2 * i]);
+    miny = std::min(miny, nxy[2 * i + 1]);
+    maxx = std::max(maxx, nxy[2 * i]);
+  }
+  const int cols = static_cast<int>(std::ceil((maxx - minx) / cell)) + 1;
+  std::vector<long long> key(n_nodes);
+  long long kmax = 0;
+  for (int i = 0; i < n_nodes; ++i) {
+    const int cx = static_cast<int>(std::floor((nxy[2 * i] - minx) / cell));
+    const int cy = static_cast<int>(std::floor((nxy[2 * i + 1] - miny) / cell));
+    key[i] = static_cast<long long>(cy) * cols + cx;
+    kmax = std::max(kmax, key[i]);
+  }
+  const long long ncells = kmax + 1;
+  if (ncells > (1LL << 28))
+    throw Error(CGB_ERR_CAPACITY, "cgb_shape_build: the node cell grid exceeds 2^28 cells (rho too small for the node extent)");
+  std::vector<int32_t> cstart(ncells + 1, 0), cnodes(n_nodes);
+  for (int i = 0; i < n_nodes; ++i) cstart[key[i] + 1]++;
+  for (long long c = 0; c < ncells; ++c) cstart[c + 1] += cstart[c];
+  {
+    std::vector<int32_t> cur(cstart.begin(), cstart.end() - 1);
+    for (int i = 0; i < n_nodes; ++i) cnodes[cur[key[i]]++] = i;  // ascending node index per cell
+  }
+  DevBuf<int32_t> d_cstart, d_cnodes;
+  DevBuf<double> d_rn;
+  upload(d_cstart, cstart.data(), cstart.size(), st);
+  upload(d_cnodes, cnodes.data(), cnodes.size(), st);
+  if (prm.rho_node) upload(d_rn, rn.data(), rn.size(), st);
+  GridDev G{minx, miny, cell, cols, ncells, d_cstart.p, d_cnodes.p};
+
+  upload(out->gp_xy, gp_xy, 2 * static_cast<size_t>(n_gp), st);
+  const double rho2 = prm.rho * prm.rho;
+  DevBuf<int32_t> d_cnt(n_gp);
+  if (n_gp > 0)
+    frnn_kernel<<<blocks_for(n_gp), kThreads, 0, st>>>(n_gp, out->gp_xy.p, ctx->node_xy.p,
+                                                        prm.rho_node ? d_rn.p : nullptr, prm.rho, rho2, G,
+                                                        nullptr, d_cnt.p, nullptr, nullptr);
+  CGB_CUDA(cudaGetLastError());
+  std::vector<int32_t> cnt(n_gp);
+  if (n_gp > 0)
+    CGB_CUDA(cudaMemcpyAsync(cnt.data(), d_cnt.p, sizeof(int32_t) * n_gp, cudaMemcpyDeviceToHost, st));
+  CGB_CUDA(cudaStreamSynchronize(st));
+  std::vector<int64_t> ptr(n_gp + 1, 0);
+  int max_n = 0;
+  for (int g = 0; g < n_gp; ++g) {
+    ptr[g + 1] = ptr[g] + cnt[g];
+    max_n = std::max(max_n, cnt[g]);
+  }
+  const int64_t nnz = ptr[n_gp];
+  if (nnz >= (1LL << 31)) throw Error(CGB_ERR_CAPACITY, "cgb_shape_build: more than 2^31 neighbour entries");
+  out->nnz = nnz;
+  out->max_n = max_n;
+  upload(out->nbr_ptr, ptr.data(), ptr.size(), st);
+  out->nbr_idx.alloc(nnz);
+  out->s.alloc(nnz);
+  if (n_gp > 0)
+    frnn_kernel<<<blocks_for(n_gp), kThreads, 0, st>>>(n_gp, out->gp_xy.p, ctx->node_xy.p,
+                                                        prm.rho_node ? d_rn.p : nullptr, prm.rho, rho2, G,
+                                                        out->nbr_ptr.p, nullptr, out->nbr_idx.p, out->s.p);
+  CGB_CUDA(cudaGetLastError());
+
+  // ---- crease indicators: per node side, per Gauss point value and derivatives ----
+  const int nc = static_cast<int>(creases.size());
+  std::vector<DevBuf<double>> cxy(nc);
+  DevBuf<int8_t> side(static_cast<size_t>(std::max(nc, 1)) * n_nodes);
+  DevBuf<double> gind(static_cast<size_t>(std::max(nc, 1)) * 6 * std::max(n_gp, 1));
+  std::vector<DevCrease> dcr(nc);
+  for (int c = 0; c < nc; ++c) {
+    upload(cxy[c], creases[c].xy.data(), creases[c].xy.size(), st);
+    dcr[c] = DevCrease{cxy[c].p, static_cast<int>(creases[c].xy.size() / 2), creases[c].extend_start,
+                       creases[c].extend_end, creases[c].is_closed};
+    node_side_kernel<<<blocks_for(n_nodes), kThreads, 0, st>>>(n_nodes, ctx->node_xy.p, dcr[c],
+                                                                 side.p + static_cast<int64_t>(c) * n_nodes);
+  }
+  // Gauss-point indicators laid out [g][c][6]: computed per crease into a temporary,
+  // then interleaved.
+  if (nc > 0 && n_gp > 0) {
+    DevBuf<double> tmp(static_cast<size_t>(6) * n_gp);
+    std::vector<double> h_all(static_cast<size_t>(6) * nc * n_gp), h_one(static_cast<size_t>(6) * n_gp);
+    for (int c = 0; c < nc; ++c) {
+      gp_indicator_kernel<<<blocks_for(n_gp), kThreads, 0, st>>>(n_gp, out->gp_xy.p, dcr[c], tmp.p);
+      CGB_CUDA(cudaMemcpyAsync(h_one.data(), tmp.p, tmp.bytes(), cudaMemcpyDeviceToHost, st));
+      CGB_CUDA(cudaStreamSynchronize(st));
+      for (int g = 0; g < n_gp; ++g)
+        std::memcpy(&h_all[(static_cast<size_t>(g) * nc + c) * 6], &h_one[static_cast<size_t>(g) * 6],
+                    6 * sizeof(double));
+    }
+    CGB_CUDA(cudaMemcpyAsync(gind.p, h_all.data(), h_all.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  CGB_CUDA(cudaGetLastError());
+
+  // ---- RKPM ----
+  out->psi.alloc(nnz);
+  out->dpsi.alloc(2 * nnz);
+  out->ddpsi.alloc(3 * nnz);
+  DevBuf<int8_t> bad(n_gp);
+  RkpmArgs ra{n_gp, n_nodes, prm.kernel, nc, prm.rho, out->gp_xy.p, ctx->node_xy.p,
+              prm.rho_node ? d_rn.p : nullptr, out->nbr_ptr.p, out->nbr_idx.p, out->s.p, gind.p,
+              side.p, out->psi.p, out->dpsi.p, out->ddpsi.p, bad.p};
+  if (n_gp > 0) {
+    switch (prm.order) {
+      case 1: rkpm_kernel<1><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
+      case 2: rkpm_kernel<2><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
+      default: rkpm_kernel<3><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
+    }
+  }
+  CGB_CUDA(cudaGetLastError());
+  std::vector<int8_t> hbad(n_gp);
+  if (n_gp > 0) CGB_CUDA(cudaMemcpyAsync(hbad.data(), bad.p, n_gp, cudaMemcpyDeviceToHost, st));
+  CGB_CUDA(cudaStreamSynchronize(st));
+  // The reference's guards (GlobalRKPM.h:241-257 after the 3x3 block, 347-359 after
+  // the bordering): singular first, then pivot collapse.
+  size_t n1 = 0, f1 = 0, n2 = 0, f2 = 0;
+  for (int g = 0; g < n_gp; ++g) {
+    if (hbad[g] == 1) { if (!n1) f1 = g; ++n1; }
+    if (hbad[g] == 2) { if (!n2) f2 = g; ++n2; }
+  }
+  if (n1) {
+    throw Error(CGB_ERR_SINGULAR,
+                "RKPM: singular moment matrix at " + std::to_string(n1) + " of " + std::to_string(n_gp) +
+                    " Gauss points (first is index " + std::to_string(f1) + " with " +
+                    std::to_string(cnt[f1]) +
+                    " neighbours). The support is rank-deficient for the requested "
+                    "basis order - typically too few visible nodes, which happens "
+                    "where a crease cuts most of a support away. Increase the support "
+                    "radius, refine the mesh there, or lower the order.");
+  }
+  if (n2) {
+    throw Error(CGB_ERR_PIVOT,
+                "RKPM: moment-matrix pivot collapsed during block inversion at " + std::to_string(n2) +
+                    " of " + std::to_string(n_gp) + " Gauss points (first is index " + std::to_string(f2) +
+                    " with " + std::to_string(cnt[f2]) +
+                    " neighbours). Same cause and remedies as a singular moment matrix.");
+  }
+}
+
+}  // namespace cgb

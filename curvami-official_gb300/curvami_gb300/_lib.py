@@ -1,0 +1,96 @@
+"""ctypes declarations of the C ABI in include/curvami_gb300.h.
+
+The shared library is built in-tree (``build.py``) and loaded from this directory;
+there is no CPU fallback — a missing library or GPU raises."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcurvami_gb300.so")
+
+CGB_OK = 0
+CGB_ERR_INVALID = 1
+CGB_ERR_CUDA = 2
+CGB_ERR_SINGULAR = 3
+CGB_ERR_PIVOT = 4
+CGB_ERR_MAPPING = 5
+CGB_ERR_CAPACITY = 6
+CGB_ERR_DEVICE = 7
+
+TANGENT = 0x1
+HINGE = 0x2
+MIXED = 0x4
+DETERMINISTIC = 0x8
+HINGE_EXACT = 0x10
+
+# Every symbol the header declares, with (restype, argtypes).
+vp, i32, i64, dbl, cp = C.c_void_p, C.c_int, C.c_int64, C.c_double, C.c_char_p
+SIGNATURES = {
+    "cgb_create": (i32, [i32, C.POINTER(vp)]),
+    "cgb_destroy": (i32, [vp]),
+    "cgb_last_error": (cp, [vp]),
+    "cgb_set_stream": (i32, [vp, vp]),
+    "cgb_synchronize": (i32, [vp]),
+    "cgb_set_nodes": (i32, [vp, vp, i32]),
+    "cgb_shape_build": (i32, [vp, vp, i32, vp, vp, i32, C.POINTER(vp)]),
+    "cgb_shape_from_host": (i32, [vp, i32, vp, vp, vp, vp, vp, C.POINTER(vp)]),
+    "cgb_shape_size": (i32, [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i32)]),
+    "cgb_shape_download": (i32, [vp, vp, vp, vp, vp, vp, vp]),
+    "cgb_shape_device": (i32, [vp, vp, vp, vp, vp, vp]),
+    "cgb_shape_destroy": (i32, [vp]),
+    "cgb_assembler_create": (i32, [vp, vp, vp, vp, i32, C.POINTER(vp)]),
+    "cgb_assembler_destroy": (i32, [vp]),
+    "cgb_assembler_pattern": (i32, [vp, C.POINTER(i32), C.POINTER(i64)]),
+    "cgb_assembler_download_pattern": (i32, [vp, vp, vp]),
+    "cgb_assembler_download_map": (i32, [vp, vp, i64]),
+    "cgb_set_material": (i32, [vp, vp, vp, vp]),
+    "cgb_assemble": (i32, [vp, vp, vp, vp, i32]),
+    "cgb_assemble_device": (i32, [vp, vp, vp, vp, i32]),
+    "cgb_energies": (i32, [vp, vp, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(dbl)]),
+}
+
+
+class Crease(C.Structure):
+    _fields_ = [("xy", vp), ("n_vertices", i32), ("extend_start", i32), ("extend_end", i32),
+                ("is_closed", i32)]
+
+
+class ShapeParams(C.Structure):
+    _fields_ = [("rho", dbl), ("rho_node", vp), ("order", i32), ("kernel", i32)]
+
+
+class Fold(C.Structure):
+    _fields_ = [("left", vp), ("right", vp), ("weight", vp), ("tangent", vp), ("Kt", dbl),
+                ("theta0", dbl), ("theta0_gp", vp), ("active", vp)]
+
+
+class CGBError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(msg)
+        self.code = code
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Load the in-tree library (build it first with build.py / __graft_entry__.build)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise CGBError(CGB_ERR_INVALID,
+                           f"{p} is missing: build it with curvami-official_gb300/build.py")
+        lib = C.CDLL(p)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+        return lib

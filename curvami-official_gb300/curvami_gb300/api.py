@@ -1,0 +1,271 @@
+"""Host-side mirror of the reference's hot-path interface over the C ABI.
+
+Names follow the reference's call sites:
+  * ``shape_functions`` = GlobalFRNN::execute + GlobalRKPM::solve for one domain
+    (core/include/curvami/FRNN.h:23, GlobalRKPM.h:19), as SetupHelper::
+    recomputeShapeFunctions calls them (plate/SetupHelper.h:112-138);
+  * ``NonLinearAssembler`` = the assembler (plate/Assembly.h:18-346) with the hinge of
+    Meshless::assembleSystem (plate/Meshless.h:102-127);
+  * ``Meshless``-style helpers ``assemble_system`` / ``assemble_internal_only``.
+Errors raise CGBError carrying the reference's message where it has one.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+class Context:
+    """One GPU, one stream (cgb_context)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = L.load_library()
+        h = C.c_void_p()
+        rc = self.lib.cgb_create(device, C.byref(h))
+        if rc != L.CGB_OK:
+            raise L.CGBError(rc, f"cgb_create failed (status {rc}): no usable CUDA device")
+        self.h = h
+        self._keep = []
+
+    def check(self, rc: int):
+        if rc != L.CGB_OK:
+            msg = self.lib.cgb_last_error(self.h).decode(errors="replace")
+            raise L.CGBError(rc, msg)
+
+    def set_nodes(self, node_xy):
+        self.node_xy = _c(node_xy, np.float64)
+        self.n_nodes = len(self.node_xy)
+        self.check(self.lib.cgb_set_nodes(self.h, _p(self.node_xy), self.n_nodes))
+
+    def synchronize(self):
+        self.check(self.lib.cgb_synchronize(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cgb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _creases_struct(creases):
+    arr = (L.Crease * max(len(creases), 1))()
+    keep = []
+    for k, cr in enumerate(creases):
+        xy = _c(cr["vertices"], np.float64).reshape(-1)
+        keep.append(xy)
+        arr[k].xy = xy.ctypes.data
+        arr[k].n_vertices = len(xy) // 2
+        arr[k].extend_start = int(bool(cr.get("extend_start", False)))
+        arr[k].extend_end = int(bool(cr.get("extend_end", False)))
+        arr[k].is_closed = int(bool(cr.get("is_closed", False)))
+    return arr, keep
+
+
+class ShapeSet:
+    """Device-resident neighbour lists and shape functions of one point set (cgb_shape)."""
+
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.h = handle
+        n = C.c_int(); nnz = C.c_int64(); mx = C.c_int()
+        ctx.check(ctx.lib.cgb_shape_size(self.h, C.byref(n), C.byref(nnz), C.byref(mx)))
+        self.n_gp, self.nnz, self.max_n = n.value, nnz.value, mx.value
+
+    def download(self):
+        ptr = np.zeros(self.n_gp + 1, np.int64)
+        idx = np.zeros(max(self.nnz, 1), np.int32)
+        s = np.zeros(max(self.nnz, 1))
+        psi = np.zeros(max(self.nnz, 1))
+        dpsi = np.zeros((max(self.nnz, 1), 2))
+        ddpsi = np.zeros((max(self.nnz, 1), 3))
+        self.ctx.check(self.ctx.lib.cgb_shape_download(self.h, _p(ptr), _p(idx), _p(s), _p(psi), _p(dpsi),
+                                                        _p(ddpsi)))
+        k = self.nnz
+        return {"ptr": ptr, "idx": idx[:k], "s": s[:k], "psi": psi[:k], "dpsi": dpsi[:k],
+                "ddpsi": ddpsi[:k]}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.cgb_shape_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def shape_functions(ctx: Context, gp_xy, rho, order=2, creases=(), rho_node=None, kernel=0) -> ShapeSet:
+    """GlobalFRNN::execute + GlobalRKPM::solve for one set of Gauss points. Raises
+    CGBError (CGB_ERR_SINGULAR / CGB_ERR_PIVOT) with the reference's message on a
+    rank-deficient support."""
+    gp_xy = _c(gp_xy, np.float64)
+    prm = L.ShapeParams()
+    prm.rho = float(rho)
+    rn = None if rho_node is None else _c(rho_node, np.float64)
+    prm.rho_node = _p(rn)
+    prm.order = int(order)
+    prm.kernel = int(kernel)
+    arr, keep = _creases_struct(list(creases))
+    h = C.c_void_p()
+    rc = ctx.lib.cgb_shape_build(ctx.h, _p(gp_xy), len(gp_xy), C.byref(prm), C.addressof(arr),
+                                 len(creases), C.byref(h))
+    del keep
+    if rc != L.CGB_OK:
+        msg = ctx.lib.cgb_last_error(ctx.h).decode(errors="replace")
+        if h.value:
+            ctx.lib.cgb_shape_destroy(h)
+        raise L.CGBError(rc, msg)
+    return ShapeSet(ctx, h)
+
+
+def shape_from_host(ctx: Context, ptr, idx, dpsi, ddpsi, psi=None) -> ShapeSet:
+    ptr = _c(ptr, np.int64); idx = _c(idx, np.int32)
+    dpsi = _c(dpsi, np.float64); ddpsi = _c(ddpsi, np.float64)
+    psi = None if psi is None else _c(psi, np.float64)
+    h = C.c_void_p()
+    ctx.check(ctx.lib.cgb_shape_from_host(ctx.h, len(ptr) - 1, _p(ptr), _p(idx), _p(psi), _p(dpsi),
+                                          _p(ddpsi), C.byref(h)))
+    return ShapeSet(ctx, h)
+
+
+class NonLinearAssembler:
+    """initSparsityPattern at construction (face + hinge union), then assemble()."""
+
+    def __init__(self, ctx: Context, faces: ShapeSet, face_weight, folds=()):
+        self.ctx = ctx
+        self.faces = faces
+        self.face_weight = _c(face_weight, np.float64)
+        arr = (L.Fold * max(len(folds), 1))()
+        keep = []
+        for k, f in enumerate(folds):
+            w = _c(f["weight"], np.float64); t = _c(f["tangent"], np.float64)
+            keep += [w, t]
+            arr[k].left = f["left"].h
+            arr[k].right = f["right"].h
+            arr[k].weight = w.ctypes.data
+            arr[k].tangent = t.ctypes.data
+            arr[k].Kt = float(f["Kt"])
+            arr[k].theta0 = float(f.get("theta0", 0.0))
+            if f.get("theta0_gp") is not None:
+                t0 = _c(f["theta0_gp"], np.float64); keep.append(t0); arr[k].theta0_gp = t0.ctypes.data
+            if f.get("active") is not None:
+                ac = _c(f["active"], np.int8); keep.append(ac); arr[k].active = ac.ctypes.data
+        self.folds = list(folds)
+        h = C.c_void_p()
+        ctx.check(ctx.lib.cgb_assembler_create(ctx.h, faces.h, _p(self.face_weight), C.addressof(arr),
+                                               len(folds), C.byref(h)))
+        del keep
+        self.h = h
+        nd = C.c_int(); nnz = C.c_int64()
+        ctx.check(ctx.lib.cgb_assembler_pattern(self.h, C.byref(nd), C.byref(nnz)))
+        self.n_dofs, self.nnz = nd.value, nnz.value
+
+    def set_material(self, A, B, D):
+        self.A, self.B, self.D = (_c(A, np.float64).reshape(9), _c(B, np.float64).reshape(9),
+                                  _c(D, np.float64).reshape(9))
+        self.ctx.check(self.ctx.lib.cgb_set_material(self.h, _p(self.A), _p(self.B), _p(self.D)))
+
+    def pattern(self):
+        outer = np.zeros(self.n_dofs + 1, np.int32)
+        inner = np.zeros(max(self.nnz, 1), np.int32)
+        self.ctx.check(self.ctx.lib.cgb_assembler_download_pattern(self.h, _p(outer), _p(inner)))
+        return outer, inner[: self.nnz]
+
+    def csr_mapping(self):
+        n = np.diff(self.faces.download()["ptr"])
+        total = int((n * (n + 1) // 2).sum())
+        m = np.zeros(max(total, 1), np.int32)
+        self.ctx.check(self.ctx.lib.cgb_assembler_download_map(self.h, _p(m), total))
+        return m[:total]
+
+    def assemble(self, x, flags=L.TANGENT | L.HINGE, K_out=None, F_out=None):
+        """Host buffers in and out (cgb_assemble)."""
+        x = _c(x, np.float64)
+        F = F_out if F_out is not None else np.empty(self.n_dofs)
+        K = None
+        if flags & L.TANGENT:
+            K = K_out if K_out is not None else np.empty(max(self.nnz, 1))
+        self.ctx.check(self.ctx.lib.cgb_assemble(self.h, _p(x), _p(K), _p(F), int(flags)))
+        return (K[: self.nnz] if K is not None else None), F
+
+    def assemble_device(self, d_x: int, d_K: int | None, d_F: int, flags):
+        """Device pointers (cgb_assemble_device), asynchronous on the context stream."""
+        self.ctx.check(self.ctx.lib.cgb_assemble_device(self.h, C.c_void_p(d_x),
+                                                        C.c_void_p(d_K) if d_K else None,
+                                                        C.c_void_p(d_F), int(flags)))
+
+    def energies(self, x):
+        x = _c(x, np.float64)
+        em = C.c_double(); eb = C.c_double(); eh = C.c_double()
+        self.ctx.check(self.ctx.lib.cgb_energies(self.h, _p(x), C.byref(em), C.byref(eb), C.byref(eh)))
+        return em.value, eb.value, eh.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.cgb_assembler_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def abd_isotropic(E: float, nu: float, h: float):
+    """A, B, D of one isotropic ply (main.cpp:53-61 through Constitutive::computeABD,
+    plate/Constitutive.h:10-50): Q = E/(1-nu^2) [[1, nu, 0], [nu, 1, 0], [0, 0, (1-nu)/2]]."""
+    den = 1.0 - nu * nu
+    G = E / (2.0 * (1.0 + nu))
+    Q = np.array([[E / den, nu * E / den, 0.0], [nu * E / den, E / den, 0.0], [0.0, 0.0, G]])
+    z0, z1 = -h / 2.0, h / 2.0
+    return Q * (z1 - z0), 0.5 * Q * (z1 * z1 - z0 * z0), (1.0 / 3.0) * Q * (z1 ** 3 - z0 ** 3)
+
+
+class PlateModel:
+    """A synthetic plate (synth.Plate) on the GPU: shape functions of the faces and of
+    every fold side, the assembler with the hinge union pattern and the material."""
+
+    def __init__(self, plate, ctx: Context | None = None):
+        self.plate = plate
+        self.ctx = ctx or Context(0)
+        self.ctx.set_nodes(plate.node_xy)
+        kw = dict(rho=plate.rho, order=plate.order, creases=plate.creases, rho_node=plate.rho_node,
+                  kernel=plate.kernel)
+        self.faces = shape_functions(self.ctx, plate.faces.xy, **kw)
+        self.fold_sets = []
+        folds = []
+        for f in plate.folds:
+            L_ = shape_functions(self.ctx, f.left.xy, **kw)
+            R_ = shape_functions(self.ctx, f.right.xy, **kw)
+            self.fold_sets.append((L_, R_))
+            folds.append({"left": L_, "right": R_, "weight": f.left.weight, "tangent": f.left.tangent,
+                          "Kt": f.Kt, "theta0": f.theta0})
+        self.fold_specs = folds
+        self.asm = NonLinearAssembler(self.ctx, self.faces, plate.faces.weight, folds)
+        A, B, D = abd_isotropic(plate.E, plate.nu, plate.thickness)
+        self.asm.set_material(A, B, D)
+
+    def assemble_system(self, x, flags=L.TANGENT | L.HINGE):
+        return self.asm.assemble(x, flags)
+
+    def assemble_internal_only(self, x, flags=L.HINGE):
+        return self.asm.assemble(x, flags & ~L.TANGENT)[1]

@@ -1,0 +1,163 @@
+/*
+ * curvami_gb300.h — C ABI of the GB300 (sm_103a) Gauss-point hot path of Curvami.
+ *
+ * Stage A: RKPM shape functions per Gauss point — neighbour gather (GlobalFRNN),
+ *          crease-cut visibility, moment matrix, factorisation, Phi / grad Phi /
+ *          Hessian Phi (GlobalRKPM).
+ * Stage B: large-rotation Kirchhoff-Love residual and tangent with the elastic-hinge
+ *          terms, scattered into the reference's CSC stiffness (NonLinearAssembler,
+ *          Constraints::evaluateElasticFold, Meshless::assembleSystem*).
+ *
+ * Plain C types only (pointers and sizes). Every call returns a status code; on a
+ * non-zero status cgb_last_error() holds the message (for the reference's own error
+ * conditions, the reference's exception text). One context drives one GPU and one
+ * CUDA stream; it is not thread-safe. There is no CPU fallback: a missing or
+ * unusable GPU is an error.
+ *
+ * Layout conventions (the reference's):
+ *  - node / point coordinates interleaved x, y (2 doubles per point);
+ *  - neighbour lists as CSR: nbr_ptr[n_gp + 1] (int64), nbr_idx[nnz] (int32), in the
+ *    FRNN order of core/include/curvami/FRNN.h:57-77;
+ *  - dpsi: 2 doubles per entry (d/dX, d/dY); ddpsi: 3 per entry (XX, YY, XY);
+ *  - x: 3 displacement dofs per node; F: 3 per node;
+ *  - K: Eigen::SparseMatrix<double> ColMajor storage of the block-upper stiffness
+ *    (plate/Assembly.h:59-99): outer[3 n_nodes + 1], inner[nnz], values[nnz]. The
+ *    pattern is the union of the face blocks and the hinge blocks that
+ *    Meshless::assembleSystem adds (plate/Meshless.h:113-127); it is fixed once the
+ *    assembler exists and values are overwritten by every assembly.
+ */
+#ifndef CURVAMI_GB300_H
+#define CURVAMI_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+enum {
+  CGB_OK = 0,
+  CGB_ERR_INVALID = 1,  /* bad argument or call order */
+  CGB_ERR_CUDA = 2,     /* CUDA runtime error (no device, out of memory, ...) */
+  CGB_ERR_SINGULAR = 3, /* RKPM: singular moment matrix (GlobalRKPM.h:241-257) */
+  CGB_ERR_PIVOT = 4,    /* RKPM: Schur pivot collapsed (GlobalRKPM.h:347-359) */
+  CGB_ERR_MAPPING = 5,  /* neighbour missing from the sparsity pattern (Assembly.h:146-152) */
+  CGB_ERR_CAPACITY = 6, /* a documented size limit of the kernels was exceeded */
+  CGB_ERR_DEVICE = 7    /* a device-side check failed (index out of range) */
+};
+
+/* ---- assembly flags ------------------------------------------------------------- */
+#define CGB_TANGENT 0x1       /* form K; without it only F (residual) is produced */
+#define CGB_HINGE 0x2         /* add elastic-hinge terms (the reference's flagRig == false) */
+#define CGB_MIXED 0x4         /* FP64 residual, FP32 tangent; default FP64 throughout */
+#define CGB_DETERMINISTIC 0x8 /* fixed-order segmented-reduction scatter; default atomics */
+#define CGB_HINGE_EXACT 0x10  /* hinge tangent with the dihedral Hessian (fold_exact_tangent) */
+
+/* ---- handles --------------------------------------------------------------------- */
+typedef struct cgb_context cgb_context;
+typedef struct cgb_shape cgb_shape;
+typedef struct cgb_assembler cgb_assembler;
+
+/* A crease polyline. Replaces Enrichment::FoldLine
+ * (core/include/curvami/Enrichment.h:10-15). */
+typedef struct {
+  const double* xy; /* 2 * n_vertices doubles */
+  int n_vertices;
+  int extend_start;
+  int extend_end;
+  int is_closed;
+} cgb_crease;
+
+/* Shape-stage parameters. rho / order as GlobalRKPM::solve (GlobalRKPM.h:19-21).
+ * rho_node: NULL for the reference's single radius, else a per-node radius (extension).
+ * kernel: 0 quartic spline (GlobalRKPM.h:15-17), 1 cubic B-spline (extension). */
+typedef struct {
+  double rho;
+  const double* rho_node;
+  int order;
+  int kernel;
+} cgb_shape_params;
+
+/* One fold for the hinge. Replaces the arguments of Constraints::evaluateElasticFold
+ * (plate/Constraints.h:341-347) for one Fold (plate/PlateData.h:54-76). */
+typedef struct {
+  const cgb_shape* left;
+  const cgb_shape* right;
+  const double* weight;    /* n_gp, the left Gauss-point weights */
+  const double* tangent;   /* 2 * n_gp, the left Gauss-point tangents */
+  double Kt;
+  double theta0;
+  const double* theta0_gp; /* n_gp or NULL (Fold::gp_theta0) */
+  const int8_t* active;    /* n_gp or NULL (Fold::gp_active) */
+} cgb_fold;
+
+/* ---- context --------------------------------------------------------------------- */
+int cgb_create(int device, cgb_context** out);
+int cgb_destroy(cgb_context* ctx);
+const char* cgb_last_error(const cgb_context* ctx);
+/* Use the caller's cudaStream_t (passed as void*) for every launch and copy. */
+int cgb_set_stream(cgb_context* ctx, void* stream);
+int cgb_synchronize(cgb_context* ctx);
+
+/* Reference node coordinates (Node::X_ref, core/include/curvami/MeshfreeData.h:7-14). */
+int cgb_set_nodes(cgb_context* ctx, const double* node_xy, int n_nodes);
+
+/* ---- stage A: shape functions ---------------------------------------------------- */
+/* GlobalFRNN::execute + GlobalRKPM::solve for one set of Gauss points
+ * (core/include/curvami/FRNN.h:23, core/include/curvami/GlobalRKPM.h:19), as called
+ * per domain by SetupHelper::recomputeShapeFunctions (plate/SetupHelper.h:112-138).
+ * Neighbour sets are bit-exact with the FRNN (inclusive FP64 distance test without
+ * FMA contraction); Phi and its derivatives are computed in FP64.
+ * Returns CGB_ERR_SINGULAR / CGB_ERR_PIVOT with the reference's message on a
+ * rank-deficient support (the shape set is still created and must be destroyed). */
+int cgb_shape_build(cgb_context* ctx, const double* gp_xy, int n_gp,
+                    const cgb_shape_params* params, const cgb_crease* creases, int n_creases,
+                    cgb_shape** out);
+/* Wrap shape functions computed elsewhere (GaussPointData::neighbor_node_ids, dPsi,
+ * ddPsi; core/include/curvami/MeshfreeData.h:28-34) for the assembly. psi may be NULL. */
+int cgb_shape_from_host(cgb_context* ctx, int n_gp, const int64_t* nbr_ptr,
+                        const int32_t* nbr_idx, const double* psi, const double* dpsi,
+                        const double* ddpsi, cgb_shape** out);
+int cgb_shape_size(const cgb_shape* sh, int* n_gp, int64_t* nnz, int* max_neighbours);
+/* Copy results to host arrays; any pointer may be NULL. */
+int cgb_shape_download(const cgb_shape* sh, int64_t* nbr_ptr, int32_t* nbr_idx, double* s,
+                       double* psi, double* dpsi, double* ddpsi);
+/* Device pointers of the shape arrays (for callers that keep data on the GPU). */
+int cgb_shape_device(const cgb_shape* sh, const int64_t** nbr_ptr, const int32_t** nbr_idx,
+                     const double** psi, const double** dpsi, const double** ddpsi);
+int cgb_shape_destroy(cgb_shape* sh);
+
+/* ---- stage B: assembly ----------------------------------------------------------- */
+/* NonLinearAssembler::initSparsityPattern (plate/Assembly.h:59-153) for the face
+ * Gauss points, widened by the hinge blocks of the folds (Meshless::assembleSystem,
+ * plate/Meshless.h:113-127). face_weight: GaussPointData::weight per face point. */
+int cgb_assembler_create(cgb_context* ctx, const cgb_shape* faces, const double* face_weight,
+                         const cgb_fold* folds, int n_folds, cgb_assembler** out);
+int cgb_assembler_destroy(cgb_assembler* a);
+int cgb_assembler_pattern(const cgb_assembler* a, int* n_dofs, int64_t* nnz);
+/* The K pattern (Eigen ColMajor outerIndexPtr / innerIndexPtr). */
+int cgb_assembler_download_pattern(const cgb_assembler* a, int32_t* outer, int32_t* inner);
+/* NonLinearAssembler::csrMapping (plate/Assembly.h:49-54) of every face Gauss point,
+ * concatenated: n(n+1)/2 entries per point, the position of min(ni, nj) among the
+ * block rows of column max(ni, nj). */
+int cgb_assembler_download_map(const cgb_assembler* a, int32_t* map, int64_t n_entries);
+/* LaminateProperties A, B, D (plate/PlateData.h:20-35), row-major 3x3 each. */
+int cgb_set_material(cgb_assembler* a, const double* A, const double* B, const double* D);
+
+/* Meshless::assembleSystem / assembleSystemInternalOnly (plate/Meshless.h:102-127)
+ * with HOST buffers: x[3 n_nodes] in, K_values[nnz] and F[3 n_nodes] out (K_values
+ * may be NULL without CGB_TANGENT). Copies x in and K/F out; synchronous. */
+int cgb_assemble(cgb_assembler* a, const double* x, double* K_values, double* F, int flags);
+/* Same with DEVICE pointers; asynchronous on the context stream. */
+int cgb_assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags);
+
+/* Meshless::computeStrainEnergies (plate/Meshless.h:204-220) and
+ * computeTotalHingeEnergy (plate/Meshless.h:197-202) at x (host buffer). */
+int cgb_energies(cgb_assembler* a, const double* x, double* E_mem, double* E_ben,
+                 double* E_hin);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CURVAMI_GB300_H */

@@ -545,7 +545,9 @@ int orc_rkpm(const double* node_xy, int n_nodes, const double* gp_xy, int n_gp,
         const double qxx = d2Mxx[kii] - (dot(d2bxx, v) + 2.0 * dot(dbx, vx) + dot(b, vxx));
         const double qyy = d2Myy[kii] - (dot(d2byy, v) + 2.0 * dot(dby, vy) + dot(b, vyy));
         const double qxy = d2Mxy[kii] - (dot(d2bxy, v) + dot(dbx, vy) + dot(dby, vx) + dot(b, vxy));
-        if (!(std::fabs(q) > 1e-12 * std::max(std::fabs(M[kii]), 1.0))) bad = 2;
+        // A point flagged singular keeps that flag (the reference throws on the singular
+        // set before the bordering, GlobalRKPM.h:241-257).
+        if (!(std::fabs(q) > 1e-12 * std::max(std::fabs(M[kii]), 1.0)) && bad == 0) bad = 2;
         const double iQ = 1.0 / q, iQ2 = iQ * iQ, iQ3 = iQ2 * iQ;
         for (int r = 0; r < it; ++r) {
           for (int c = r; c < it; ++c) {
