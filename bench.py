@@ -1,0 +1,408 @@
+"""Benchmark: Gauss-point residual+tangent evaluations per second on one GB300.
+
+Workload (the single-plate assembly at scale): 201x201 jittered nodes (h = 0.5,
++/-0.1 jitter) on [0,100]^2, a 4x4 Gauss rule per cell (640,000 Gauss points),
+quadratic RKPM basis with the quartic window and a support radius of 3h, a circular-arc
+crease of radius 60 crossing the node layout (elastic hinge, Kt = 1e-3), and a seeded
+smooth displacement (8 Fourier modes per component, wavelengths 20-200, rotations up to
+60 degrees). A step is one full residual + tangent assembly (faces and hinge) scattered
+into the reference's CSC stiffness.
+
+The headline arm is the mixed-precision assembly (FP64 residual, FP32 tangent, atomic
+scatter); the FP64 assembly of the same library is timed alongside as the metric's
+denominator, with the error of the mixed result against it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference's CPU algorithm (the C++ restatement of its
+OpenMP loops, built with the reference's release flags) on the host cores, on a bounded
+sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "curvami-official_gb300")
+for _p in (ROOT, PKG_DIR):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Gauss-pt residual+tangent evals/s, mixed vs FP64 GPU at stated error"
+UNIT = "GP evals/s"
+SEED = 1003
+WORKLOAD = ("single-plate assembly at scale: 201x201 jittered nodes, 4x4 Gauss rule (640,000 "
+            "Gauss points), quadratic RKPM, quartic window, rho = 3h, circular-arc crease R = 60 "
+            "with elastic hinge Kt = 1e-3, seeded 8-mode Fourier displacement (rotations up to 60 "
+            "deg); one residual + tangent assembly into the CSC stiffness per step")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n-side", type=int, default=201, help="nodes per side (201 = the workload)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-rows", type=int, default=20,
+                    help="cell rows of the plate in the CPU sample (200 rows = the whole plate)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def build_workload(n_side):
+    from curvami_gb300 import synth
+
+    plate = synth.config_assembly(rule=4, n_side=n_side, seed=SEED)
+    x = synth.fourier_field(plate.node_xy, np.random.default_rng(SEED + 1))
+    return plate, x
+
+
+# ---------------------------------------------------------------------------------
+# CPU side (the oracle's restatement of the reference's OpenMP assembly)
+# ---------------------------------------------------------------------------------
+
+def cpu_sample(plate, x, rows):
+    """A bounded sample of the same workload: the Gauss points of the first `rows` cell
+    rows of the plate, with their own pattern, shape functions from the oracle."""
+    from oracle import Oracle
+
+    h = plate.meta["h"]
+    keep = plate.faces.xy[:, 1] < rows * h
+    o = Oracle(native=True)
+    gp = plate.faces.xy[keep]
+    w = plate.faces.weight[keep]
+    ptr, idx, s = o.frnn(plate.node_xy, gp, plate.rho)
+    psi, dpsi, ddpsi, bad, rc = o.rkpm(plate.node_xy, gp, ptr, idx, s, plate.rho, plate.order, plate.creases)
+    folds = []
+    for f in plate.folds:
+        sel = f.left.xy[:, 1] < rows * h
+        side = {}
+        for nm, ps in (("left", f.left), ("right", f.right)):
+            fp, fi, fs = o.frnn(plate.node_xy, ps.xy[sel], plate.rho)
+            _, fd, _, _, _ = o.rkpm(plate.node_xy, ps.xy[sel], fp, fi, fs, plate.rho, plate.order, plate.creases)
+            side[nm] = {"ptr": fp, "idx": fi, "dpsi": fd}
+        folds.append({"left": side["left"], "right": side["right"], "weight": f.left.weight[sel],
+                      "tangent": f.left.tangent[sel], "Kt": f.Kt, "theta0": f.theta0})
+    outer, inner, col_ptr, col_nodes, mp = o.pattern(plate.n_nodes, ptr, idx, folds)
+    A, B, D = o.abd(plate.E, plate.nu, plate.thickness)
+    return dict(o=o, n_gp=int(keep.sum()), w=w, ptr=ptr, idx=idx, dpsi=dpsi, ddpsi=ddpsi, folds=folds,
+                outer=outer, col_ptr=col_ptr, col_nodes=col_nodes, mp=mp, A=A, B=B, D=D, x=x,
+                n_nodes=plate.n_nodes)
+
+
+def cpu_step(S, threads):
+    o = S["o"]
+    K, F = o.update_stiffness(S["n_nodes"], S["w"], S["ptr"], S["idx"], S["dpsi"], S["ddpsi"], S["outer"],
+                              S["mp"], S["x"], S["A"], S["B"], S["D"], want_K=True, n_threads=threads)
+    o.hinge(S["n_nodes"], S["x"], S["folds"], S["outer"], S["col_ptr"], S["col_nodes"], K, F)
+
+
+def cpu_time(S, threads, steps, warmup=1):
+    for _ in range(warmup):
+        cpu_step(S, threads)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        cpu_step(S, threads)
+    return (time.perf_counter() - t0) / steps
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    plate, x = build_workload(args.n_side)
+    S = cpu_sample(plate, x, args.cpu_sample_rows)
+    cores = os.cpu_count() or 1
+    t = cpu_time(S, cores, max(args.steps, 1), max(args.warmup, 1))
+    v = S["n_gp"] / t
+    sample = (f"first {args.cpu_sample_rows} of 200 cell rows of the workload ({S['n_gp']} Gauss points, "
+              f"their own pattern and hinge points); per step NonLinearAssembler::updateStiffness + "
+              f"evaluateElasticFold")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "seed": SEED, "threads": cores},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# ---------------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) over the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[3:7]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fma_peaks(device):
+    import ctypes as C
+
+    path = os.path.join(PKG_DIR, "curvami_gb300", "libcgb_peaks.so")
+    lib = C.CDLL(path)
+    lib.cgb_measure_fma_peaks.restype = C.c_int
+    lib.cgb_measure_fma_peaks.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    f64 = C.c_double(); f32 = C.c_double()
+    lib.cgb_measure_fma_peaks(device, C.byref(f64), C.byref(f32))
+    return f64.value, f32.value
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def run_gpu(args):
+    import torch
+
+    import curvami_gb300 as cg
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        import torch.distributed as dist
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    plate, x = build_workload(args.n_side)
+    ctx = cg.Context(local)
+    t0 = time.perf_counter()
+    model = cg.PlateModel(plate, ctx)
+    setup_s = time.perf_counter() - t0
+    asm = model.asm
+    n_gp = model.faces.n_gp
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    x_d = torch.from_numpy(x).to("cuda")
+    K_d = torch.empty(asm.nnz, dtype=torch.float64, device="cuda")
+    F_d = torch.empty(asm.n_dofs, dtype=torch.float64, device="cuda")
+    MIX = cg.TANGENT | cg.HINGE | cg.MIXED
+    F64 = cg.TANGENT | cg.HINGE
+    DET = cg.TANGENT | cg.HINGE | cg.MIXED | cg.DETERMINISTIC
+
+    def step(flags):
+        asm.assemble_device(x_d.data_ptr(), K_d.data_ptr(), F_d.data_ptr(), flags)
+
+    def timed(flags, steps, warmup, sampler=None):
+        for _ in range(warmup):
+            step(flags)
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step(flags)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        return max_over_ranks(e0.elapsed_time(e1) / steps)
+
+    # Accuracy of the mixed assembly against the FP64 one on the same input.
+    step(F64)
+    K64 = K_d.cpu().numpy().copy(); F64v = F_d.cpu().numpy().copy()
+    step(MIX)
+    Km = K_d.cpu().numpy(); Fm = F_d.cpu().numpy()
+    err = {"F_rel_inf": float(np.abs(Fm - F64v).max() / np.abs(F64v).max()),
+           "K_rel_fro": float(np.linalg.norm(Km - K64) / np.linalg.norm(K64)),
+           "K_rel_max": float(np.abs(Km - K64).max() / np.abs(K64).max())}
+    del K64
+
+    W = max(args.warmup, 3)
+    with ClockSampler(local) as clk:
+        ms_mix = timed(MIX, args.steps, W)
+    clocks = clk.summary()
+    ms_f64 = timed(F64, max(3, args.steps // 4), 3)
+    ms_det = timed(DET, max(3, args.steps // 4), 3)
+
+    # Per-phase device times of the mixed step (events inside the library).
+    ctx.profile(True)
+    ctx.profile_read(reset=True)
+    for _ in range(args.steps):
+        step(MIX)
+    torch.cuda.synchronize()
+    ph_ms, ph_n = ctx.profile_read(reset=True)
+    for _ in range(max(3, args.steps // 4)):
+        step(F64)
+    torch.cuda.synchronize()
+    ph64_ms, ph64_n = ctx.profile_read(reset=True)
+    ctx.profile(False)
+    launches_per_step = int(sum(ph_n.values())) // max(args.steps, 1)
+
+    # End to end through the public API with pinned host buffers: x in, K and F out.
+    x_h = torch.empty(asm.n_dofs, dtype=torch.float64, pin_memory=True).numpy()
+    x_h[:] = x
+    K_h = torch.empty(asm.nnz, dtype=torch.float64, pin_memory=True).numpy()
+    F_h = torch.empty(asm.n_dofs, dtype=torch.float64, pin_memory=True).numpy()
+    for _ in range(W):
+        asm.assemble(x_h, MIX, K_out=K_h, F_out=F_h)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        asm.assemble(x_h, MIX, K_out=K_h, F_out=F_h)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
+    barrier()
+
+    # Roofline of the dominant kernel (face kernel, mixed).
+    ptr = model.faces.download()["ptr"]
+    n = np.diff(ptr).astype(np.float64)
+    face_ms = ph_ms["face"] / max(ph_n["face"], 1)
+    # Compulsory bytes per launch: neighbour ids 4n, grad/Hessian Phi 40n (FP64), slot
+    # map 4 n(n+1)/2, F 24n, and the FP32 block accumulator written once.
+    alg_bytes = float((4 * n + 40 * n + 2 * n * (n + 1) + 24 * n).sum() + 36.0 * asm.nnz / 9.0)
+    flops_fp64 = float((121 * n + 200).sum())                 # residual path (FP64)
+    flops_total = float((181 * n * (n + 1) / 2 + 364 * n + 200).sum())
+    flops_fp32 = flops_total - flops_fp64
+    peaks, peak_kind = measured_peaks()
+    p64, p32 = fma_peaks(local)
+    achieved_gbs = alg_bytes / (face_ms * 1e-3) / 1e9
+    roofline = {
+        "bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,
+        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+        "kernel": "face_kernel<float, atomic, tangent>", "launch_ms": face_ms,
+        "algorithmic_bytes_per_launch": alg_bytes,
+        "pipes": {
+            "fp64": {"achieved_tflops": flops_fp64 / (face_ms * 1e-3) / 1e12, "peak_tflops": p64,
+                     "frac": flops_fp64 / (face_ms * 1e-3) / 1e12 / p64 if p64 > 0 else None,
+                     "flops_per_launch": flops_fp64, "peak_source": "measured live (FMA probe)"},
+            "fp32": {"achieved_tflops": flops_fp32 / (face_ms * 1e-3) / 1e12, "peak_tflops": p32,
+                     "frac": flops_fp32 / (face_ms * 1e-3) / 1e12 / p32 if p32 > 0 else None,
+                     "flops_per_launch": flops_fp32, "peak_source": "measured live (FMA probe)"},
+        },
+    }
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        S = cpu_sample(plate, x, args.cpu_sample_rows)
+        cores = os.cpu_count() or 1
+        t_all = cpu_time(S, cores, 2)
+        cpu = {"value": S["n_gp"] / t_all, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": (f"first {args.cpu_sample_rows} of 200 cell rows ({S['n_gp']} Gauss points, own "
+                          f"pattern and hinge points), updateStiffness + evaluateElasticFold, OpenMP "
+                          f"restatement built with the reference's -O2 native flags, mean of 2 runs")}
+
+    v_mix = world * n_gp / (ms_mix * 1e-3)
+    v_f64 = world * n_gp / (ms_f64 * 1e-3)
+    line = {
+        "metric": METRIC, "value": v_mix, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": W, "ms_per_step": ms_mix, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp64 residual + fp32 tangent",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": WORKLOAD, "seed": SEED, "n_gauss_points": n_gp, "n_nodes": plate.n_nodes,
+                   "nnz_K": asm.nnz, "mean_neighbours": float(n.mean()), "max_neighbours": int(n.max()),
+                   "precision": "mixed", "scatter": "atomic",
+                   "l2": "inputs larger than L2 every step (grad/Hessian Phi 0.73 GB + slot map 1.0 GB)",
+                   "setup_s": setup_s},
+        "fp64": {"value": v_f64, "ms_per_step": ms_f64, "mixed_over_fp64": ms_f64 / ms_mix,
+                 "phases_ms": {k: v / max(3, args.steps // 4) for k, v in ph64_ms.items()}},
+        "deterministic_mixed": {"value": world * n_gp / (ms_det * 1e-3), "ms_per_step": ms_det},
+        "error_mixed_vs_fp64": err,
+        "phases_ms": {k: v / max(args.steps, 1) for k, v in ph_ms.items()},
+        "e2e": {"value": world * n_gp / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": int(asm.n_dofs * 8),
+                "d2h_bytes_per_step": int(asm.nnz * 8 + asm.n_dofs * 8)},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -694,6 +694,7 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
 
   const int64_t ndof = 3 * static_cast<int64_t>(a->n_nodes);
   // Accumulators.
+  prof_begin(ctx, CGB_PHASE_ZERO);
   if (!det) CGB_CUDA(cudaMemsetAsync(d_F, 0, ndof * sizeof(double), st));
   if (want_K && !det) {
     if (mixed) {
@@ -720,6 +721,8 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     }
   }
 
+  prof_end(ctx, CGB_PHASE_ZERO, 0);
+
   // Face kernel.
   FaceArgs fa{};
   fa.n_gp = S->n_gp;
@@ -740,7 +743,9 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   const unsigned grid = std::max(1u, std::min(nb(S->n_gp, kFaceWarps), static_cast<unsigned>(sms * 16)));
   auto launch = [&](auto kern) {
     if (smem > 48 * 1024) CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    prof_begin(ctx, CGB_PHASE_FACE);
     if (S->n_gp) kern<<<grid, 32 * kFaceWarps, smem, st>>>(fa);
+    prof_end(ctx, CGB_PHASE_FACE, S->n_gp ? 1 : 0);
   };
   if (mixed) {
     if (det) { if (want_K) launch(face_kernel<float, true, true>); else launch(face_kernel<float, true, false>); }
@@ -753,6 +758,8 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
 
   // Hinge.
   if (hinge) {
+    prof_begin(ctx, CGB_PHASE_HINGE);
+    int nl = 0;
     int64_t kb = a->hinge_pair_base, fb = a->hinge_f_base;
     for (auto& f : a->folds) {
       if (f.n_gp == 0) continue;
@@ -768,23 +775,30 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
       if (hs > 48 * 1024) CGB_CUDA(cudaFuncSetAttribute(hinge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(hs)));
       hinge_kernel<<<nb(f.n_gp, kHingeWarps), 32 * kHingeWarps, hs, st>>>(h);
       CGB_CUDA(cudaGetLastError());
+      ++nl;
       kb += f.n_pairs;
       fb += f.n_u;
     }
+    prof_end(ctx, CGB_PHASE_HINGE, nl);
   }
 
   // Reductions / output.
   const unsigned cg = std::max(1u, std::min(nb(a->n_nodes, 4), static_cast<unsigned>(sms * 32)));
+  prof_begin(ctx, CGB_PHASE_REDUCE);
+  int nred = 0;
   if (det) {
+    nred = want_K ? 2 : 1;
     det_reduce_F<<<nb(a->n_nodes, 128), 128, 0, st>>>(a->n_nodes, a->node_list_ptr.p, a->node_list.p, a->fcontrib.p, d_F);
     if (want_K) {
       if (mixed) det_reduce_blocks<float><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->blk_list_ptr.p, a->blk_list.p, a->contrib32.p, d_K);
       else det_reduce_blocks<double><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->blk_list_ptr.p, a->blk_list.p, a->contrib64.p, d_K);
     }
   } else if (want_K) {
+    nred = 1;
     if (mixed) blocks_to_csc<float, 12><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->kacc32.p, d_K);
     else blocks_to_csc<double, 9><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->kacc64.p, d_K);
   }
+  prof_end(ctx, CGB_PHASE_REDUCE, nred);
   CGB_CUDA(cudaGetLastError());
 }
 

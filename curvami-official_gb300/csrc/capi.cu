@@ -37,9 +37,78 @@ void need(bool ok, const char* msg) {
 
 void bind_device(cgb_context* ctx) { CGB_CUDA(cudaSetDevice(ctx->device)); }
 
+cudaEvent_t take_event(cgb_context* ctx) {
+  if (!ctx->event_pool.empty()) {
+    cudaEvent_t e = ctx->event_pool.back();
+    ctx->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  CGB_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+void collect_marks(cgb_context* ctx) {
+  for (auto& m : ctx->marks) {
+    if (m.stop) {
+      CGB_CUDA(cudaEventSynchronize(m.stop));
+      float ms = 0.0f;
+      CGB_CUDA(cudaEventElapsedTime(&ms, m.start, m.stop));
+      ctx->prof_ms[m.phase] += ms;
+      ctx->prof_launches[m.phase] += m.launches;
+      ctx->event_pool.push_back(m.stop);
+    }
+    ctx->event_pool.push_back(m.start);
+  }
+  ctx->marks.clear();
+}
+
 }  // namespace
 
+namespace cgb {
+void prof_begin(cgb_context* ctx, int phase) {
+  if (!ctx->profile) return;
+  cgb_context::Mark m{phase, take_event(ctx), nullptr, 0};
+  CGB_CUDA(cudaEventRecord(m.start, ctx->stream));
+  ctx->marks.push_back(m);
+}
+void prof_end(cgb_context* ctx, int phase, int launches) {
+  if (!ctx->profile) return;
+  for (auto it = ctx->marks.rbegin(); it != ctx->marks.rend(); ++it) {
+    if (it->phase == phase && !it->stop) {
+      it->stop = take_event(ctx);
+      it->launches = launches;
+      CGB_CUDA(cudaEventRecord(it->stop, ctx->stream));
+      break;
+    }
+  }
+  if (ctx->marks.size() > 4096) collect_marks(ctx);
+}
+}  // namespace cgb
+
 extern "C" {
+
+int cgb_profile_enable(cgb_context* ctx, int on) {
+  if (!ctx) return CGB_ERR_INVALID;
+  return guarded(ctx, [&] {
+    bind_device(ctx);
+    if (!on) collect_marks(ctx);
+    ctx->profile = on != 0;
+  });
+}
+
+int cgb_profile_read(cgb_context* ctx, double* ms, int64_t* launches, int reset) {
+  if (!ctx) return CGB_ERR_INVALID;
+  return guarded(ctx, [&] {
+    bind_device(ctx);
+    collect_marks(ctx);
+    for (int p = 0; p < CGB_N_PHASES; ++p) {
+      if (ms) ms[p] = ctx->prof_ms[p];
+      if (launches) launches[p] = ctx->prof_launches[p];
+      if (reset) { ctx->prof_ms[p] = 0.0; ctx->prof_launches[p] = 0; }
+    }
+  });
+}
 
 int cgb_create(int device, cgb_context** out) {
   if (!out) return CGB_ERR_INVALID;
@@ -74,6 +143,11 @@ int cgb_destroy(cgb_context* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->node_xy.reset();
   ctx->dev_err.reset();
+  for (auto& m : ctx->marks) {
+    if (m.start) cudaEventDestroy(m.start);
+    if (m.stop) cudaEventDestroy(m.stop);
+  }
+  for (auto e : ctx->event_pool) cudaEventDestroy(e);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return CGB_OK;
@@ -368,10 +442,14 @@ int cgb_assemble(cgb_assembler* a, const double* x, double* K_values, double* F,
     const size_t nnz = 9 * static_cast<size_t>(a->n_blocks);
     const bool want_K = (flags & CGB_TANGENT) != 0;
     if (want_K) a->K.ensure(nnz);
+    cgb::prof_begin(ctx, CGB_PHASE_H2D);
     CGB_CUDA(cudaMemcpyAsync(a->x.p, x, ndof * sizeof(double), cudaMemcpyHostToDevice, st));
+    cgb::prof_end(ctx, CGB_PHASE_H2D, 0);
     cgb::assemble_device(a, a->x.p, want_K ? a->K.p : nullptr, a->F.p, flags);
+    cgb::prof_begin(ctx, CGB_PHASE_D2H);
     if (want_K) CGB_CUDA(cudaMemcpyAsync(K_values, a->K.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, st));
     CGB_CUDA(cudaMemcpyAsync(F, a->F.p, ndof * sizeof(double), cudaMemcpyDeviceToHost, st));
+    cgb::prof_end(ctx, CGB_PHASE_D2H, 0);
     CGB_CUDA(cudaStreamSynchronize(st));
   });
 }

@@ -82,6 +82,13 @@ struct cgb_context {
   // Device-side error word written by kernels (bounds checks, capacity).
   cgb::DevBuf<int> dev_err;
   int* h_err = nullptr;  // pinned mirror
+  // Tracing: event pairs per phase, summed when read.
+  bool profile = false;
+  struct Mark { int phase; cudaEvent_t start, stop; int launches; };
+  std::vector<Mark> marks;
+  std::vector<cudaEvent_t> event_pool;
+  double prof_ms[CGB_N_PHASES] = {0};
+  int64_t prof_launches[CGB_N_PHASES] = {0};
 };
 
 struct cgb_shape {
@@ -162,6 +169,9 @@ struct cgb_assembler {
 };
 
 namespace cgb {
+// Tracing helpers (capi.cu): no-ops unless profiling is enabled on the context.
+void prof_begin(cgb_context* ctx, int phase);
+void prof_end(cgb_context* ctx, int phase, int launches);
 // shape.cu
 void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shape_params& prm,
                  const std::vector<Crease>& creases, cgb_shape* out);

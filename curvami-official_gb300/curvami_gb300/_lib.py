@@ -50,7 +50,11 @@ SIGNATURES = {
     "cgb_assemble": (i32, [vp, vp, vp, vp, i32]),
     "cgb_assemble_device": (i32, [vp, vp, vp, vp, i32]),
     "cgb_energies": (i32, [vp, vp, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(dbl)]),
+    "cgb_profile_enable": (i32, [vp, i32]),
+    "cgb_profile_read": (i32, [vp, vp, vp, i32]),
 }
+
+PHASES = ("h2d", "zero", "face", "hinge", "reduce", "d2h")
 
 
 class Crease(C.Structure):

@@ -51,6 +51,20 @@ class Context:
     def synchronize(self):
         self.check(self.lib.cgb_synchronize(self.h))
 
+    def set_stream(self, stream_ptr: int):
+        """Launch on the caller's cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
+        self.check(self.lib.cgb_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    def profile(self, on: bool):
+        self.check(self.lib.cgb_profile_enable(self.h, int(bool(on))))
+
+    def profile_read(self, reset: bool = True):
+        """Per-phase device ms and kernel launches since the last reset."""
+        ms = np.zeros(len(L.PHASES))
+        n = np.zeros(len(L.PHASES), np.int64)
+        self.check(self.lib.cgb_profile_read(self.h, _p(ms), _p(n), int(bool(reset))))
+        return dict(zip(L.PHASES, ms)), dict(zip(L.PHASES, n))
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.cgb_destroy(self.h)

@@ -157,6 +157,23 @@ int cgb_assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double
 int cgb_energies(cgb_assembler* a, const double* x, double* E_mem, double* E_ben,
                  double* E_hin);
 
+/* ---- tracing (library extension; the reference only prints wall-clock times) ------ */
+/* CUDA events around every phase of cgb_assemble / cgb_assemble_device, summed per
+ * phase until read. Off by default; costs two event records per phase when on. */
+enum {
+  CGB_PHASE_H2D = 0,    /* x host -> device (cgb_assemble only) */
+  CGB_PHASE_ZERO = 1,   /* clearing of the accumulators */
+  CGB_PHASE_FACE = 2,   /* face Gauss points: residual, tangent, scatter */
+  CGB_PHASE_HINGE = 3,  /* elastic hinge */
+  CGB_PHASE_REDUCE = 4, /* block -> CSC output, or the deterministic reductions */
+  CGB_PHASE_D2H = 5,    /* K, F device -> host (cgb_assemble only) */
+  CGB_N_PHASES = 6
+};
+int cgb_profile_enable(cgb_context* ctx, int on);
+/* ms[CGB_N_PHASES] summed device time, launches[CGB_N_PHASES] kernels launched by the
+ * library in each phase; reset != 0 clears the totals after reading. */
+int cgb_profile_read(cgb_context* ctx, double* ms, int64_t* launches, int reset);
+
 #ifdef __cplusplus
 }
 #endif

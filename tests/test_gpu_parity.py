@@ -1,0 +1,300 @@
+"""GPU parity: the sm_103a library through its C ABI against the CPU oracle.
+
+Bars: neighbour sets, distances, the K pattern and the Gauss-point -> CSC map bit-exact;
+FP64 shape functions to 1e-12 of each array's scale where the supports are well
+conditioned (crease-truncated supports are ill-conditioned, looser bound stated); the
+FP64 assembly on identical shape functions to 1e-13; the mixed assembly's residual to
+1e-12 (the metric requires <= 1e-10) and its tangent to 1e-5 (FP32); the deterministic
+scatter bitwise run to run.
+"""
+import numpy as np
+import pytest
+
+import curvami_gb300 as cg
+from curvami_gb300 import synth
+from oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def o():
+    return Oracle()
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import __graft_entry__ as ge
+
+    ge.build()
+    c = cg.Context(0)
+    yield c
+
+
+def rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-300))
+
+
+def oracle_shapes(o, p, pts):
+    ptr, idx, s = o.frnn(p.node_xy, pts, p.rho, p.rho_node)
+    psi, dpsi, ddpsi, bad, rc = o.rkpm(p.node_xy, pts, ptr, idx, s, p.rho, p.order, p.creases, p.rho_node,
+                                       p.kernel)
+    return dict(ptr=ptr, idx=idx, s=s, psi=psi, dpsi=dpsi, ddpsi=ddpsi, bad=bad, rc=rc)
+
+
+SHAPE_CASES = {
+    "row_r3_quartic": lambda: synth.square_plate(21, 0.5, 3, crease="row", seed=1),
+    "arc_r4_jitter": lambda: synth.square_plate(25, 0.5, 4, jitter=0.1, crease="arc", seed=2),
+    "nocrease_order1": lambda: synth.square_plate(15, 0.5, 3, jitter=0.05, crease=None, order=1, seed=3),
+    "nocrease_order3": lambda: synth.square_plate(15, 0.5, 3, jitter=0.05, crease=None, order=3,
+                                                  rho_factor=4.5, seed=3),
+    "cubic_bspline": lambda: synth.square_plate(15, 0.5, 4, jitter=0.05, crease="row", kernel=1, seed=4),
+}
+
+
+@pytest.mark.parametrize("name", sorted(SHAPE_CASES))
+def test_shape_functions(o, ctx, name):
+    p = SHAPE_CASES[name]()
+    ctx.set_nodes(p.node_xy)
+    sh = cg.shape_functions(ctx, p.faces.xy, p.rho, p.order, p.creases, p.rho_node, p.kernel).download()
+    ref = oracle_shapes(o, p, p.faces.xy)
+    assert np.array_equal(sh["ptr"], ref["ptr"])
+    assert np.array_equal(sh["idx"], ref["idx"])
+    assert np.array_equal(sh["s"], ref["s"])
+    tol = 1e-12 if p.creases == [] else 1e-10
+    for k in ("psi", "dpsi", "ddpsi"):
+        assert rel(sh[k], ref[k]) < tol, k
+
+
+def test_shape_functions_per_node_radius(o, ctx):
+    plate, pts = synth.config_shape_points(n_points=20000, n_side=61, per_node_rho=True, seed=11)
+    ctx.set_nodes(plate.node_xy)
+    sh = cg.shape_functions(ctx, pts, plate.rho, 2, plate.creases, plate.rho_node, 0).download()
+    ref = oracle_shapes(o, plate, pts)
+    assert np.array_equal(sh["ptr"], ref["ptr"]) and np.array_equal(sh["idx"], ref["idx"])
+    assert np.array_equal(sh["s"], ref["s"])
+    for k in ("psi", "dpsi", "ddpsi"):
+        assert rel(sh[k], ref[k]) < 1e-9, k
+
+
+def test_empty_and_isolated_points(o, ctx):
+    p = synth.square_plate(9, 0.5, 2, crease=None)
+    ctx.set_nodes(p.node_xy)
+    sh = cg.shape_functions(ctx, np.zeros((0, 2)), p.rho, 2)
+    assert sh.n_gp == 0 and sh.nnz == 0
+    with pytest.raises(cg.CGBError) as e:  # no neighbours: singular moment matrix
+        cg.shape_functions(ctx, np.array([[100.0, 100.0]]), p.rho, 2)
+    assert e.value.code == 3 and "singular moment matrix" in str(e.value)
+
+
+def test_singular_support_message(ctx):
+    nodes = np.array([[0.0, 0.0], [0.5, 0.0], [1.0, 0.0]])
+    ctx.set_nodes(nodes)
+    with pytest.raises(cg.CGBError) as e:
+        cg.shape_functions(ctx, np.array([[0.5, 0.0]]), 1.5, 2)
+    assert e.value.code in (3, 4)
+    assert str(e.value).startswith("RKPM:")
+
+
+# ---- assembly ---------------------------------------------------------------------------
+
+class Case:
+    """A plate with GPU shape functions for folds, oracle shape functions uploaded for the
+    faces (so both sides assemble from identical inputs), and the oracle's K and F."""
+
+    def __init__(self, o, ctx, p, x):
+        self.p, self.x = p, x
+        ctx.set_nodes(p.node_xy)
+        self.model = cg.PlateModel(p, ctx)
+        self.ref = oracle_shapes(o, p, p.faces.xy)
+        r = self.ref
+        self.faces_o = cg.shape_from_host(ctx, r["ptr"], r["idx"], r["dpsi"], r["ddpsi"], r["psi"])
+        self.asm = cg.NonLinearAssembler(ctx, self.faces_o, p.faces.weight, self.model.fold_specs)
+        self.asm.set_material(*cg.abd_isotropic(p.E, p.nu, p.thickness))
+        self.folds = []
+        for (L, R), f in zip(self.model.fold_sets, p.folds):
+            dl, dr = L.download(), R.download()
+            self.folds.append({"left": {"ptr": dl["ptr"], "idx": dl["idx"], "dpsi": dl["dpsi"]},
+                               "right": {"ptr": dr["ptr"], "idx": dr["idx"], "dpsi": dr["dpsi"]},
+                               "weight": f.left.weight, "tangent": f.left.tangent, "Kt": f.Kt,
+                               "theta0": f.theta0})
+        (self.outer, self.inner, self.col_ptr, self.col_nodes,
+         self.mp) = o.pattern(p.n_nodes, r["ptr"], r["idx"], self.folds)
+        self.A, self.B, self.D = o.abd(p.E, p.nu, p.thickness)
+        self.o = o
+
+    def oracle(self, x, hinge=True, exact=False, want_K=True):
+        r = self.ref
+        K, F = self.o.update_stiffness(self.p.n_nodes, self.p.faces.weight, r["ptr"], r["idx"], r["dpsi"],
+                                       r["ddpsi"], self.outer, self.mp, x, self.A, self.B, self.D,
+                                       want_K=want_K)
+        if hinge:
+            K, F = self.o.hinge(self.p.n_nodes, x, self.folds, self.outer, self.col_ptr, self.col_nodes,
+                                K, F, exact_tangent=exact)
+        return K, F
+
+
+@pytest.fixture(scope="module")
+def arc_case(o, ctx):
+    p = synth.square_plate(23, 0.5, 4, jitter=0.08, seed=21, crease="arc", Kt=1e-3)
+    x = 0.3 * synth.fourier_field(p.node_xy, np.random.default_rng(22), lam=(3.0, 10.0))
+    return Case(o, ctx, p, x)
+
+
+@pytest.fixture(scope="module")
+def row_case(o, ctx):
+    p = synth.config_smallplate(rule=3)
+    x = 0.2 * synth.fourier_field(p.node_xy, np.random.default_rng(23), lam=(5.0, 20.0))
+    return Case(o, ctx, p, x)
+
+
+@pytest.mark.parametrize("which", ["arc", "row"])
+def test_pattern_and_map_bit_exact(which, arc_case, row_case):
+    c = arc_case if which == "arc" else row_case
+    outer, inner = c.asm.pattern()
+    assert np.array_equal(outer, c.outer) and np.array_equal(inner, c.inner)
+    assert np.array_equal(c.asm.csr_mapping(), c.mp)
+    # the GPU-built shape set gives the same pattern
+    o2, i2 = c.model.asm.pattern()
+    assert np.array_equal(o2, c.outer) and np.array_equal(i2, c.inner)
+
+
+@pytest.mark.parametrize("which", ["arc", "row"])
+@pytest.mark.parametrize("det", [False, True])
+def test_fp64_assembly(which, det, arc_case, row_case):
+    c = arc_case if which == "arc" else row_case
+    Ko, Fo = c.oracle(c.x)
+    fl = cg.TANGENT | cg.HINGE | (cg.DETERMINISTIC if det else 0)
+    K, F = c.asm.assemble(c.x, fl)
+    assert rel(K, Ko) < 1e-13
+    assert rel(F, Fo) < 1e-13
+
+
+@pytest.mark.parametrize("det", [False, True])
+def test_mixed_assembly(det, arc_case):
+    c = arc_case
+    Ko, Fo = c.oracle(c.x)
+    fl = cg.TANGENT | cg.HINGE | cg.MIXED | (cg.DETERMINISTIC if det else 0)
+    K, F = c.asm.assemble(c.x, fl)
+    assert rel(F, Fo) < 1e-12  # FP64 residual
+    assert rel(K, Ko) < 1e-5   # FP32 tangent
+    assert np.linalg.norm(K - Ko) / np.linalg.norm(Ko) < 1e-6
+
+
+def test_residual_only_matches(arc_case):
+    c = arc_case
+    _, F_full = c.asm.assemble(c.x, cg.TANGENT | cg.HINGE)
+    _, F_res = c.asm.assemble(c.x, cg.HINGE)
+    assert np.array_equal(F_full, F_res)
+    _, Fo = c.oracle(c.x, want_K=False)
+    assert rel(F_res, Fo) < 1e-13
+
+
+def test_no_hinge_flag(arc_case):
+    c = arc_case
+    Ko, Fo = c.oracle(c.x, hinge=False)
+    K, F = c.asm.assemble(c.x, cg.TANGENT)
+    assert rel(K, Ko) < 1e-13 and rel(F, Fo) < 1e-13
+
+
+def test_exact_hinge_tangent(arc_case):
+    c = arc_case
+    Ko, Fo = c.oracle(c.x, exact=True)
+    K, F = c.asm.assemble(c.x, cg.TANGENT | cg.HINGE | cg.HINGE_EXACT)
+    # the Hessian is a central difference of the gradient (step 1e-6), so the two
+    # implementations agree to the difference stencil's sensitivity, not to round-off
+    assert rel(K, Ko) < 1e-9 and rel(F, Fo) < 1e-13
+
+
+def test_deterministic_bitwise(arc_case):
+    c = arc_case
+    for fl in (cg.TANGENT | cg.HINGE | cg.DETERMINISTIC, cg.TANGENT | cg.HINGE | cg.MIXED | cg.DETERMINISTIC):
+        K1, F1 = c.asm.assemble(c.x, fl)
+        K2, F2 = c.asm.assemble(c.x, fl)
+        assert np.array_equal(K1, K2) and np.array_equal(F1, F2)
+
+
+def test_tangent_check_on_gpu(arc_case):
+    """main.cpp:651-710 on the GPU's own residual and tangent."""
+    import scipy.sparse as sp
+
+    c = arc_case
+    n = 3 * c.p.n_nodes
+    for mixed, bound in ((False, 1e-6), (True, 1e-5)):
+        fl = cg.TANGENT | cg.HINGE | cg.HINGE_EXACT | (cg.MIXED if mixed else 0)
+        K, _ = c.asm.assemble(c.x, fl)
+        Kd = sp.csc_matrix((K, c.inner, c.outer), shape=(n, n)).toarray()
+        U = np.triu(Kd)
+        Ks = U + U.T - np.diag(np.diag(Kd))
+        rng = np.random.default_rng(12345)
+        h = 1e-6 * max(1.0, abs(c.x).max())
+        worst = 0.0
+        for _ in range(3):
+            v = rng.uniform(-1, 1, n)
+            v /= np.linalg.norm(v)
+            _, Fp = c.asm.assemble(c.x + h * v, cg.HINGE)
+            _, Fm = c.asm.assemble(c.x - h * v, cg.HINGE)
+            fd = (Fp - Fm) / (2 * h)
+            worst = max(worst, np.linalg.norm(fd - Ks @ v) / np.linalg.norm(fd))
+        assert worst < bound, (mixed, worst)
+
+
+def test_energies(arc_case):
+    c = arc_case
+    r = c.ref
+    em, eb = c.o.strain_energies(c.p.faces.weight, r["ptr"], r["idx"], r["dpsi"], r["ddpsi"], c.x, c.A, c.B, c.D)
+    eh = c.o.hinge_energy(c.x, c.folds)
+    g = c.asm.energies(c.x)
+    assert abs(g[0] - em) <= 1e-12 * abs(em)
+    assert abs(g[1] - eb) <= 1e-12 * abs(eb)
+    assert abs(g[2] - eh) <= 1e-12 * abs(eh)
+
+
+def test_inactive_crease_points_and_rest_angles(o, ctx):
+    p = synth.square_plate(17, 0.5, 3, seed=31, crease="row", Kt=5e-3)
+    x = 0.2 * synth.fourier_field(p.node_xy, np.random.default_rng(3), lam=(3.0, 9.0))
+    ctx.set_nodes(p.node_xy)
+    model = cg.PlateModel(p, ctx)
+    nf = len(p.folds[0].left.xy)
+    rng = np.random.default_rng(4)
+    active = (rng.uniform(size=nf) > 0.3).astype(np.int8)
+    theta0 = rng.uniform(-0.2, 0.2, nf)
+    spec = dict(model.fold_specs[0], active=active, theta0_gp=theta0)
+    asm = cg.NonLinearAssembler(ctx, model.faces, p.faces.weight, [spec])
+    asm.set_material(*cg.abd_isotropic(p.E, p.nu, p.thickness))
+    K, F = asm.assemble(x, cg.TANGENT | cg.HINGE)
+    Kd, Fd = asm.assemble(x, cg.TANGENT | cg.HINGE | cg.DETERMINISTIC)
+    sh = model.faces.download()
+    (L, R) = model.fold_sets[0]
+    dl, dr = L.download(), R.download()
+    folds = [{"left": {"ptr": dl["ptr"], "idx": dl["idx"], "dpsi": dl["dpsi"]},
+              "right": {"ptr": dr["ptr"], "idx": dr["idx"], "dpsi": dr["dpsi"]},
+              "weight": p.folds[0].left.weight, "tangent": p.folds[0].left.tangent, "Kt": 5e-3,
+              "active": active, "theta0_gp": theta0}]
+    outer, inner, col_ptr, col_nodes, mp = o.pattern(p.n_nodes, sh["ptr"], sh["idx"], folds)
+    A, B, D = o.abd(p.E, p.nu, p.thickness)
+    Ko, Fo = o.update_stiffness(p.n_nodes, p.faces.weight, sh["ptr"], sh["idx"], sh["dpsi"], sh["ddpsi"],
+                                outer, mp, x, A, B, D)
+    Ko, Fo = o.hinge(p.n_nodes, x, folds, outer, col_ptr, col_nodes, Ko, Fo)
+    assert rel(K, Ko) < 1e-13 and rel(F, Fo) < 1e-13
+    assert rel(Kd, Ko) < 1e-13 and rel(Fd, Fo) < 1e-13
+
+
+def test_full_size_properties(ctx):
+    """At the benchmark's full size (640,000 Gauss points): mixed vs FP64 residual within
+    the metric's 1e-10, atomic vs deterministic agreement, residual-only consistency."""
+    p = synth.config_assembly()
+    x = synth.fourier_field(p.node_xy, np.random.default_rng(1004))
+    ctx.set_nodes(p.node_xy)
+    m = cg.PlateModel(p, ctx)
+    assert m.faces.n_gp == 640000
+    K64, F64 = m.asm.assemble(x, cg.TANGENT | cg.HINGE)
+    Kmx, Fmx = m.asm.assemble(x, cg.TANGENT | cg.HINGE | cg.MIXED)
+    Kd, Fd = m.asm.assemble(x, cg.TANGENT | cg.HINGE | cg.DETERMINISTIC)
+    assert rel(Fmx, F64) <= 1e-10
+    assert np.linalg.norm(Kmx - K64) / np.linalg.norm(K64) < 1e-6
+    assert rel(Kd, K64) < 1e-12 and rel(Fd, F64) < 1e-12
+    _, Fr = m.asm.assemble(x, cg.HINGE | cg.MIXED)
+    assert np.array_equal(Fr, Fmx)
+    # K's checksum is independent of the scatter order up to round-off
+    assert abs(Kd.sum() - K64.sum()) <= 1e-10 * np.abs(K64).sum()
