@@ -299,13 +299,20 @@ def square_plate(n_side: int, h: float, rule: int, *, jitter: float = 0.0, seed:
                        "crease": crease, "split": nsplit})
 
 
-def config_smallplate(rule: int = 3, kernel: int = 0, seed: int = 1001) -> Plate:
+def config_smallplate(rule: int = 3, kernel: int = 0, seed: int = 1001,
+                      rho_factor: float = 3.5) -> Plate:
     """Plain FP64 method, small: [0,20]^2, 41x41 nodes (h = 0.5), quadratic basis,
-    support radius 3h, straight elastic hinge on the node column x = 10 (Kt = 1e-3),
-    E = 1, nu = 0.3, t = 0.05. rule 3 / quartic is the reference-exact variant,
-    rule 4 / cubic B-spline the literal one."""
+    straight elastic hinge on the node column x = 10 (Kt = 1e-3), E = 1, nu = 0.3,
+    t = 0.05. rule 3 / quartic is the reference-exact variant, rule 4 / cubic B-spline
+    the literal one.
+
+    The support radius defaults to 3.5h, not 3h: with a crease on a node column and
+    rho = 3h, the crease points on the far side see the node columns at h and 2h only
+    (the column at 3h has weight w(1) = 0), so the quadratic moment matrix is singular
+    there and the reference itself stops with "RKPM: moment-matrix pivot collapsed".
+    """
     return square_plate(41, 0.5, rule, seed=seed, crease="row", Kt=1e-3, kernel=kernel,
-                        name=f"plate41_r{rule}")
+                        rho_factor=rho_factor, name=f"plate41_r{rule}")
 
 
 def config_assembly(rule: int = 4, n_side: int = 201, kernel: int = 0, seed: int = 1003) -> Plate:

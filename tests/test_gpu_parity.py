@@ -42,6 +42,17 @@ def oracle_shapes(o, p, pts):
     return dict(ptr=ptr, idx=idx, s=s, psi=psi, dpsi=dpsi, ddpsi=ddpsi, bad=bad, rc=rc)
 
 
+def crease_distance(p, pts):
+    d = np.full(len(pts), np.inf)
+    for cr in p.creases:
+        V = np.asarray(cr["vertices"])
+        for a, b in zip(V[:-1], V[1:]):
+            v = b - a
+            t = np.clip(((pts - a) @ v) / (v @ v), 0.0, 1.0)
+            d = np.minimum(d, np.linalg.norm(pts - (a + t[:, None] * v), axis=1))
+    return d
+
+
 SHAPE_CASES = {
     "row_r3_quartic": lambda: synth.square_plate(21, 0.5, 3, crease="row", seed=1),
     "arc_r4_jitter": lambda: synth.square_plate(25, 0.5, 4, jitter=0.1, crease="arc", seed=2),
@@ -61,9 +72,13 @@ def test_shape_functions(o, ctx, name):
     assert np.array_equal(sh["ptr"], ref["ptr"])
     assert np.array_equal(sh["idx"], ref["idx"])
     assert np.array_equal(sh["s"], ref["s"])
-    tol = 1e-12 if p.creases == [] else 1e-10
+    # Points whose support a crease truncates have ill-conditioned moment matrices (the
+    # visible nodes lie on one side), so two FP64 evaluations differ there by about
+    # cond(M) * eps; away from the creases the bar is 1e-12.
+    far = np.repeat(crease_distance(p, p.faces.xy) > p.rho, np.diff(ref["ptr"]))
     for k in ("psi", "dpsi", "ddpsi"):
-        assert rel(sh[k], ref[k]) < tol, k
+        assert rel(sh[k][far], ref[k][far]) < 1e-12, k
+        assert rel(sh[k], ref[k]) < 1e-8, k
 
 
 def test_shape_functions_per_node_radius(o, ctx):
@@ -73,8 +88,10 @@ def test_shape_functions_per_node_radius(o, ctx):
     ref = oracle_shapes(o, plate, pts)
     assert np.array_equal(sh["ptr"], ref["ptr"]) and np.array_equal(sh["idx"], ref["idx"])
     assert np.array_equal(sh["s"], ref["s"])
+    far = np.repeat(crease_distance(plate, pts) > 1.75, np.diff(ref["ptr"]))
     for k in ("psi", "dpsi", "ddpsi"):
-        assert rel(sh[k], ref[k]) < 1e-9, k
+        assert rel(sh[k][far], ref[k][far]) < 1e-12, k
+        assert rel(sh[k], ref[k]) < 1e-8, k
 
 
 def test_empty_and_isolated_points(o, ctx):
@@ -183,9 +200,11 @@ def test_mixed_assembly(det, arc_case):
 
 def test_residual_only_matches(arc_case):
     c = arc_case
-    _, F_full = c.asm.assemble(c.x, cg.TANGENT | cg.HINGE)
+    _, F_full = c.asm.assemble(c.x, cg.TANGENT | cg.HINGE | cg.DETERMINISTIC)
+    _, F_res = c.asm.assemble(c.x, cg.HINGE | cg.DETERMINISTIC)
+    assert np.array_equal(F_full, F_res)  # same fixed-order sums with and without K
     _, F_res = c.asm.assemble(c.x, cg.HINGE)
-    assert np.array_equal(F_full, F_res)
+    assert rel(F_res, F_full) < 1e-14     # atomics: same terms, order varies
     _, Fo = c.oracle(c.x, want_K=False)
     assert rel(F_res, Fo) < 1e-13
 
@@ -251,7 +270,7 @@ def test_energies(arc_case):
 
 
 def test_inactive_crease_points_and_rest_angles(o, ctx):
-    p = synth.square_plate(17, 0.5, 3, seed=31, crease="row", Kt=5e-3)
+    p = synth.square_plate(17, 0.5, 3, seed=31, crease="row", Kt=5e-3, rho_factor=3.5)
     x = 0.2 * synth.fourier_field(p.node_xy, np.random.default_rng(3), lam=(3.0, 9.0))
     ctx.set_nodes(p.node_xy)
     model = cg.PlateModel(p, ctx)
@@ -295,6 +314,6 @@ def test_full_size_properties(ctx):
     assert np.linalg.norm(Kmx - K64) / np.linalg.norm(K64) < 1e-6
     assert rel(Kd, K64) < 1e-12 and rel(Fd, F64) < 1e-12
     _, Fr = m.asm.assemble(x, cg.HINGE | cg.MIXED)
-    assert np.array_equal(Fr, Fmx)
+    assert rel(Fr, Fmx) < 1e-14
     # K's checksum is independent of the scatter order up to round-off
     assert abs(Kd.sum() - K64.sum()) <= 1e-10 * np.abs(K64).sum()
