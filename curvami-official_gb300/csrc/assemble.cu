@@ -53,6 +53,8 @@ struct FaceArgs {
   const int32_t* idx;
   const double* dpsi;
   const double* ddpsi;
+  const void* dpsi_t;   // grad / Hessian Phi in the tangent's precision (FP32 copies in mixed mode)
+  const void* ddpsi_t;
   const double* weight;
   const double* x;
   const int64_t* map_ptr;
@@ -171,147 +173,213 @@ __device__ __forceinline__ void store_contrib(void* cbuf, int64_t q, bool flip, 
     for (int c = 0; c < 3; ++c) d[3 * r + c] = flip ? v[3 * c + r] : v[3 * r + c];
 }
 
+// Per-point state handed from the FP64 phase to the pair phase, [field][32] in shared
+// memory: a1(3) a2(3) b(3) r0XX(3) r0YY(3) r0XY(3) C0^-1(4) N(3) M(3) pXY(2) bv W.
+constexpr int kState = 32;
+enum : int { S_A1 = 0, S_A2 = 3, S_B = 6, S_RXX = 9, S_RYY = 12, S_RXY = 15, S_CI = 18, S_N = 22,
+             S_M = 25, S_P = 28, S_BV = 30, S_W = 31 };
+
 template <typename TK, bool DET, bool WANT_K>
 __global__ void __launch_bounds__(32 * kFaceWarps) face_kernel(FaceArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nmax = a.nmax;
-  TK* rec = reinterpret_cast<TK*>(smem_raw) + static_cast<size_t>(w) * kRec * nmax;
-  int* nid = reinterpret_cast<int*>(reinterpret_cast<TK*>(smem_raw) + static_cast<size_t>(kFaceWarps) * kRec * nmax) +
-             w * nmax;
+  TK* base_w = reinterpret_cast<TK*>(smem_raw) + static_cast<size_t>(w) * (kState * 32 + kRec * nmax);
+  TK* st = base_w;                 // [kState][32]
+  TK* rec = base_w + kState * 32;  // [kRec][nmax]
+  int* nid = reinterpret_cast<int*>(reinterpret_cast<TK*>(smem_raw) +
+                                    static_cast<size_t>(kFaceWarps) * (kState * 32 + kRec * nmax)) + w * nmax;
   const Material& m = a.mat;
-  TK At[9], Bt[9], Dt[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) { At[k] = static_cast<TK>(m.A[k]); Bt[k] = static_cast<TK>(m.B[k]); Dt[k] = static_cast<TK>(m.D[k]); }
+  const TK* dpsi_t = static_cast<const TK*>(a.dpsi_t);
+  const TK* ddpsi_t = static_cast<const TK*>(a.ddpsi_t);
 
-  for (int g = blockIdx.x * kFaceWarps + w; g < a.n_gp; g += gridDim.x * kFaceWarps) {
-    const int64_t p0 = a.ptr[g];
-    const int n = static_cast<int>(a.ptr[g + 1] - p0);
-    if (n == 0) continue;  // Assembly.h:208
-    double s[15];
-    kin_sums(lane, p0, n, a.idx, a.dpsi, a.ddpsi, a.x, s);
-    PointState P;
-    point_state(s, m, P);
-    const double W = a.weight[g];
-
-    // ---- per neighbour: residual (FP64) and the pair-loop record ----
-    for (int i = lane; i < n; i += 32) {
-      const int64_t e = p0 + i;
-      const int node = a.idx[e];
-      const double2 d = reinterpret_cast<const double2*>(a.dpsi)[e];
-      const double dxx = a.ddpsi[3 * e], dyy = a.ddpsi[3 * e + 1], dxy = a.ddpsi[3 * e + 2];
-      const double c0 = P.Ci[0] * d.x + P.Ci[1] * d.y;
-      const double c1 = P.Ci[2] * d.x + P.Ci[3] * d.y;
-      double gI[3];
+  // Each warp owns 32 consecutive Gauss points per round.
+  for (int g0 = (blockIdx.x * kFaceWarps + w) * 32; g0 < a.n_gp; g0 += gridDim.x * kFaceWarps * 32) {
+    // ---- phase 1, one Gauss point per lane, FP64: kinematics, resultants, residual.
+    // Every lane does distinct work, so no FP64 issue slot is spent on a redundant or
+    // masked copy (on GB300 an FP64 warp instruction costs the same with 1 or 32 lanes).
+    const int g = g0 + lane;
+    if (g < a.n_gp) {
+      const int64_t p0 = a.ptr[g];
+      const int n = static_cast<int>(a.ptr[g + 1] - p0);
+      double s[15];
 #pragma unroll
-      for (int r = 0; r < 3; ++r) gI[r] = P.a1[r] * c0 + P.a2[r] * c1;
-      const double SXX = P.rxx[0] * gI[0] + P.rxx[1] * gI[1] + P.rxx[2] * gI[2];
-      const double SYY = P.ryy[0] * gI[0] + P.ryy[1] * gI[1] + P.ryy[2] * gI[2];
-      const double SXY = P.rxy[0] * gI[0] + P.rxy[1] * gI[1] + P.rxy[2] * gI[2];
-      const double be0 = -dxx + SXX, be1 = -dyy + SYY, be2 = 2.0 * (-dxy + SXY);
-      // f = (Bm^T N + Bb^T M) W (Assembly.h:249-250).
-      const double fm1 = d.x * P.N[0] + d.y * P.N[2];
-      const double fm2 = d.y * P.N[1] + d.x * P.N[2];
-      const double fbm = be0 * P.M[0] + be1 * P.M[1] + be2 * P.M[2];
-      double f[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) f[c] = (P.a1[c] * fm1 + P.a2[c] * fm2 + P.b[c] * fbm) * W;
-      if (DET) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) a.Fc[3 * e + c] = f[c];
-      } else {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) atomicAdd(a.F + 3 * static_cast<int64_t>(node) + c, f[c]);
+      for (int k = 0; k < 15; ++k) s[k] = 0.0;
+      for (int q = 0; q < n; ++q) {
+        const int64_t e = p0 + q;
+        const int64_t j = a.idx[e];
+        const double u0 = a.x[3 * j], u1 = a.x[3 * j + 1], u2 = a.x[3 * j + 2];
+        const double2 d = reinterpret_cast<const double2*>(a.dpsi)[e];
+        const double dxx = a.ddpsi[3 * e], dyy = a.ddpsi[3 * e + 1], dxy = a.ddpsi[3 * e + 2];
+        s[0] += u0 * d.x; s[1] += u1 * d.x; s[2] += u2 * d.x;
+        s[3] += u0 * d.y; s[4] += u1 * d.y; s[5] += u2 * d.y;
+        s[6] += u0 * dxx; s[7] += u1 * dxx; s[8] += u2 * dxx;
+        s[9] += u0 * dyy; s[10] += u1 * dyy; s[11] += u2 * dyy;
+        s[12] += u0 * dxy; s[13] += u1 * dxy; s[14] += u2 * dxy;
       }
-      if (!WANT_K) continue;
-      // Record in the tangent's precision.
-      const TK dx = static_cast<TK>(d.x), dy = static_cast<TK>(d.y);
-      const TK b0 = static_cast<TK>(be0), b1 = static_cast<TK>(be1), b2 = static_cast<TK>(be2);
-      const TK Tu = static_cast<TK>(d.x * P.pXY[0] + d.y * P.pXY[1] -
-                                    (dxx * P.M[0] + 2.0 * dxy * P.M[2] + dyy * P.M[1]));
-      const TK Wt = static_cast<TK>(W);
-      TK* R = rec + i;
-      R[0 * nmax] = dx; R[1 * nmax] = dy;
-      R[2 * nmax] = b0; R[3 * nmax] = b1; R[4 * nmax] = b2;
-      R[5 * nmax] = Tu;
+      PointState P;
+      point_state(s, m, P);
+      const double W = a.weight[g];
+      // f_I = W (Bm_I^T N + Bb_I^T M) (Assembly.h:249) = W (a1 u1 + a2 u2 + b Tu_I), since
+      // beta_I . M = dPhi_I . pXY - (Phi_XX M0 + 2 Phi_XY M2 + Phi_YY M1) = Tu_I.
+      const double NW0 = P.N[0] * W, NW1 = P.N[1] * W, NW2 = P.N[2] * W;
+      const double MW0 = P.M[0] * W, MW1 = P.M[1] * W, MW2 = 2.0 * P.M[2] * W;
+      const double pW0 = P.pXY[0] * W, pW1 = P.pXY[1] * W;
+      if (n > 0) {
+        for (int q = 0; q < n; ++q) {
+          const int64_t e = p0 + q;
+          const double2 d = reinterpret_cast<const double2*>(a.dpsi)[e];
+          const double dxx = a.ddpsi[3 * e], dyy = a.ddpsi[3 * e + 1], dxy = a.ddpsi[3 * e + 2];
+          const double v1 = d.x * NW0 + d.y * NW2;
+          const double v2 = d.y * NW1 + d.x * NW2;
+          const double tu = d.x * pW0 + d.y * pW1 - (dxx * MW0 + dxy * MW2 + dyy * MW1);
+          double f[3];
 #pragma unroll
-      for (int r = 0; r < 3; ++r) R[(6 + r) * nmax] = static_cast<TK>(gI[r]);
-      // P = A Bm + B Bb, Q = B Bm + D Bb (Assembly.h:255-256), times W:
-      //   P(r,c) = a1_c pa_r + a2_c pb_r + b_c pc_r.
-      TK a1t[3], a2t[3], bt[3];
+          for (int c = 0; c < 3; ++c) f[c] = P.a1[c] * v1 + P.a2[c] * v2 + P.b[c] * tu;
+          if (DET) {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) { a1t[c] = static_cast<TK>(P.a1[c]); a2t[c] = static_cast<TK>(P.a2[c]); bt[c] = static_cast<TK>(P.b[c]); }
+            for (int c = 0; c < 3; ++c) a.Fc[3 * e + c] = f[c];
+          } else {
+            const int64_t node = a.idx[e];
 #pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        const TK pa = (At[3 * r] * dx + At[3 * r + 2] * dy) * Wt;
-        const TK pb = (At[3 * r + 1] * dy + At[3 * r + 2] * dx) * Wt;
-        const TK pc = (Bt[3 * r] * b0 + Bt[3 * r + 1] * b1 + Bt[3 * r + 2] * b2) * Wt;
-        const TK qa = (Bt[3 * r] * dx + Bt[3 * r + 2] * dy) * Wt;
-        const TK qb = (Bt[3 * r + 1] * dy + Bt[3 * r + 2] * dx) * Wt;
-        const TK qc = (Dt[3 * r] * b0 + Dt[3 * r + 1] * b1 + Dt[3 * r + 2] * b2) * Wt;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          R[(kRecI + 3 * r + c) * nmax] = a1t[c] * pa + a2t[c] * pb + bt[c] * pc;
-          R[(kRecI + 9 + 3 * r + c) * nmax] = a1t[c] * qa + a2t[c] * qb + bt[c] * qc;
+            for (int c = 0; c < 3; ++c) atomicAdd(a.F + 3 * node + c, f[c]);
+          }
         }
       }
-      R[(kRecI + 18) * nmax] = static_cast<TK>(c0 * W);
-      R[(kRecI + 19) * nmax] = static_cast<TK>(c1 * W);
-      R[(kRecI + 20) * nmax] = static_cast<TK>((P.N[0] * d.x + P.N[2] * d.y) * W);
-      R[(kRecI + 21) * nmax] = static_cast<TK>((P.N[2] * d.x + P.N[1] * d.y) * W);
-      R[(kRecI + 22) * nmax] = Tu * Wt;
-      nid[i] = node;
+      if (WANT_K) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          st[(S_A1 + c) * 32 + lane] = static_cast<TK>(P.a1[c]);
+          st[(S_A2 + c) * 32 + lane] = static_cast<TK>(P.a2[c]);
+          st[(S_B + c) * 32 + lane] = static_cast<TK>(P.b[c]);
+          st[(S_RXX + c) * 32 + lane] = static_cast<TK>(P.rxx[c]);
+          st[(S_RYY + c) * 32 + lane] = static_cast<TK>(P.ryy[c]);
+          st[(S_RXY + c) * 32 + lane] = static_cast<TK>(P.rxy[c]);
+          st[(S_N + c) * 32 + lane] = static_cast<TK>(P.N[c]);
+          st[(S_M + c) * 32 + lane] = static_cast<TK>(P.M[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) st[(S_CI + c) * 32 + lane] = static_cast<TK>(P.Ci[c]);
+        st[(S_P + 0) * 32 + lane] = static_cast<TK>(P.pXY[0]);
+        st[(S_P + 1) * 32 + lane] = static_cast<TK>(P.pXY[1]);
+        st[S_BV * 32 + lane] = static_cast<TK>(P.bv);
+        st[S_W * 32 + lane] = static_cast<TK>(W);
+      }
     }
     if (!WANT_K) continue;
     __syncwarp();
 
-    // ---- pair loop ----
-    TK a1t[3], a2t[3], bt[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) { a1t[c] = static_cast<TK>(P.a1[c]); a2t[c] = static_cast<TK>(P.a2[c]); bt[c] = static_cast<TK>(P.b[c]); }
-    const TK bv = static_cast<TK>(P.bv);
-    const int64_t np = static_cast<int64_t>(n) * (n + 1) / 2;
-    const int64_t m0 = a.map_ptr[g];
-    int i = 0, off = lane;
-    while (i < n && off >= n - i) { off -= n - i; ++i; }
-    for (int64_t p = lane; p < np; p += 32) {
-      const int j = i + off;
-      const TK* RI = rec + i;
-      const TK* RJ = rec + j;
-      const TK dxi = RI[0], dyi = RI[nmax], be0 = RI[2 * nmax], be1 = RI[3 * nmax], be2 = RI[4 * nmax];
-      const TK Tui = RI[5 * nmax], gi0 = RI[6 * nmax], gi1 = RI[7 * nmax], gi2 = RI[8 * nmax];
-      const TK cj0 = RJ[(kRecI + 18) * nmax], cj1 = RJ[(kRecI + 19) * nmax];
-      const TK nj0 = RJ[(kRecI + 20) * nmax], nj1 = RJ[(kRecI + 21) * nmax];
-      const TK TuWj = RJ[(kRecI + 22) * nmax];
-      const TK s1 = Tui * cj0, s2 = Tui * cj1;
-      const TK t3 = bv * (dxi * cj0 + dyi * cj1);
-      const TK geo = dxi * nj0 + dyi * nj1;
-      TK Y1[3], Y2[3], Y3[3];
+    // ---- phase 2, one Gauss point at a time across the warp, in the tangent's precision.
+    const int kend = min(32, a.n_gp - g0);
+    for (int k = 0; k < kend; ++k) {
+      const int gg = g0 + k;
+      const int64_t p0 = a.ptr[gg];
+      const int n = static_cast<int>(a.ptr[gg + 1] - p0);
+      if (n == 0) continue;  // Assembly.h:208
+      TK a1t[3], a2t[3], bt[3], rxx[3], ryy[3], rxy[3], Nt[3], Mt[3], Ci[4];
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const TK P0 = RJ[(kRecI + c) * nmax], P1 = RJ[(kRecI + 3 + c) * nmax], P2 = RJ[(kRecI + 6 + c) * nmax];
-        const TK Q0 = RJ[(kRecI + 9 + c) * nmax], Q1 = RJ[(kRecI + 12 + c) * nmax], Q2 = RJ[(kRecI + 15 + c) * nmax];
-        const TK gic = c == 0 ? gi0 : (c == 1 ? gi1 : gi2);
-        Y1[c] = dxi * P0 + dyi * P2 - s1 * bt[c];
-        Y2[c] = dyi * P1 + dxi * P2 - s2 * bt[c];
-        Y3[c] = be0 * Q0 + be1 * Q1 + be2 * Q2 + t3 * bt[c] - TuWj * gic;
+        a1t[c] = st[(S_A1 + c) * 32 + k]; a2t[c] = st[(S_A2 + c) * 32 + k]; bt[c] = st[(S_B + c) * 32 + k];
+        rxx[c] = st[(S_RXX + c) * 32 + k]; ryy[c] = st[(S_RYY + c) * 32 + k]; rxy[c] = st[(S_RXY + c) * 32 + k];
+        Nt[c] = st[(S_N + c) * 32 + k]; Mt[c] = st[(S_M + c) * 32 + k];
       }
-      TK v[9];
 #pragma unroll
-      for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 4; ++c) Ci[c] = st[(S_CI + c) * 32 + k];
+      const TK pX = st[S_P * 32 + k], pY = st[(S_P + 1) * 32 + k];
+      const TK bv = st[S_BV * 32 + k], Wt = st[S_W * 32 + k];
+
+      // Records of the neighbours (lane per neighbour).
+      for (int i = lane; i < n; i += 32) {
+        const int64_t e = p0 + i;
+        const TK dx = dpsi_t[2 * e], dy = dpsi_t[2 * e + 1];
+        const TK dxx = ddpsi_t[3 * e], dyy = ddpsi_t[3 * e + 1], dxy = ddpsi_t[3 * e + 2];
+        const TK c0 = Ci[0] * dx + Ci[1] * dy;
+        const TK c1 = Ci[2] * dx + Ci[3] * dy;
+        TK gI[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-          v[3 * r + c] = a1t[r] * Y1[c] + a2t[r] * Y2[c] + bt[r] * Y3[c] + (r == c ? geo : TK(0));
-      const bool flip = nid[i] > nid[j];
-      if (DET) {
-        store_contrib<TK>(a.Kc, m0 + p, flip, v);
-      } else {
-        scatter_atomic<TK>(a.Kacc, a.map_slot[m0 + p], flip, v);
+        for (int r = 0; r < 3; ++r) gI[r] = a1t[r] * c0 + a2t[r] * c1;
+        const TK b0 = -dxx + (rxx[0] * gI[0] + rxx[1] * gI[1] + rxx[2] * gI[2]);
+        const TK b1 = -dyy + (ryy[0] * gI[0] + ryy[1] * gI[1] + ryy[2] * gI[2]);
+        const TK b2 = TK(2) * (-dxy + (rxy[0] * gI[0] + rxy[1] * gI[1] + rxy[2] * gI[2]));
+        const TK Tu = dx * pX + dy * pY - (dxx * Mt[0] + TK(2) * dxy * Mt[2] + dyy * Mt[1]);
+        TK* R = rec + i;
+        R[0 * nmax] = dx; R[1 * nmax] = dy;
+        R[2 * nmax] = b0; R[3 * nmax] = b1; R[4 * nmax] = b2;
+        R[5 * nmax] = Tu;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) R[(6 + r) * nmax] = gI[r];
+        // P = A Bm + B Bb, Q = B Bm + D Bb (Assembly.h:255-256), times W:
+        //   P(r,c) = a1_c pa_r + a2_c pb_r + b_c pc_r.
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          const TK Ar0 = static_cast<TK>(m.A[3 * r]), Ar1 = static_cast<TK>(m.A[3 * r + 1]), Ar2 = static_cast<TK>(m.A[3 * r + 2]);
+          const TK Br0 = static_cast<TK>(m.B[3 * r]), Br1 = static_cast<TK>(m.B[3 * r + 1]), Br2 = static_cast<TK>(m.B[3 * r + 2]);
+          const TK Dr0 = static_cast<TK>(m.D[3 * r]), Dr1 = static_cast<TK>(m.D[3 * r + 1]), Dr2 = static_cast<TK>(m.D[3 * r + 2]);
+          const TK pa = (Ar0 * dx + Ar2 * dy) * Wt;
+          const TK pb = (Ar1 * dy + Ar2 * dx) * Wt;
+          const TK pc = (Br0 * b0 + Br1 * b1 + Br2 * b2) * Wt;
+          const TK qa = (Br0 * dx + Br2 * dy) * Wt;
+          const TK qb = (Br1 * dy + Br2 * dx) * Wt;
+          const TK qc = (Dr0 * b0 + Dr1 * b1 + Dr2 * b2) * Wt;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            R[(kRecI + 3 * r + c) * nmax] = a1t[c] * pa + a2t[c] * pb + bt[c] * pc;
+            R[(kRecI + 9 + 3 * r + c) * nmax] = a1t[c] * qa + a2t[c] * qb + bt[c] * qc;
+          }
+        }
+        R[(kRecI + 18) * nmax] = c0 * Wt;
+        R[(kRecI + 19) * nmax] = c1 * Wt;
+        R[(kRecI + 20) * nmax] = (Nt[0] * dx + Nt[2] * dy) * Wt;
+        R[(kRecI + 21) * nmax] = (Nt[2] * dx + Nt[1] * dy) * Wt;
+        R[(kRecI + 22) * nmax] = Tu * Wt;
+        nid[i] = a.idx[e];
       }
-      off += 32;
+      __syncwarp();
+
+      // Pair loop: the n(n+1)/2 blocks of this point spread over the lanes.
+      const int64_t np = static_cast<int64_t>(n) * (n + 1) / 2;
+      const int64_t m0 = a.map_ptr[gg];
+      int i = 0, off = lane;
       while (i < n && off >= n - i) { off -= n - i; ++i; }
+      for (int64_t p = lane; p < np; p += 32) {
+        const int j = i + off;
+        const TK* RI = rec + i;
+        const TK* RJ = rec + j;
+        const TK dxi = RI[0], dyi = RI[nmax], be0 = RI[2 * nmax], be1 = RI[3 * nmax], be2 = RI[4 * nmax];
+        const TK Tui = RI[5 * nmax], gi0 = RI[6 * nmax], gi1 = RI[7 * nmax], gi2 = RI[8 * nmax];
+        const TK cj0 = RJ[(kRecI + 18) * nmax], cj1 = RJ[(kRecI + 19) * nmax];
+        const TK nj0 = RJ[(kRecI + 20) * nmax], nj1 = RJ[(kRecI + 21) * nmax];
+        const TK TuWj = RJ[(kRecI + 22) * nmax];
+        const TK s1 = Tui * cj0, s2 = Tui * cj1;
+        const TK t3 = bv * (dxi * cj0 + dyi * cj1);
+        const TK geo = dxi * nj0 + dyi * nj1;
+        TK Y1[3], Y2[3], Y3[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const TK P0 = RJ[(kRecI + c) * nmax], P1 = RJ[(kRecI + 3 + c) * nmax], P2 = RJ[(kRecI + 6 + c) * nmax];
+          const TK Q0 = RJ[(kRecI + 9 + c) * nmax], Q1 = RJ[(kRecI + 12 + c) * nmax], Q2 = RJ[(kRecI + 15 + c) * nmax];
+          const TK gic = c == 0 ? gi0 : (c == 1 ? gi1 : gi2);
+          Y1[c] = dxi * P0 + dyi * P2 - s1 * bt[c];
+          Y2[c] = dyi * P1 + dxi * P2 - s2 * bt[c];
+          Y3[c] = be0 * Q0 + be1 * Q1 + be2 * Q2 + t3 * bt[c] - TuWj * gic;
+        }
+        TK v[9];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            v[3 * r + c] = a1t[r] * Y1[c] + a2t[r] * Y2[c] + bt[r] * Y3[c] + (r == c ? geo : TK(0));
+        const bool flip = nid[i] > nid[j];
+        if (DET) {
+          store_contrib<TK>(a.Kc, m0 + p, flip, v);
+        } else {
+          scatter_atomic<TK>(a.Kacc, a.map_slot[m0 + p], flip, v);
+        }
+        off += 32;
+        while (i < n && off >= n - i) { off -= n - i; ++i; }
+      }
+      __syncwarp();
     }
-    __syncwarp();
   }
 }
 
@@ -678,6 +746,25 @@ HingeArgs hinge_args(cgb_assembler* a, cgb_fold_dev& f, const double* d_x, int f
   return h;
 }
 
+__global__ void to_float(int64_t n, const double* __restrict__ src, float* __restrict__ dst) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (i < n) dst[i] = static_cast<float>(src[i]);
+}
+
+// FP32 copies of grad / Hessian Phi for the FP32 pair phase (made once per assembler).
+void ensure_fp32_shapes(cgb_assembler* a) {
+  if (a->dpsi32.p) return;
+  const cgb_shape* S = a->faces;
+  cudaStream_t st = a->ctx->stream;
+  a->dpsi32.alloc(2 * S->nnz);
+  a->ddpsi32.alloc(3 * S->nnz);
+  if (S->nnz) {
+    to_float<<<nb(2 * S->nnz, 256), 256, 0, st>>>(2 * S->nnz, S->dpsi.p, a->dpsi32.p);
+    to_float<<<nb(3 * S->nnz, 256), 256, 0, st>>>(3 * S->nnz, S->ddpsi.p, a->ddpsi32.p);
+  }
+  CGB_CUDA(cudaGetLastError());
+}
+
 }  // namespace
 
 void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags) {
@@ -736,11 +823,20 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   fa.Kacc = mixed ? static_cast<void*>(a->kacc32.p) : static_cast<void*>(a->kacc64.p);
   fa.Kc = mixed ? static_cast<void*>(a->contrib32.p) : static_cast<void*>(a->contrib64.p);
   const size_t tk = mixed ? sizeof(float) : sizeof(double);
-  const size_t smem = want_K ? static_cast<size_t>(kFaceWarps) * fa.nmax * (kRec * tk + sizeof(int)) : 0;
+  const size_t smem = want_K ? static_cast<size_t>(kFaceWarps) * ((kState * 32 + kRec * fa.nmax) * tk +
+                                                                 fa.nmax * sizeof(int)) : 0;
+  if (mixed && want_K) {
+    ensure_fp32_shapes(a);
+    fa.dpsi_t = a->dpsi32.p;
+    fa.ddpsi_t = a->ddpsi32.p;
+  } else {
+    fa.dpsi_t = S->dpsi.p;
+    fa.ddpsi_t = S->ddpsi.p;
+  }
   if (smem > 200 * 1024)
     throw Error(CGB_ERR_CAPACITY, "assemble: " + std::to_string(S->max_n) + " neighbours per Gauss point exceed the shared-memory staging");
   const int sms = sm_count(ctx->device);
-  const unsigned grid = std::max(1u, std::min(nb(S->n_gp, kFaceWarps), static_cast<unsigned>(sms * 16)));
+  const unsigned grid = std::max(1u, std::min(nb(S->n_gp, 32 * kFaceWarps), static_cast<unsigned>(sms * 8)));
   auto launch = [&](auto kern) {
     if (smem > 48 * 1024) CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     prof_begin(ctx, CGB_PHASE_FACE);

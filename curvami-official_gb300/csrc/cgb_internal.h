@@ -149,6 +149,7 @@ struct cgb_assembler {
   cgb::DevBuf<double> F;            // 3 n_nodes (device scratch for host-buffer calls)
   cgb::DevBuf<double> K;            // 9 n_blocks (device scratch for host-buffer calls)
   cgb::DevBuf<double> x;            // 3 n_nodes
+  cgb::DevBuf<float> dpsi32, ddpsi32; // FP32 copies of the face shape derivatives (mixed mode)
   // Deterministic scatter: per pair contributions and per-block ordered lists.
   bool det_ready = false;
   cgb::DevBuf<int64_t> blk_list_ptr;  // n_blocks + 1
