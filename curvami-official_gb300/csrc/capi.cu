@@ -139,6 +139,17 @@ int cgb_create(int device, cgb_context** out) {
 
 int cgb_destroy(cgb_context* ctx) {
   if (!ctx) return CGB_OK;
+  ctx->closed = true;
+  cgb::ctx_release(ctx);
+  return CGB_OK;
+}
+
+}  // extern "C"
+
+namespace cgb {
+void ctx_retain(cgb_context* ctx) { ++ctx->refs; }
+void ctx_release(cgb_context* ctx) {
+  if (--ctx->refs > 0) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->node_xy.reset();
@@ -150,8 +161,10 @@ int cgb_destroy(cgb_context* ctx) {
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
-  return CGB_OK;
 }
+}  // namespace cgb
+
+extern "C" {
 
 const char* cgb_last_error(const cgb_context* ctx) {
   return ctx ? ctx->last_error.c_str() : "null context";
@@ -208,8 +221,13 @@ int cgb_shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_s
   });
   // A rank-deficient support still returns the (flagged) shape set, as the reference
   // has filled every array before it throws.
-  if (rc == CGB_OK || rc == CGB_ERR_SINGULAR || rc == CGB_ERR_PIVOT) *out = sh;
-  else delete sh;
+  if (rc == CGB_OK || rc == CGB_ERR_SINGULAR || rc == CGB_ERR_PIVOT) {
+    sh->ctx = ctx;
+    cgb::ctx_retain(ctx);
+    *out = sh;
+  } else {
+    delete sh;
+  }
   return rc;
 }
 
@@ -243,7 +261,12 @@ int cgb_shape_from_host(cgb_context* ctx, int n_gp, const int64_t* nbr_ptr, cons
     cgb::upload(sh->ddpsi, ddpsi, 3 * nnz, st);
     CGB_CUDA(cudaStreamSynchronize(st));
   });
-  if (rc == CGB_OK) *out = sh; else delete sh;
+  if (rc == CGB_OK) {
+    cgb::ctx_retain(ctx);
+    *out = sh;
+  } else {
+    delete sh;
+  }
   return rc;
 }
 
@@ -288,11 +311,13 @@ int cgb_shape_device(const cgb_shape* sh, const int64_t** nbr_ptr, const int32_t
 
 int cgb_shape_destroy(cgb_shape* sh) {
   if (!sh) return CGB_OK;
-  if (sh->ctx) {
-    cudaSetDevice(sh->ctx->device);
-    cudaStreamSynchronize(sh->ctx->stream);
+  cgb_context* ctx = sh->ctx;
+  if (ctx) {
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
   }
   delete sh;
+  if (ctx) cgb::ctx_release(ctx);
   return CGB_OK;
 }
 
@@ -334,18 +359,25 @@ int cgb_assembler_create(cgb_context* ctx, const cgb_shape* faces, const double*
     a->F.alloc(3 * static_cast<size_t>(a->n_nodes));
     a->x.alloc(3 * static_cast<size_t>(a->n_nodes));
   });
-  if (rc == CGB_OK) *out = a; else delete a;
+  if (rc == CGB_OK) {
+    cgb::ctx_retain(ctx);
+    *out = a;
+  } else {
+    delete a;
+  }
   return rc;
 }
 
 int cgb_assembler_destroy(cgb_assembler* a) {
   if (!a) return CGB_OK;
-  if (a->ctx) {
-    cudaSetDevice(a->ctx->device);
-    cudaStreamSynchronize(a->ctx->stream);
+  cgb_context* ctx = a->ctx;
+  if (ctx) {
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
   }
   if (a->h_stage) cudaFreeHost(a->h_stage);
   delete a;
+  if (ctx) cgb::ctx_release(ctx);
   return CGB_OK;
 }
 

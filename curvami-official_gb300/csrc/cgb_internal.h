@@ -71,6 +71,10 @@ struct Crease {
 
 // Opaque handles of the C ABI.
 struct cgb_context {
+  // Shape sets and assemblers keep their context alive: cgb_destroy only drops the
+  // caller's reference, the context is freed when the last handle that uses it is.
+  int refs = 1;
+  bool closed = false;
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -170,6 +174,8 @@ struct cgb_assembler {
 };
 
 namespace cgb {
+void ctx_retain(cgb_context* ctx);
+void ctx_release(cgb_context* ctx);
 // Tracing helpers (capi.cu): no-ops unless profiling is enabled on the context.
 void prof_begin(cgb_context* ctx, int phase);
 void prof_end(cgb_context* ctx, int phase, int launches);

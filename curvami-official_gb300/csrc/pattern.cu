@@ -237,7 +237,7 @@ void pattern_build(cgb_assembler* a) {
   DevBuf<int64_t> d_hptr;
   DevBuf<int32_t> d_hidx;
   upload(d_hptr, hptr.data(), hptr.size(), st);
-  upload(d_hidx, hidx.data(), std::max<size_t>(hidx.size(), 1), st);
+  upload(d_hidx, hidx.data(), hidx.size(), st);
 
   // ---- node -> list inverse index ----
   DevBuf<int32_t> cnt(n_nodes);
@@ -338,7 +338,7 @@ void pattern_build(cgb_assembler* a) {
       hoff += f.n_gp;
       f.n_pairs = static_cast<int64_t>(ps.size());
       upload(f.pair_ptr, pp.data(), pp.size(), st);
-      upload(f.pair_slot, ps.data(), std::max<size_t>(ps.size(), 1), st);
+      upload(f.pair_slot, ps.data(), ps.size(), st);
       CGB_CUDA(cudaStreamSynchronize(st));
     }
   }
