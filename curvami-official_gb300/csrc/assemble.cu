@@ -59,6 +59,7 @@ struct FaceArgs {
   const double* x;
   const int64_t* map_ptr;
   const int32_t* map_slot;
+  const int32_t* outer;  // scalar CSC column starts (POS_MAP only)
   Material mat;
   double* F;         // atomic F (3 n_nodes)
   double* Fc;        // deterministic F contributions (3 per entry)
@@ -179,7 +180,10 @@ constexpr int kState = 32;
 enum : int { S_A1 = 0, S_A2 = 3, S_B = 6, S_RXX = 9, S_RYY = 12, S_RXY = 15, S_CI = 18, S_N = 22,
              S_M = 25, S_P = 28, S_BV = 30, S_W = 31 };
 
-template <typename TK, bool DET, bool WANT_K>
+// TIN: element type of the grad / Hessian Phi arrays the pair phase reads (TK, or FP64
+// read and rounded in the kernel). POS_MAP: map_slot holds the reference's csrMapping
+// positions and the block slot is outer[3 max(ni, nj)] / 9 + position.
+template <typename TK, bool DET, bool WANT_K, typename TIN = TK, bool POS_MAP = false>
 __global__ void __launch_bounds__(32 * kFaceWarps) face_kernel(FaceArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -190,8 +194,8 @@ __global__ void __launch_bounds__(32 * kFaceWarps) face_kernel(FaceArgs a) {
   int* nid = reinterpret_cast<int*>(reinterpret_cast<TK*>(smem_raw) +
                                     static_cast<size_t>(kFaceWarps) * (kState * 32 + kRec * nmax)) + w * nmax;
   const Material& m = a.mat;
-  const TK* dpsi_t = static_cast<const TK*>(a.dpsi_t);
-  const TK* ddpsi_t = static_cast<const TK*>(a.ddpsi_t);
+  const TIN* dpsi_t = static_cast<const TIN*>(a.dpsi_t);
+  const TIN* ddpsi_t = static_cast<const TIN*>(a.ddpsi_t);
 
   // Each warp owns 32 consecutive Gauss points per round.
   for (int g0 = (blockIdx.x * kFaceWarps + w) * 32; g0 < a.n_gp; g0 += gridDim.x * kFaceWarps * 32) {
@@ -291,8 +295,9 @@ __global__ void __launch_bounds__(32 * kFaceWarps) face_kernel(FaceArgs a) {
       // Records of the neighbours (lane per neighbour).
       for (int i = lane; i < n; i += 32) {
         const int64_t e = p0 + i;
-        const TK dx = dpsi_t[2 * e], dy = dpsi_t[2 * e + 1];
-        const TK dxx = ddpsi_t[3 * e], dyy = ddpsi_t[3 * e + 1], dxy = ddpsi_t[3 * e + 2];
+        const TK dx = static_cast<TK>(dpsi_t[2 * e]), dy = static_cast<TK>(dpsi_t[2 * e + 1]);
+        const TK dxx = static_cast<TK>(ddpsi_t[3 * e]), dyy = static_cast<TK>(ddpsi_t[3 * e + 1]);
+        const TK dxy = static_cast<TK>(ddpsi_t[3 * e + 2]);
         const TK c0 = Ci[0] * dx + Ci[1] * dy;
         const TK c1 = Ci[2] * dx + Ci[3] * dy;
         TK gI[3];
@@ -372,6 +377,9 @@ __global__ void __launch_bounds__(32 * kFaceWarps) face_kernel(FaceArgs a) {
         const bool flip = nid[i] > nid[j];
         if (DET) {
           store_contrib<TK>(a.Kc, m0 + p, flip, v);
+        } else if (POS_MAP) {
+          const int hi = flip ? nid[i] : nid[j];
+          scatter_atomic<TK>(a.Kacc, a.outer[3 * static_cast<int64_t>(hi)] / 9 + a.map_slot[m0 + p], flip, v);
         } else {
           scatter_atomic<TK>(a.Kacc, a.map_slot[m0 + p], flip, v);
         }
@@ -628,6 +636,25 @@ __global__ void blocks_to_csc(int n_nodes, const int64_t* __restrict__ col_ptr, 
     double* col = K + 9 * b0;
     for (int t = lane; t < 9 * len; t += 32) {
       // t enumerates the column's output in storage order: c major, then (pos, r).
+      const int c = t / (3 * len), rem = t - c * 3 * len, pos = rem / 3, r = rem - 3 * pos;
+      col[t] = static_cast<double>(acc[(b0 + pos) * STRIDE + 3 * r + c]);
+    }
+  }
+}
+
+// The same output step with the block columns taken from the scalar CSC outer index:
+// column node j starts at block outer[3j] / 9 and holds (outer[3j+1] - outer[3j]) / 3 blocks.
+template <typename TA, int STRIDE>
+__global__ void blocks_to_csc_outer(int n_nodes, const int32_t* __restrict__ outer, const TA* __restrict__ acc,
+                                    double* __restrict__ K) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t j = warp; j < n_nodes; j += nw) {
+    const int64_t b0 = outer[3 * j] / 9;
+    const int len = (outer[3 * j + 1] - outer[3 * j]) / 3;
+    double* col = K + outer[3 * j];
+    for (int t = lane; t < 9 * len; t += 32) {
       const int c = t / (3 * len), rem = t - c * 3 * len, pos = rem / 3, r = rem - 3 * pos;
       col[t] = static_cast<double>(acc[(b0 + pos) * STRIDE + 3 * r + c]);
     }
@@ -895,6 +922,40 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     else blocks_to_csc<double, 9><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->kacc64.p, d_K);
   }
   prof_end(ctx, CGB_PHASE_REDUCE, nred);
+  CGB_CUDA(cudaGetLastError());
+}
+
+// Mixed-precision face assembly on caller-owned device arrays, with the FP32 block
+// accumulator supplied by the caller (the allocation-free entry point, noalloc.cu).
+void face_mixed_on_arrays(const cgb_face_problem& pr, const double* d_x, double* d_K, double* d_F,
+                          float* kacc, cudaStream_t st) {
+  FaceArgs fa{};
+  fa.n_gp = pr.n_gp;
+  fa.nmax = std::max(pr.max_neighbours, 1);
+  fa.ptr = pr.nbr_ptr; fa.idx = pr.nbr_idx; fa.dpsi = pr.dpsi; fa.ddpsi = pr.ddpsi;
+  fa.dpsi_t = pr.dpsi; fa.ddpsi_t = pr.ddpsi;
+  fa.weight = pr.weight; fa.x = d_x;
+  fa.map_ptr = pr.map_ptr; fa.map_slot = pr.csr_map; fa.outer = pr.outer;
+  std::memcpy(fa.mat.A, pr.A, sizeof fa.mat.A); std::memcpy(fa.mat.B, pr.B, sizeof fa.mat.B);
+  std::memcpy(fa.mat.D, pr.D, sizeof fa.mat.D);
+  fa.F = d_F;
+  fa.Kacc = kacc;
+  const int64_t n_blocks = static_cast<int64_t>(pr.nnz / 9);
+  CGB_CUDA(cudaMemsetAsync(d_F, 0, 3 * static_cast<size_t>(pr.n_nodes) * sizeof(double), st));
+  CGB_CUDA(cudaMemsetAsync(kacc, 0, 12 * static_cast<size_t>(n_blocks) * sizeof(float), st));
+  const size_t smem = static_cast<size_t>(kFaceWarps) * ((kState * 32 + kRec * fa.nmax) * sizeof(float) +
+                                                        fa.nmax * sizeof(int));
+  auto kern = face_kernel<float, false, true, double, true>;
+  if (smem > 48 * 1024) CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  int dev = 0;
+  CGB_CUDA(cudaGetDevice(&dev));
+  const int sms = sm_count(dev);
+  if (pr.n_gp > 0) {
+    const unsigned grid = std::max(1u, std::min(nb(pr.n_gp, 32 * kFaceWarps), static_cast<unsigned>(sms * 8)));
+    kern<<<grid, 32 * kFaceWarps, smem, st>>>(fa);
+  }
+  const unsigned cg = std::max(1u, std::min(nb(pr.n_nodes, 4), static_cast<unsigned>(sms * 32)));
+  blocks_to_csc_outer<float, 12><<<cg, 128, 0, st>>>(pr.n_nodes, pr.outer, kacc, d_K);
   CGB_CUDA(cudaGetLastError());
 }
 

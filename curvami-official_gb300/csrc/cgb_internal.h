@@ -188,4 +188,6 @@ void deterministic_prepare(cgb_assembler* a);
 // assemble.cu
 void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags);
 void energies_device(cgb_assembler* a, const double* d_x, double* out3);
+void face_mixed_on_arrays(const cgb_face_problem& pr, const double* d_x, double* d_K, double* d_F,
+                          float* kacc, cudaStream_t st);
 }  // namespace cgb

@@ -50,6 +50,7 @@ SIGNATURES = {
     "cgb_assemble": (i32, [vp, vp, vp, vp, i32]),
     "cgb_assemble_device": (i32, [vp, vp, vp, vp, i32]),
     "cgb_energies": (i32, [vp, vp, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(dbl)]),
+    "cgb_assemble_face_noalloc": (i32, [vp, vp, vp, vp, vp]),
     "cgb_profile_enable": (i32, [vp, i32]),
     "cgb_profile_read": (i32, [vp, vp, vp, i32]),
 }
@@ -69,6 +70,17 @@ class ShapeParams(C.Structure):
 class Fold(C.Structure):
     _fields_ = [("left", vp), ("right", vp), ("weight", vp), ("tangent", vp), ("Kt", dbl),
                 ("theta0", dbl), ("theta0_gp", vp), ("active", vp)]
+
+
+NOALLOC_MAX_BLOCKS = 699050
+
+
+class FaceProblem(C.Structure):
+    """cgb_face_problem: device pointers of the allocation-free face assembly."""
+    _fields_ = [("n_gp", i32), ("n_nodes", i32), ("max_neighbours", i32), ("nnz", i64),
+                ("nbr_ptr", vp), ("nbr_idx", vp), ("dpsi", vp), ("ddpsi", vp), ("weight", vp),
+                ("map_ptr", vp), ("csr_map", vp), ("outer", vp),
+                ("A", dbl * 9), ("B", dbl * 9), ("D", dbl * 9)]
 
 
 class CGBError(RuntimeError):

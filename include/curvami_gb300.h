@@ -157,6 +157,47 @@ int cgb_assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double
 int cgb_energies(cgb_assembler* a, const double* x, double* E_mem, double* E_ben,
                  double* E_hin);
 
+/* ---- allocation-free face assembly -------------------------------------------------- */
+/* No counterpart in the reference. It serves callers that cannot allocate GPU memory
+ * while they assemble: cudaMalloc / cudaFree may synchronise the whole device (stalling
+ * every other stream of the process), are not allowed while a stream is being captured,
+ * and some host frameworks hand out device memory only through their own pool. Such a
+ * caller keeps every input in its own device memory and calls this entry point, which
+ * allocates nothing.
+ *
+ * It runs the mixed-precision face assembly (FP64 residual, FP32 tangent, atomic
+ * scatter; the same arithmetic as cgb_assemble_device with CGB_TANGENT | CGB_MIXED,
+ * faces only, no hinge) on caller-owned arrays in the reference's own formats: the
+ * neighbour lists and shape derivatives of the face Gauss points, the K column starts
+ * (Eigen outerIndexPtr) and the concatenated NonLinearAssembler::csrMapping positions.
+ * Its FP32 block accumulator lives in a fixed array inside the library (every GPU that
+ * loads the library holds CGB_NOALLOC_MAX_BLOCKS * 48 bytes = 32 MiB of it until the
+ * process exits). nnz / 9 above CGB_NOALLOC_MAX_BLOCKS is rejected with
+ * CGB_ERR_CAPACITY. The first call on a device looks the array's address up for that
+ * device (current device = ctx's); make that first call before any stream capture.
+ * Every call shares the one array: calls whose executions overlap on the GPU (other
+ * streams, other contexts of the process on the same device) race and corrupt each
+ * other's K, so serialise them. All pointers in prob and the x / K / F arguments are
+ * device pointers; the call is asynchronous on ctx's stream. */
+#define CGB_NOALLOC_MAX_BLOCKS 699050
+typedef struct {
+  int n_gp;                /* face Gauss points */
+  int n_nodes;
+  int max_neighbours;      /* largest neighbour count of any Gauss point */
+  int64_t nnz;             /* outer[3 n_nodes] */
+  const int64_t* nbr_ptr;  /* n_gp + 1 */
+  const int32_t* nbr_idx;
+  const double* dpsi;      /* 2 per entry */
+  const double* ddpsi;     /* 3 per entry */
+  const double* weight;    /* n_gp */
+  const int64_t* map_ptr;  /* n_gp + 1: sum of n(n+1)/2 over the earlier points */
+  const int32_t* csr_map;  /* csrMapping positions, concatenated */
+  const int32_t* outer;    /* 3 n_nodes + 1 */
+  double A[9], B[9], D[9]; /* laminate stiffness, row-major, host values */
+} cgb_face_problem;
+int cgb_assemble_face_noalloc(cgb_context* ctx, const cgb_face_problem* prob, const double* d_x,
+                              double* d_K, double* d_F);
+
 /* ---- tracing (library extension; the reference only prints wall-clock times) ------ */
 /* CUDA events around every phase of cgb_assemble / cgb_assemble_device, summed per
  * phase until read. Off by default; costs two event records per phase when on. */

@@ -1,0 +1,82 @@
+"""The allocation-free entry point cgb_assemble_face_noalloc, through the C ABI.
+
+It exists for callers that cannot allocate GPU memory while they assemble (cudaMalloc
+may synchronise the device, is not allowed during stream capture, or is reserved to a
+host framework's own pool): they hold every input in their own device memory and the
+library keeps its one scratch array (the FP32 block accumulator) in a fixed,
+file-scope device array. The test allocates the caller's arrays itself (torch), then
+checks two calls in a row against the allocating entry point (cgb_assemble_device with
+CGB_TANGENT | CGB_MIXED): the residual to 1e-13 and the FP32 tangent to 1e-6 of its
+scale, the same bars the mixed path meets elsewhere. Collected last, so a failure here
+leaves every other test already run.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import curvami_gb300 as cg
+from curvami_gb300 import _lib, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def test_noalloc_matches_allocating_path():
+    torch = pytest.importorskip("torch")
+    import __graft_entry__ as ge
+
+    ge.build()
+    ctx = cg.Context(0)
+    p = synth.config_smallplate(rule=4)  # 41x41 nodes, 25,600 Gauss points
+    ctx.set_nodes(p.node_xy)
+    faces = cg.shape_functions(ctx, p.faces.xy, p.rho, p.order, p.creases, p.rho_node, p.kernel)
+    asm = cg.NonLinearAssembler(ctx, faces, p.faces.weight)
+    A, B, D = cg.abd_isotropic(p.E, p.nu, p.thickness)
+    asm.set_material(A, B, D)
+    assert asm.nnz // 9 <= _lib.NOALLOC_MAX_BLOCKS
+
+    # The caller's own device copies of the inputs, in the reference's formats.
+    sh = faces.download()
+    outer, _ = asm.pattern()
+    csr_map = asm.csr_mapping()
+    n = np.diff(sh["ptr"])
+    map_ptr = np.concatenate([[0], np.cumsum(n * (n + 1) // 2)]).astype(np.int64)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    d = {"nbr_ptr": dev(sh["ptr"]), "nbr_idx": dev(sh["idx"]), "dpsi": dev(sh["dpsi"]),
+         "ddpsi": dev(sh["ddpsi"]), "weight": dev(p.faces.weight), "map_ptr": dev(map_ptr),
+         "csr_map": dev(csr_map), "outer": dev(outer)}
+    prob = _lib.FaceProblem()
+    prob.n_gp = faces.n_gp
+    prob.n_nodes = p.n_nodes
+    prob.max_neighbours = faces.max_n
+    prob.nnz = asm.nnz
+    for k, t in d.items():
+        setattr(prob, k, t.data_ptr())
+    for name, M in (("A", A), ("B", B), ("D", D)):
+        getattr(prob, name)[:] = [float(v) for v in np.asarray(M).ravel()]
+
+    rng = np.random.default_rng(8)
+    for call in range(2):
+        x = 0.2 * synth.fourier_field(p.node_xy, rng, lam=(5.0, 20.0))
+        x_d = dev(x)
+        K_ref = torch.empty(asm.nnz, dtype=torch.float64, device="cuda")
+        F_ref = torch.empty(3 * p.n_nodes, dtype=torch.float64, device="cuda")
+        asm.assemble_device(x_d.data_ptr(), K_ref.data_ptr(), F_ref.data_ptr(), cg.TANGENT | cg.MIXED)
+        ctx.synchronize()
+        K = torch.full((asm.nnz,), np.nan, dtype=torch.float64, device="cuda")
+        F = torch.full((3 * p.n_nodes,), np.nan, dtype=torch.float64, device="cuda")
+        rc = ctx.lib.cgb_assemble_face_noalloc(ctx.h, C.byref(prob), C.c_void_p(x_d.data_ptr()),
+                                               C.c_void_p(K.data_ptr()), C.c_void_p(F.data_ptr()))
+        assert rc == 0, ctx.lib.cgb_last_error(ctx.h)
+        ctx.synchronize()
+        K, F, K_ref, F_ref = (t.cpu().numpy() for t in (K, F, K_ref, F_ref))
+        assert np.isfinite(K).all() and np.isfinite(F).all()
+        assert np.abs(F - F_ref).max() <= 1e-13 * np.abs(F_ref).max(), call
+        assert np.abs(K - K_ref).max() <= 1e-6 * np.abs(K_ref).max(), call
+
+    # Sizes beyond the fixed accumulator are refused with a clear error.
+    prob.nnz = 9 * (_lib.NOALLOC_MAX_BLOCKS + 1)
+    rc = ctx.lib.cgb_assemble_face_noalloc(ctx.h, C.byref(prob), C.c_void_p(x_d.data_ptr()),
+                                           C.c_void_p(1), C.c_void_p(1))
+    assert rc == _lib.CGB_ERR_CAPACITY
+    assert b"exceeds the fixed accumulator" in ctx.lib.cgb_last_error(ctx.h)
