@@ -60,6 +60,12 @@ struct FaceArgs {
   const int64_t* map_ptr;
   const int32_t* map_slot;
   const int32_t* outer;  // scalar CSC column starts (POS_MAP only)
+  // Phase-1 copy of the neighbour data in sliced-ELL order: Gauss point 32 W + l, entry
+  // q at sell_ptr[W] + 32 q + l (null: read the CSR arrays).
+  const int64_t* sell_ptr;
+  const int32_t* sidx;
+  const double* sdpsi;
+  const double* sddpsi;
   Material mat;
   double* F;         // atomic F (3 n_nodes)
   double* Fc;        // deterministic F contributions (3 per entry)
@@ -183,38 +189,39 @@ enum : int { S_A1 = 0, S_A2 = 3, S_B = 6, S_RXX = 9, S_RYY = 12, S_RXY = 15, S_C
 // TIN: element type of the grad / Hessian Phi arrays the pair phase reads (TK, or FP64
 // read and rounded in the kernel). POS_MAP: map_slot holds the reference's csrMapping
 // positions and the block slot is outer[3 max(ni, nj)] / 9 + position.
-template <typename TK, bool DET, bool WANT_K, typename TIN = TK, bool POS_MAP = false>
-__global__ void __launch_bounds__(32 * kFaceWarps) face_kernel(FaceArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nmax = a.nmax;
-  TK* base_w = reinterpret_cast<TK*>(smem_raw) + static_cast<size_t>(w) * (kState * 32 + kRec * nmax);
-  TK* st = base_w;                 // [kState][32]
-  TK* rec = base_w + kState * 32;  // [kRec][nmax]
-  int* nid = reinterpret_cast<int*>(reinterpret_cast<TK*>(smem_raw) +
-                                    static_cast<size_t>(kFaceWarps) * (kState * 32 + kRec * nmax)) + w * nmax;
+// BZERO: the laminate coupling matrix B is zero (every symmetric laminate, and the
+// single isotropic ply of the reference's app, whose B = Q (z1^2 - z0^2) / 2 is exactly
+// 0). Then P = A Bm = a1 (x) pa + a2 (x) pb and Q = D Bb = b (x) qc, and the J-side
+// record shrinks from 23 to 14 values.
+// Phase 1 for the Gauss point g0 + lane (g0 a multiple of 32): FP64 kinematics,
+// resultants and residual (F atomics, or per-entry contributions when DET); when st is
+// not null the point's state goes to st[field * st_stride + st_idx] in TK.
+template <typename TK, bool DET>
+__device__ __forceinline__ void phase1_point(const FaceArgs& a, int g0, int lane, TK* st, int64_t st_stride,
+                                             int64_t st_idx) {
   const Material& m = a.mat;
-  const TIN* dpsi_t = static_cast<const TIN*>(a.dpsi_t);
-  const TIN* ddpsi_t = static_cast<const TIN*>(a.ddpsi_t);
-
-  // Each warp owns 32 consecutive Gauss points per round.
-  for (int g0 = (blockIdx.x * kFaceWarps + w) * 32; g0 < a.n_gp; g0 += gridDim.x * kFaceWarps * 32) {
-    // ---- phase 1, one Gauss point per lane, FP64: kinematics, resultants, residual.
-    // Every lane does distinct work, so no FP64 issue slot is spent on a redundant or
-    // masked copy (on GB300 an FP64 warp instruction costs the same with 1 or 32 lanes).
-    const int g = g0 + lane;
-    if (g < a.n_gp) {
+  const int g = g0 + lane;
+  if (g < a.n_gp) {
       const int64_t p0 = a.ptr[g];
       const int n = static_cast<int>(a.ptr[g + 1] - p0);
+      // Entry q of this lane's point: CSR p0 + q, or sliced-ELL sb + 32 q (coalesced
+      // across the warp: the 32 lanes read 32 consecutive entries per q).
+      const bool sell = a.sell_ptr != nullptr;
+      const int64_t sb = sell ? a.sell_ptr[g0 >> 5] + lane : p0;
+      const int64_t stride = sell ? 32 : 1;
+      const int32_t* Ix = sell ? a.sidx : a.idx;
+      const double* Dp = sell ? a.sdpsi : a.dpsi;
+      const double* Ddp = sell ? a.sddpsi : a.ddpsi;
       double s[15];
 #pragma unroll
       for (int k = 0; k < 15; ++k) s[k] = 0.0;
+#pragma unroll 4
       for (int q = 0; q < n; ++q) {
-        const int64_t e = p0 + q;
-        const int64_t j = a.idx[e];
+        const int64_t e = sb + q * stride;
+        const int64_t j = Ix[e];
         const double u0 = a.x[3 * j], u1 = a.x[3 * j + 1], u2 = a.x[3 * j + 2];
-        const double2 d = reinterpret_cast<const double2*>(a.dpsi)[e];
-        const double dxx = a.ddpsi[3 * e], dyy = a.ddpsi[3 * e + 1], dxy = a.ddpsi[3 * e + 2];
+        const double2 d = reinterpret_cast<const double2*>(Dp)[e];
+        const double dxx = Ddp[3 * e], dyy = Ddp[3 * e + 1], dxy = Ddp[3 * e + 2];
         s[0] += u0 * d.x; s[1] += u1 * d.x; s[2] += u2 * d.x;
         s[3] += u0 * d.y; s[4] += u1 * d.y; s[5] += u2 * d.y;
         s[6] += u0 * dxx; s[7] += u1 * dxx; s[8] += u2 * dxx;
@@ -230,10 +237,12 @@ __global__ void __launch_bounds__(32 * kFaceWarps) face_kernel(FaceArgs a) {
       const double MW0 = P.M[0] * W, MW1 = P.M[1] * W, MW2 = 2.0 * P.M[2] * W;
       const double pW0 = P.pXY[0] * W, pW1 = P.pXY[1] * W;
       if (n > 0) {
+#pragma unroll 2
         for (int q = 0; q < n; ++q) {
+          const int64_t es = sb + q * stride;
           const int64_t e = p0 + q;
-          const double2 d = reinterpret_cast<const double2*>(a.dpsi)[e];
-          const double dxx = a.ddpsi[3 * e], dyy = a.ddpsi[3 * e + 1], dxy = a.ddpsi[3 * e + 2];
+          const double2 d = reinterpret_cast<const double2*>(Dp)[es];
+          const double dxx = Ddp[3 * es], dyy = Ddp[3 * es + 1], dxy = Ddp[3 * es + 2];
           const double v1 = d.x * NW0 + d.y * NW2;
           const double v2 = d.y * NW1 + d.x * NW2;
           const double tu = d.x * pW0 + d.y * pW1 - (dxx * MW0 + dxy * MW2 + dyy * MW1);
@@ -244,150 +253,256 @@ __global__ void __launch_bounds__(32 * kFaceWarps) face_kernel(FaceArgs a) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) a.Fc[3 * e + c] = f[c];
           } else {
-            const int64_t node = a.idx[e];
+            const int64_t node = Ix[es];
 #pragma unroll
             for (int c = 0; c < 3; ++c) atomicAdd(a.F + 3 * node + c, f[c]);
           }
         }
       }
-      if (WANT_K) {
+      if (st) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          st[(S_A1 + c) * 32 + lane] = static_cast<TK>(P.a1[c]);
-          st[(S_A2 + c) * 32 + lane] = static_cast<TK>(P.a2[c]);
-          st[(S_B + c) * 32 + lane] = static_cast<TK>(P.b[c]);
-          st[(S_RXX + c) * 32 + lane] = static_cast<TK>(P.rxx[c]);
-          st[(S_RYY + c) * 32 + lane] = static_cast<TK>(P.ryy[c]);
-          st[(S_RXY + c) * 32 + lane] = static_cast<TK>(P.rxy[c]);
-          st[(S_N + c) * 32 + lane] = static_cast<TK>(P.N[c]);
-          st[(S_M + c) * 32 + lane] = static_cast<TK>(P.M[c]);
+          st[(S_A1 + c) * st_stride + st_idx] = static_cast<TK>(P.a1[c]);
+          st[(S_A2 + c) * st_stride + st_idx] = static_cast<TK>(P.a2[c]);
+          st[(S_B + c) * st_stride + st_idx] = static_cast<TK>(P.b[c]);
+          st[(S_RXX + c) * st_stride + st_idx] = static_cast<TK>(P.rxx[c]);
+          st[(S_RYY + c) * st_stride + st_idx] = static_cast<TK>(P.ryy[c]);
+          st[(S_RXY + c) * st_stride + st_idx] = static_cast<TK>(P.rxy[c]);
+          st[(S_N + c) * st_stride + st_idx] = static_cast<TK>(P.N[c]);
+          st[(S_M + c) * st_stride + st_idx] = static_cast<TK>(P.M[c]);
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) st[(S_CI + c) * 32 + lane] = static_cast<TK>(P.Ci[c]);
-        st[(S_P + 0) * 32 + lane] = static_cast<TK>(P.pXY[0]);
-        st[(S_P + 1) * 32 + lane] = static_cast<TK>(P.pXY[1]);
-        st[S_BV * 32 + lane] = static_cast<TK>(P.bv);
-        st[S_W * 32 + lane] = static_cast<TK>(W);
+        for (int c = 0; c < 4; ++c) st[(S_CI + c) * st_stride + st_idx] = static_cast<TK>(P.Ci[c]);
+        st[(S_P + 0) * st_stride + st_idx] = static_cast<TK>(P.pXY[0]);
+        st[(S_P + 1) * st_stride + st_idx] = static_cast<TK>(P.pXY[1]);
+        st[S_BV * st_stride + st_idx] = static_cast<TK>(P.bv);
+        st[S_W * st_stride + st_idx] = static_cast<TK>(W);
       }
     }
-    if (!WANT_K) continue;
-    __syncwarp();
+}
 
-    // ---- phase 2, one Gauss point at a time across the warp, in the tangent's precision.
-    const int kend = min(32, a.n_gp - g0);
-    for (int k = 0; k < kend; ++k) {
-      const int gg = g0 + k;
-      const int64_t p0 = a.ptr[gg];
-      const int n = static_cast<int>(a.ptr[gg + 1] - p0);
-      if (n == 0) continue;  // Assembly.h:208
-      TK a1t[3], a2t[3], bt[3], rxx[3], ryy[3], rxy[3], Nt[3], Mt[3], Ci[4];
+// Phase 2 for the Gauss points g0 .. g0 + 31 across the warp, in the tangent's precision:
+// per-neighbour records in shared memory, then the pair loop and the scatter. st holds
+// the 32 points' states as [field][32].
+template <typename TK, bool DET, typename TIN, bool POS_MAP, bool BZERO>
+__device__ __forceinline__ void phase2_group(const FaceArgs& a, int g0, int lane, const TK* st, TK* rec, int* nid) {
+  const Material& m = a.mat;
+  const int nmax = a.nmax;
+  const TIN* dpsi_t = static_cast<const TIN*>(a.dpsi_t);
+  const TIN* ddpsi_t = static_cast<const TIN*>(a.ddpsi_t);
+  const int kend = min(32, a.n_gp - g0);
+  for (int k = 0; k < kend; ++k) {
+    const int gg = g0 + k;
+    const int64_t p0 = a.ptr[gg];
+    const int n = static_cast<int>(a.ptr[gg + 1] - p0);
+    if (n == 0) continue;  // Assembly.h:208
+    TK a1t[3], a2t[3], bt[3], rxx[3], ryy[3], rxy[3], Nt[3], Mt[3], Ci[4];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        a1t[c] = st[(S_A1 + c) * 32 + k]; a2t[c] = st[(S_A2 + c) * 32 + k]; bt[c] = st[(S_B + c) * 32 + k];
-        rxx[c] = st[(S_RXX + c) * 32 + k]; ryy[c] = st[(S_RYY + c) * 32 + k]; rxy[c] = st[(S_RXY + c) * 32 + k];
-        Nt[c] = st[(S_N + c) * 32 + k]; Mt[c] = st[(S_M + c) * 32 + k];
-      }
+    for (int c = 0; c < 3; ++c) {
+      a1t[c] = st[(S_A1 + c) * 32 + k]; a2t[c] = st[(S_A2 + c) * 32 + k]; bt[c] = st[(S_B + c) * 32 + k];
+      rxx[c] = st[(S_RXX + c) * 32 + k]; ryy[c] = st[(S_RYY + c) * 32 + k]; rxy[c] = st[(S_RXY + c) * 32 + k];
+      Nt[c] = st[(S_N + c) * 32 + k]; Mt[c] = st[(S_M + c) * 32 + k];
+    }
 #pragma unroll
-      for (int c = 0; c < 4; ++c) Ci[c] = st[(S_CI + c) * 32 + k];
-      const TK pX = st[S_P * 32 + k], pY = st[(S_P + 1) * 32 + k];
-      const TK bv = st[S_BV * 32 + k], Wt = st[S_W * 32 + k];
+    for (int c = 0; c < 4; ++c) Ci[c] = st[(S_CI + c) * 32 + k];
+    const TK pX = st[S_P * 32 + k], pY = st[(S_P + 1) * 32 + k];
+    const TK bv = st[S_BV * 32 + k], Wt = st[S_W * 32 + k];
 
-      // Records of the neighbours (lane per neighbour).
-      for (int i = lane; i < n; i += 32) {
-        const int64_t e = p0 + i;
-        const TK dx = static_cast<TK>(dpsi_t[2 * e]), dy = static_cast<TK>(dpsi_t[2 * e + 1]);
-        const TK dxx = static_cast<TK>(ddpsi_t[3 * e]), dyy = static_cast<TK>(ddpsi_t[3 * e + 1]);
-        const TK dxy = static_cast<TK>(ddpsi_t[3 * e + 2]);
-        const TK c0 = Ci[0] * dx + Ci[1] * dy;
-        const TK c1 = Ci[2] * dx + Ci[3] * dy;
-        TK gI[3];
+    // Records of the neighbours (lane per neighbour).
+    for (int i = lane; i < n; i += 32) {
+      const int64_t e = p0 + i;
+      const TK dx = static_cast<TK>(dpsi_t[2 * e]), dy = static_cast<TK>(dpsi_t[2 * e + 1]);
+      const TK dxx = static_cast<TK>(ddpsi_t[3 * e]), dyy = static_cast<TK>(ddpsi_t[3 * e + 1]);
+      const TK dxy = static_cast<TK>(ddpsi_t[3 * e + 2]);
+      const TK c0 = Ci[0] * dx + Ci[1] * dy;
+      const TK c1 = Ci[2] * dx + Ci[3] * dy;
+      TK gI[3];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) gI[r] = a1t[r] * c0 + a2t[r] * c1;
-        const TK b0 = -dxx + (rxx[0] * gI[0] + rxx[1] * gI[1] + rxx[2] * gI[2]);
-        const TK b1 = -dyy + (ryy[0] * gI[0] + ryy[1] * gI[1] + ryy[2] * gI[2]);
-        const TK b2 = TK(2) * (-dxy + (rxy[0] * gI[0] + rxy[1] * gI[1] + rxy[2] * gI[2]));
-        const TK Tu = dx * pX + dy * pY - (dxx * Mt[0] + TK(2) * dxy * Mt[2] + dyy * Mt[1]);
-        TK* R = rec + i;
-        R[0 * nmax] = dx; R[1 * nmax] = dy;
-        R[2 * nmax] = b0; R[3 * nmax] = b1; R[4 * nmax] = b2;
-        R[5 * nmax] = Tu;
+      for (int r = 0; r < 3; ++r) gI[r] = a1t[r] * c0 + a2t[r] * c1;
+      const TK b0 = -dxx + (rxx[0] * gI[0] + rxx[1] * gI[1] + rxx[2] * gI[2]);
+      const TK b1 = -dyy + (ryy[0] * gI[0] + ryy[1] * gI[1] + ryy[2] * gI[2]);
+      const TK b2 = TK(2) * (-dxy + (rxy[0] * gI[0] + rxy[1] * gI[1] + rxy[2] * gI[2]));
+      const TK Tu = dx * pX + dy * pY - (dxx * Mt[0] + TK(2) * dxy * Mt[2] + dyy * Mt[1]);
+      TK* R = rec + i;
+      R[0 * nmax] = dx; R[1 * nmax] = dy;
+      R[2 * nmax] = b0; R[3 * nmax] = b1; R[4 * nmax] = b2;
+      R[5 * nmax] = Tu;
 #pragma unroll
-        for (int r = 0; r < 3; ++r) R[(6 + r) * nmax] = gI[r];
-        // P = A Bm + B Bb, Q = B Bm + D Bb (Assembly.h:255-256), times W:
-        //   P(r,c) = a1_c pa_r + a2_c pb_r + b_c pc_r.
+      for (int r = 0; r < 3; ++r) R[(6 + r) * nmax] = gI[r];
+      if constexpr (BZERO) {
+        // J side: pa(3) pb(3) qc(3) cW(2) nW(2) TuW, all times W.
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
           const TK Ar0 = static_cast<TK>(m.A[3 * r]), Ar1 = static_cast<TK>(m.A[3 * r + 1]), Ar2 = static_cast<TK>(m.A[3 * r + 2]);
-          const TK Br0 = static_cast<TK>(m.B[3 * r]), Br1 = static_cast<TK>(m.B[3 * r + 1]), Br2 = static_cast<TK>(m.B[3 * r + 2]);
           const TK Dr0 = static_cast<TK>(m.D[3 * r]), Dr1 = static_cast<TK>(m.D[3 * r + 1]), Dr2 = static_cast<TK>(m.D[3 * r + 2]);
-          const TK pa = (Ar0 * dx + Ar2 * dy) * Wt;
-          const TK pb = (Ar1 * dy + Ar2 * dx) * Wt;
-          const TK pc = (Br0 * b0 + Br1 * b1 + Br2 * b2) * Wt;
-          const TK qa = (Br0 * dx + Br2 * dy) * Wt;
-          const TK qb = (Br1 * dy + Br2 * dx) * Wt;
-          const TK qc = (Dr0 * b0 + Dr1 * b1 + Dr2 * b2) * Wt;
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            R[(kRecI + 3 * r + c) * nmax] = a1t[c] * pa + a2t[c] * pb + bt[c] * pc;
-            R[(kRecI + 9 + 3 * r + c) * nmax] = a1t[c] * qa + a2t[c] * qb + bt[c] * qc;
-          }
+          R[(kRecI + r) * nmax] = (Ar0 * dx + Ar2 * dy) * Wt;
+          R[(kRecI + 3 + r) * nmax] = (Ar1 * dy + Ar2 * dx) * Wt;
+          R[(kRecI + 6 + r) * nmax] = (Dr0 * b0 + Dr1 * b1 + Dr2 * b2) * Wt;
         }
-        R[(kRecI + 18) * nmax] = c0 * Wt;
-        R[(kRecI + 19) * nmax] = c1 * Wt;
-        R[(kRecI + 20) * nmax] = (Nt[0] * dx + Nt[2] * dy) * Wt;
-        R[(kRecI + 21) * nmax] = (Nt[2] * dx + Nt[1] * dy) * Wt;
-        R[(kRecI + 22) * nmax] = Tu * Wt;
-        nid[i] = a.idx[e];
-      }
-      __syncwarp();
-
-      // Pair loop: the n(n+1)/2 blocks of this point spread over the lanes.
-      const int64_t np = static_cast<int64_t>(n) * (n + 1) / 2;
-      const int64_t m0 = a.map_ptr[gg];
-      int i = 0, off = lane;
-      while (i < n && off >= n - i) { off -= n - i; ++i; }
-      for (int64_t p = lane; p < np; p += 32) {
-        const int j = i + off;
-        const TK* RI = rec + i;
-        const TK* RJ = rec + j;
-        const TK dxi = RI[0], dyi = RI[nmax], be0 = RI[2 * nmax], be1 = RI[3 * nmax], be2 = RI[4 * nmax];
-        const TK Tui = RI[5 * nmax], gi0 = RI[6 * nmax], gi1 = RI[7 * nmax], gi2 = RI[8 * nmax];
-        const TK cj0 = RJ[(kRecI + 18) * nmax], cj1 = RJ[(kRecI + 19) * nmax];
-        const TK nj0 = RJ[(kRecI + 20) * nmax], nj1 = RJ[(kRecI + 21) * nmax];
-        const TK TuWj = RJ[(kRecI + 22) * nmax];
-        const TK s1 = Tui * cj0, s2 = Tui * cj1;
-        const TK t3 = bv * (dxi * cj0 + dyi * cj1);
-        const TK geo = dxi * nj0 + dyi * nj1;
-        TK Y1[3], Y2[3], Y3[3];
+        R[(kRecI + 9) * nmax] = c0 * Wt;
+        R[(kRecI + 10) * nmax] = c1 * Wt;
+        R[(kRecI + 11) * nmax] = (Nt[0] * dx + Nt[2] * dy) * Wt;
+        R[(kRecI + 12) * nmax] = (Nt[2] * dx + Nt[1] * dy) * Wt;
+        R[(kRecI + 13) * nmax] = Tu * Wt;
+      } else {
+      // P = A Bm + B Bb, Q = B Bm + D Bb (Assembly.h:255-256), times W:
+      //   P(r,c) = a1_c pa_r + a2_c pb_r + b_c pc_r.
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const TK Ar0 = static_cast<TK>(m.A[3 * r]), Ar1 = static_cast<TK>(m.A[3 * r + 1]), Ar2 = static_cast<TK>(m.A[3 * r + 2]);
+        const TK Br0 = static_cast<TK>(m.B[3 * r]), Br1 = static_cast<TK>(m.B[3 * r + 1]), Br2 = static_cast<TK>(m.B[3 * r + 2]);
+        const TK Dr0 = static_cast<TK>(m.D[3 * r]), Dr1 = static_cast<TK>(m.D[3 * r + 1]), Dr2 = static_cast<TK>(m.D[3 * r + 2]);
+        const TK pa = (Ar0 * dx + Ar2 * dy) * Wt;
+        const TK pb = (Ar1 * dy + Ar2 * dx) * Wt;
+        const TK pc = (Br0 * b0 + Br1 * b1 + Br2 * b2) * Wt;
+        const TK qa = (Br0 * dx + Br2 * dy) * Wt;
+        const TK qb = (Br1 * dy + Br2 * dx) * Wt;
+        const TK qc = (Dr0 * b0 + Dr1 * b1 + Dr2 * b2) * Wt;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          const TK P0 = RJ[(kRecI + c) * nmax], P1 = RJ[(kRecI + 3 + c) * nmax], P2 = RJ[(kRecI + 6 + c) * nmax];
-          const TK Q0 = RJ[(kRecI + 9 + c) * nmax], Q1 = RJ[(kRecI + 12 + c) * nmax], Q2 = RJ[(kRecI + 15 + c) * nmax];
-          const TK gic = c == 0 ? gi0 : (c == 1 ? gi1 : gi2);
-          Y1[c] = dxi * P0 + dyi * P2 - s1 * bt[c];
-          Y2[c] = dyi * P1 + dxi * P2 - s2 * bt[c];
-          Y3[c] = be0 * Q0 + be1 * Q1 + be2 * Q2 + t3 * bt[c] - TuWj * gic;
+          R[(kRecI + 3 * r + c) * nmax] = a1t[c] * pa + a2t[c] * pb + bt[c] * pc;
+          R[(kRecI + 9 + 3 * r + c) * nmax] = a1t[c] * qa + a2t[c] * qb + bt[c] * qc;
         }
-        TK v[9];
+      }
+      R[(kRecI + 18) * nmax] = c0 * Wt;
+      R[(kRecI + 19) * nmax] = c1 * Wt;
+      R[(kRecI + 20) * nmax] = (Nt[0] * dx + Nt[2] * dy) * Wt;
+      R[(kRecI + 21) * nmax] = (Nt[2] * dx + Nt[1] * dy) * Wt;
+      R[(kRecI + 22) * nmax] = Tu * Wt;
+      }
+      nid[i] = a.idx[e];
+    }
+    __syncwarp();
+
+    // Pair loop: the n(n+1)/2 blocks of this point spread over the lanes.
+    const int64_t np = static_cast<int64_t>(n) * (n + 1) / 2;
+    const int64_t m0 = a.map_ptr[gg];
+    int i = 0, off = lane;
+    while (i < n && off >= n - i) { off -= n - i; ++i; }
+    for (int64_t p = lane; p < np; p += 32) {
+      const int j = i + off;
+      const TK* RI = rec + i;
+      const TK* RJ = rec + j;
+      const TK dxi = RI[0], dyi = RI[nmax], be0 = RI[2 * nmax], be1 = RI[3 * nmax], be2 = RI[4 * nmax];
+      const TK Tui = RI[5 * nmax], gi0 = RI[6 * nmax], gi1 = RI[7 * nmax], gi2 = RI[8 * nmax];
+      TK v[9];
+      if constexpr (BZERO) {
+        const TK pa0 = RJ[kRecI * nmax], pa1 = RJ[(kRecI + 1) * nmax], pa2 = RJ[(kRecI + 2) * nmax];
+        const TK pb0 = RJ[(kRecI + 3) * nmax], pb1 = RJ[(kRecI + 4) * nmax], pb2 = RJ[(kRecI + 5) * nmax];
+        const TK qc0 = RJ[(kRecI + 6) * nmax], qc1 = RJ[(kRecI + 7) * nmax], qc2 = RJ[(kRecI + 8) * nmax];
+        const TK cj0 = RJ[(kRecI + 9) * nmax], cj1 = RJ[(kRecI + 10) * nmax];
+        const TK nj0 = RJ[(kRecI + 11) * nmax], nj1 = RJ[(kRecI + 12) * nmax];
+        const TK TuWj = RJ[(kRecI + 13) * nmax];
+        const TK s1 = Tui * cj0, s2 = Tui * cj1;
+        const TK geo = dxi * nj0 + dyi * nj1;
+        const TK z11 = dxi * pa0 + dyi * pa2, z12 = dxi * pb0 + dyi * pb2;
+        const TK z21 = dyi * pa1 + dxi * pa2, z22 = dyi * pb1 + dxi * pb2;
+        const TK z33 = be0 * qc0 + be1 * qc1 + be2 * qc2 + bv * (dxi * cj0 + dyi * cj1);
+        TK Y1[3], Y2[3], Y3[3];
+        const TK gi[3] = {gi0, gi1, gi2};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          Y1[c] = a1t[c] * z11 + a2t[c] * z12 - s1 * bt[c];
+          Y2[c] = a1t[c] * z21 + a2t[c] * z22 - s2 * bt[c];
+          Y3[c] = bt[c] * z33 - TuWj * gi[c];
+        }
 #pragma unroll
         for (int r = 0; r < 3; ++r)
 #pragma unroll
           for (int c = 0; c < 3; ++c)
             v[3 * r + c] = a1t[r] * Y1[c] + a2t[r] * Y2[c] + bt[r] * Y3[c] + (r == c ? geo : TK(0));
-        const bool flip = nid[i] > nid[j];
-        if (DET) {
-          store_contrib<TK>(a.Kc, m0 + p, flip, v);
-        } else if (POS_MAP) {
-          const int hi = flip ? nid[i] : nid[j];
-          scatter_atomic<TK>(a.Kacc, a.outer[3 * static_cast<int64_t>(hi)] / 9 + a.map_slot[m0 + p], flip, v);
-        } else {
-          scatter_atomic<TK>(a.Kacc, a.map_slot[m0 + p], flip, v);
-        }
-        off += 32;
-        while (i < n && off >= n - i) { off -= n - i; ++i; }
+      } else {
+      const TK cj0 = RJ[(kRecI + 18) * nmax], cj1 = RJ[(kRecI + 19) * nmax];
+      const TK nj0 = RJ[(kRecI + 20) * nmax], nj1 = RJ[(kRecI + 21) * nmax];
+      const TK TuWj = RJ[(kRecI + 22) * nmax];
+      const TK s1 = Tui * cj0, s2 = Tui * cj1;
+      const TK t3 = bv * (dxi * cj0 + dyi * cj1);
+      const TK geo = dxi * nj0 + dyi * nj1;
+      TK Y1[3], Y2[3], Y3[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const TK P0 = RJ[(kRecI + c) * nmax], P1 = RJ[(kRecI + 3 + c) * nmax], P2 = RJ[(kRecI + 6 + c) * nmax];
+        const TK Q0 = RJ[(kRecI + 9 + c) * nmax], Q1 = RJ[(kRecI + 12 + c) * nmax], Q2 = RJ[(kRecI + 15 + c) * nmax];
+        const TK gic = c == 0 ? gi0 : (c == 1 ? gi1 : gi2);
+        Y1[c] = dxi * P0 + dyi * P2 - s1 * bt[c];
+        Y2[c] = dyi * P1 + dxi * P2 - s2 * bt[c];
+        Y3[c] = be0 * Q0 + be1 * Q1 + be2 * Q2 + t3 * bt[c] - TuWj * gic;
       }
-      __syncwarp();
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          v[3 * r + c] = a1t[r] * Y1[c] + a2t[r] * Y2[c] + bt[r] * Y3[c] + (r == c ? geo : TK(0));
+      }
+      const bool flip = nid[i] > nid[j];
+      if (DET) {
+        store_contrib<TK>(a.Kc, m0 + p, flip, v);
+      } else if (POS_MAP) {
+        const int hi = flip ? nid[i] : nid[j];
+        scatter_atomic<TK>(a.Kacc, a.outer[3 * static_cast<int64_t>(hi)] / 9 + a.map_slot[m0 + p], flip, v);
+      } else {
+        scatter_atomic<TK>(a.Kacc, a.map_slot[m0 + p], flip, v);
+      }
+      off += 32;
+      while (i < n && off >= n - i) { off -= n - i; ++i; }
     }
+    __syncwarp();
+  }
+}
+
+template <typename TK, bool DET, bool WANT_K, typename TIN = TK, bool POS_MAP = false, bool BZERO = false>
+__global__ void __launch_bounds__(32 * kFaceWarps, sizeof(TK) == 4 ? 5 : 3) face_kernel(FaceArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nmax = a.nmax;
+  TK* base_w = reinterpret_cast<TK*>(smem_raw) + static_cast<size_t>(w) * (kState * 32 + kRec * nmax);
+  TK* st = base_w;                 // [kState][32]
+  TK* rec = base_w + kState * 32;  // [kRec][nmax]
+  int* nid = reinterpret_cast<int*>(reinterpret_cast<TK*>(smem_raw) +
+                                    static_cast<size_t>(kFaceWarps) * (kState * 32 + kRec * nmax)) + w * nmax;
+  // Each warp owns 32 consecutive Gauss points per round.
+  for (int g0 = (blockIdx.x * kFaceWarps + w) * 32; g0 < a.n_gp; g0 += gridDim.x * kFaceWarps * 32) {
+    // Phase 1: one Gauss point per lane, FP64. Every lane does distinct work, so no FP64
+    // issue slot is spent on a redundant or masked copy (on GB300 an FP64 warp
+    // instruction costs the same with 1 or 32 lanes).
+    phase1_point<TK, DET>(a, g0, lane, WANT_K ? st : static_cast<TK*>(nullptr), 32, lane);
+    if (!WANT_K) continue;
+    __syncwarp();
+    phase2_group<TK, DET, TIN, POS_MAP, BZERO>(a, g0, lane, st, rec, nid);
+  }
+}
+
+// The same work as two kernels, each sized for its own occupancy: the residual kernel
+// (phase 1, one Gauss point per thread, FP64 bound) writes the per-point state to
+// global memory ([field][n_gp]); the tangent kernel (phase 2) stages 32 points' states
+// in shared memory and runs the pair loop.
+template <typename TK, bool DET, bool STORE>
+__global__ void __launch_bounds__(256) face_residual_kernel(FaceArgs a, TK* gstate) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g - lane < a.n_gp; g += stride)
+    phase1_point<TK, DET>(a, static_cast<int>(g - lane), lane, STORE ? gstate : static_cast<TK*>(nullptr),
+                          a.n_gp, g);
+}
+
+constexpr int kTanWarps = 4;
+
+template <typename TK, bool DET, bool BZERO>
+__global__ void __launch_bounds__(32 * kTanWarps) face_tangent_kernel(FaceArgs a, const TK* __restrict__ gstate) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nmax = a.nmax;
+  TK* base_w = reinterpret_cast<TK*>(smem_raw) + static_cast<size_t>(w) * (kState * 32 + kRec * nmax);
+  TK* st = base_w;
+  TK* rec = base_w + kState * 32;
+  int* nid = reinterpret_cast<int*>(reinterpret_cast<TK*>(smem_raw) +
+                                    static_cast<size_t>(kTanWarps) * (kState * 32 + kRec * nmax)) + w * nmax;
+  for (int g0 = (blockIdx.x * kTanWarps + w) * 32; g0 < a.n_gp; g0 += gridDim.x * kTanWarps * 32) {
+    const int g = g0 + lane;
+#pragma unroll 4
+    for (int f = 0; f < kState; ++f) st[f * 32 + lane] = g < a.n_gp ? gstate[static_cast<int64_t>(f) * a.n_gp + g] : TK(0);
+    __syncwarp();
+    phase2_group<TK, DET, TK, false, BZERO>(a, g0, lane, st, rec, nid);
   }
 }
 
@@ -792,6 +907,52 @@ void ensure_fp32_shapes(cgb_assembler* a) {
   CGB_CUDA(cudaGetLastError());
 }
 
+// Sliced-ELL copy of the face neighbour data for phase 1: groups of 32 consecutive Gauss
+// points, each group padded to its longest list; entry q of point 32 W + l at
+// sell_ptr[W] + 32 q + l. Padding entries are never read (q < n of the point).
+__global__ void fill_sell(int n_gp, const int64_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                          const double* __restrict__ dpsi, const double* __restrict__ ddpsi,
+                          const int64_t* __restrict__ sell_ptr, int32_t* __restrict__ sidx,
+                          double* __restrict__ sdpsi, double* __restrict__ sddpsi) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_gp) return;
+  const int64_t base = sell_ptr[g >> 5] + (g & 31);
+  for (int64_t e = ptr[g], q = 0; e < ptr[g + 1]; ++e, ++q) {
+    const int64_t d = base + 32 * q;
+    sidx[d] = idx[e];
+    sdpsi[2 * d] = dpsi[2 * e];
+    sdpsi[2 * d + 1] = dpsi[2 * e + 1];
+    sddpsi[3 * d] = ddpsi[3 * e];
+    sddpsi[3 * d + 1] = ddpsi[3 * e + 1];
+    sddpsi[3 * d + 2] = ddpsi[3 * e + 2];
+  }
+}
+
+void ensure_sell(cgb_assembler* a) {
+  if (a->sell_ptr.p) return;
+  const cgb_shape* S = a->faces;
+  cudaStream_t st = a->ctx->stream;
+  std::vector<int64_t> ptr(S->n_gp + 1);
+  CGB_CUDA(cudaMemcpyAsync(ptr.data(), S->nbr_ptr.p, ptr.size() * 8, cudaMemcpyDeviceToHost, st));
+  CGB_CUDA(cudaStreamSynchronize(st));
+  const int ngroups = (S->n_gp + 31) / 32;
+  std::vector<int64_t> sp(ngroups + 1, 0);
+  for (int W = 0; W < ngroups; ++W) {
+    int64_t mx = 0;
+    for (int g = 32 * W; g < std::min(S->n_gp, 32 * W + 32); ++g) mx = std::max(mx, ptr[g + 1] - ptr[g]);
+    sp[W + 1] = sp[W] + 32 * mx;
+  }
+  upload(a->sell_ptr, sp.data(), sp.size(), st);
+  a->sidx.alloc(sp[ngroups]);
+  a->sdpsi.alloc(2 * sp[ngroups]);
+  a->sddpsi.alloc(3 * sp[ngroups]);
+  CGB_CUDA(cudaMemsetAsync(a->sidx.p, 0, a->sidx.bytes(), st));
+  if (S->n_gp)
+    fill_sell<<<nb(S->n_gp, 128), 128, 0, st>>>(S->n_gp, S->nbr_ptr.p, S->nbr_idx.p, S->dpsi.p, S->ddpsi.p,
+                                                a->sell_ptr.p, a->sidx.p, a->sdpsi.p, a->sddpsi.p);
+  CGB_CUDA(cudaGetLastError());
+}
+
 }  // namespace
 
 void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags) {
@@ -844,6 +1005,8 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   fa.ptr = S->nbr_ptr.p; fa.idx = S->nbr_idx.p; fa.dpsi = S->dpsi.p; fa.ddpsi = S->ddpsi.p;
   fa.weight = a->weight.p; fa.x = d_x;
   fa.map_ptr = a->map_ptr.p; fa.map_slot = a->map_slot.p;
+  ensure_sell(a);
+  fa.sell_ptr = a->sell_ptr.p; fa.sidx = a->sidx.p; fa.sdpsi = a->sdpsi.p; fa.sddpsi = a->sddpsi.p;
   std::memcpy(fa.mat.A, a->A, sizeof a->A); std::memcpy(fa.mat.B, a->B, sizeof a->B); std::memcpy(fa.mat.D, a->D, sizeof a->D);
   fa.F = d_F;
   fa.Fc = a->fcontrib.p;
@@ -864,20 +1027,53 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     throw Error(CGB_ERR_CAPACITY, "assemble: " + std::to_string(S->max_n) + " neighbours per Gauss point exceed the shared-memory staging");
   const int sms = sm_count(ctx->device);
   const unsigned grid = std::max(1u, std::min(nb(S->n_gp, 32 * kFaceWarps), static_cast<unsigned>(sms * 8)));
-  auto launch = [&](auto kern) {
-    if (smem > 48 * 1024) CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    prof_begin(ctx, CGB_PHASE_FACE);
-    if (S->n_gp) kern<<<grid, 32 * kFaceWarps, smem, st>>>(fa);
-    prof_end(ctx, CGB_PHASE_FACE, S->n_gp ? 1 : 0);
-  };
-  if (mixed) {
-    if (det) { if (want_K) launch(face_kernel<float, true, true>); else launch(face_kernel<float, true, false>); }
-    else { if (want_K) launch(face_kernel<float, false, true>); else launch(face_kernel<float, false, false>); }
-  } else {
-    if (det) { if (want_K) launch(face_kernel<double, true, true>); else launch(face_kernel<double, true, false>); }
-    else { if (want_K) launch(face_kernel<double, false, true>); else launch(face_kernel<double, false, false>); }
+  (void)grid;
+  bool bzero = true;
+  for (double v : a->B) bzero = bzero && (v == 0.0);
+  // Residual kernel (phase 1) then tangent kernel (phase 2), each at its own occupancy.
+  const size_t state_bytes = static_cast<size_t>(kState) * std::max(S->n_gp, 1) * tk;
+  if (want_K) {
+    if (mixed) a->state32.ensure(state_bytes / sizeof(float));
+    else a->state64.ensure(state_bytes / sizeof(double));
   }
-  CGB_CUDA(cudaGetLastError());
+  float* st32 = a->state32.p;
+  double* st64 = a->state64.p;
+  const unsigned rgrid = std::max(1u, std::min(nb(S->n_gp, 256), static_cast<unsigned>(sms * 16)));
+  prof_begin(ctx, CGB_PHASE_FACE);
+  int nface = 0;
+  if (S->n_gp) {
+    if (mixed) {
+      if (det) { if (want_K) face_residual_kernel<float, true, true><<<rgrid, 256, 0, st>>>(fa, st32);
+                 else face_residual_kernel<float, true, false><<<rgrid, 256, 0, st>>>(fa, st32); }
+      else { if (want_K) face_residual_kernel<float, false, true><<<rgrid, 256, 0, st>>>(fa, st32);
+             else face_residual_kernel<float, false, false><<<rgrid, 256, 0, st>>>(fa, st32); }
+    } else {
+      if (det) { if (want_K) face_residual_kernel<double, true, true><<<rgrid, 256, 0, st>>>(fa, st64);
+                 else face_residual_kernel<double, true, false><<<rgrid, 256, 0, st>>>(fa, st64); }
+      else { if (want_K) face_residual_kernel<double, false, true><<<rgrid, 256, 0, st>>>(fa, st64);
+             else face_residual_kernel<double, false, false><<<rgrid, 256, 0, st>>>(fa, st64); }
+    }
+    ++nface;
+    CGB_CUDA(cudaGetLastError());
+    if (want_K) {
+      const size_t tsm = static_cast<size_t>(kTanWarps) * ((kState * 32 + kRec * fa.nmax) * tk + fa.nmax * sizeof(int));
+      const unsigned tgrid = std::max(1u, std::min(nb(S->n_gp, 32 * kTanWarps), static_cast<unsigned>(sms * 16)));
+      auto tl = [&](auto kern, auto* stp) {
+        if (tsm > 48 * 1024) CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tsm)));
+        kern<<<tgrid, 32 * kTanWarps, tsm, st>>>(fa, stp);
+      };
+      if (mixed) {
+        if (det) { if (bzero) tl(face_tangent_kernel<float, true, true>, st32); else tl(face_tangent_kernel<float, true, false>, st32); }
+        else { if (bzero) tl(face_tangent_kernel<float, false, true>, st32); else tl(face_tangent_kernel<float, false, false>, st32); }
+      } else {
+        if (det) { if (bzero) tl(face_tangent_kernel<double, true, true>, st64); else tl(face_tangent_kernel<double, true, false>, st64); }
+        else { if (bzero) tl(face_tangent_kernel<double, false, true>, st64); else tl(face_tangent_kernel<double, false, false>, st64); }
+      }
+      ++nface;
+      CGB_CUDA(cudaGetLastError());
+    }
+  }
+  prof_end(ctx, CGB_PHASE_FACE, nface);
 
   // Hinge.
   if (hinge) {

@@ -154,6 +154,11 @@ struct cgb_assembler {
   cgb::DevBuf<double> K;            // 9 n_blocks (device scratch for host-buffer calls)
   cgb::DevBuf<double> x;            // 3 n_nodes
   cgb::DevBuf<float> dpsi32, ddpsi32; // FP32 copies of the face shape derivatives (mixed mode)
+  cgb::DevBuf<float> state32;         // per-point state between the residual and tangent kernels
+  cgb::DevBuf<double> state64;
+  cgb::DevBuf<int64_t> sell_ptr;      // sliced-ELL copy for the FP64 phase (groups of 32 points)
+  cgb::DevBuf<int32_t> sidx;
+  cgb::DevBuf<double> sdpsi, sddpsi;
   // Deterministic scatter: per pair contributions and per-block ordered lists.
   bool det_ready = false;
   cgb::DevBuf<int64_t> blk_list_ptr;  // n_blocks + 1
