@@ -48,6 +48,7 @@ struct Material { double A[9], B[9], D[9]; };
 
 struct FaceArgs {
   int n_gp;
+  int g_begin, g_end;  // the Gauss points [g_begin, g_end) of this launch (multiples of 32 apart)
   int nmax;
   const int64_t* ptr;
   const int32_t* idx;
@@ -201,7 +202,7 @@ __device__ __forceinline__ void phase1_point(const FaceArgs& a, int g0, int lane
                                              int64_t st_idx) {
   const Material& m = a.mat;
   const int g = g0 + lane;
-  if (g < a.n_gp) {
+  if (g < a.g_end) {
       const int64_t p0 = a.ptr[g];
       const int n = static_cast<int>(a.ptr[g + 1] - p0);
       // Entry q of this lane's point: CSR p0 + q, or sliced-ELL sb + 32 q (coalesced
@@ -290,7 +291,7 @@ __device__ __forceinline__ void phase2_group(const FaceArgs& a, int g0, int lane
   const int nmax = a.nmax;
   const TIN* dpsi_t = static_cast<const TIN*>(a.dpsi_t);
   const TIN* ddpsi_t = static_cast<const TIN*>(a.ddpsi_t);
-  const int kend = min(32, a.n_gp - g0);
+  const int kend = min(32, a.g_end - g0);
   for (int k = 0; k < kend; ++k) {
     const int gg = g0 + k;
     const int64_t p0 = a.ptr[gg];
@@ -480,7 +481,8 @@ template <typename TK, bool DET, bool STORE>
 __global__ void __launch_bounds__(256) face_residual_kernel(FaceArgs a, TK* gstate) {
   const int lane = threadIdx.x & 31;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g - lane < a.n_gp; g += stride)
+  for (int64_t g = a.g_begin + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g - lane < a.g_end;
+       g += stride)
     phase1_point<TK, DET>(a, static_cast<int>(g - lane), lane, STORE ? gstate : static_cast<TK*>(nullptr),
                           a.n_gp, g);
 }
@@ -497,10 +499,10 @@ __global__ void __launch_bounds__(32 * kTanWarps) face_tangent_kernel(FaceArgs a
   TK* rec = base_w + kState * 32;
   int* nid = reinterpret_cast<int*>(reinterpret_cast<TK*>(smem_raw) +
                                     static_cast<size_t>(kTanWarps) * (kState * 32 + kRec * nmax)) + w * nmax;
-  for (int g0 = (blockIdx.x * kTanWarps + w) * 32; g0 < a.n_gp; g0 += gridDim.x * kTanWarps * 32) {
+  for (int g0 = a.g_begin + (blockIdx.x * kTanWarps + w) * 32; g0 < a.g_end; g0 += gridDim.x * kTanWarps * 32) {
     const int g = g0 + lane;
 #pragma unroll 4
-    for (int f = 0; f < kState; ++f) st[f * 32 + lane] = g < a.n_gp ? gstate[static_cast<int64_t>(f) * a.n_gp + g] : TK(0);
+    for (int f = 0; f < kState; ++f) st[f * 32 + lane] = g < a.g_end ? gstate[static_cast<int64_t>(f) * a.n_gp + g] : TK(0);
     __syncwarp();
     phase2_group<TK, DET, TK, false, BZERO>(a, g0, lane, st, rec, nid);
   }
@@ -856,6 +858,228 @@ __global__ void hinge_energy_kernel(HingeArgs a, double* out) {
   atomicAdd(out, a.weight[g] * (0.5 * a.Kt * (d * d)));
 }
 
+// ---- FP32 tangent with merged contributions ------------------------------------------
+// One CTA per group of kMG consecutive Gauss points. The CTA builds the group's
+// per-neighbour records (AoS, 16-byte rows) and point frames in shared memory, then each
+// thread takes distinct blocks ("entries") of the group, sums every contribution to its
+// block in registers (in a fixed order: point, then local pair) and scatters it once with
+// three 16-byte vector atomics. On GB300 a scattered 48-byte block costs ~14 ns of L2
+// atomic throughput per SM-slot (~70 G blocks/s for the chip); merging the ~7.5
+// contributions per block of a 4x4 quadrature cell divides that traffic accordingly.
+constexpr int kMG = 16;          // points per group (the setup kernel uses the same)
+constexpr int kMrgThreads = 256;
+
+struct MergeArgs {
+  const int64_t* ent_ptr;
+  const int32_t* ent_slot;
+  const int32_t* ent_cstart;  // (count << 16) | first contribution
+  const int8_t* direct;
+  const uint16_t* code;       // point (4) | i (6) | j (6)
+};
+
+// The block of the local pair (i, j) of one point from the frame (fr[0..2]), the
+// I-side record (ri[0..2]) and the J-side record (rj), as in phase2_group.
+template <bool BZERO>
+__device__ __forceinline__ void merged_pair(const float4* fr, const float4* ri, const float4* rj, float v[9]) {
+  const float4 f0 = fr[0], f1 = fr[1], f2 = fr[2];
+  const float a1t[3] = {f0.x, f0.y, f0.z}, a2t[3] = {f1.x, f1.y, f1.z}, bt[3] = {f2.x, f2.y, f2.z};
+  const float bv = f0.w;
+  const float4 i0 = ri[0], i1 = ri[1], i2 = ri[2];
+  const float dxi = i0.x, dyi = i0.y, be0 = i0.z, be1 = i0.w, be2 = i1.x, Tui = i1.y;
+  const float gi[3] = {i1.z, i1.w, i2.x};
+  float Y1[3], Y2[3], Y3[3], geo;
+  if constexpr (BZERO) {
+    const float4 j0 = rj[0], j1 = rj[1], j2 = rj[2], j3 = rj[3];
+    const float pa0 = j0.x, pa1 = j0.y, pa2 = j0.z, pb0 = j0.w, pb1 = j1.x, pb2 = j1.y;
+    const float qc0 = j1.z, qc1 = j1.w, qc2 = j2.x, cj0 = j2.y, cj1 = j2.z, nj0 = j2.w, nj1 = j3.x, TuWj = j3.y;
+    const float s1 = Tui * cj0, s2 = Tui * cj1;
+    geo = dxi * nj0 + dyi * nj1;
+    const float z11 = dxi * pa0 + dyi * pa2, z12 = dxi * pb0 + dyi * pb2;
+    const float z21 = dyi * pa1 + dxi * pa2, z22 = dyi * pb1 + dxi * pb2;
+    const float z33 = be0 * qc0 + be1 * qc1 + be2 * qc2 + bv * (dxi * cj0 + dyi * cj1);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      Y1[c] = a1t[c] * z11 + a2t[c] * z12 - s1 * bt[c];
+      Y2[c] = a1t[c] * z21 + a2t[c] * z22 - s2 * bt[c];
+      Y3[c] = bt[c] * z33 - TuWj * gi[c];
+    }
+  } else {
+    float J[24];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const float4 t = rj[q];
+      J[4 * q] = t.x; J[4 * q + 1] = t.y; J[4 * q + 2] = t.z; J[4 * q + 3] = t.w;
+    }
+    const float cj0 = J[18], cj1 = J[19], nj0 = J[20], nj1 = J[21], TuWj = J[22];
+    const float s1 = Tui * cj0, s2 = Tui * cj1;
+    const float t3 = bv * (dxi * cj0 + dyi * cj1);
+    geo = dxi * nj0 + dyi * nj1;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      Y1[c] = dxi * J[c] + dyi * J[6 + c] - s1 * bt[c];
+      Y2[c] = dyi * J[3 + c] + dxi * J[6 + c] - s2 * bt[c];
+      Y3[c] = be0 * J[9 + c] + be1 * J[12 + c] + be2 * J[15 + c] + t3 * bt[c] - TuWj * gi[c];
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[3 * r + c] = a1t[r] * Y1[c] + a2t[r] * Y2[c] + bt[r] * Y3[c] + (r == c ? geo : 0.0f);
+}
+
+template <bool BZERO>
+__global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(FaceArgs a, const float* __restrict__ gstate,
+                                                                            MergeArgs mg) {
+  constexpr int JW = BZERO ? 4 : 6;  // float4 rows of a J-side record
+  extern __shared__ __align__(16) float msm[];
+  const int nmax = a.nmax;
+  float* st = msm;                                          // [kState][kMG]
+  float4* fr = reinterpret_cast<float4*>(st + kState * kMG); // [kMG][3]
+  float4* ri = fr + 3 * kMG;                                // [kMG * nmax][3]
+  float4* rj = ri + 3 * kMG * nmax;                         // [kMG * nmax][JW]
+  int* nid = reinterpret_cast<int*>(rj + JW * kMG * nmax);  // [kMG * nmax]
+  const float* dpsi_t = static_cast<const float*>(a.dpsi_t);
+  const float* ddpsi_t = static_cast<const float*>(a.ddpsi_t);
+  const Material& m = a.mat;
+  // Groups of this launch: [g_begin, g_end) are multiples of kMG apart (chunk bounds are
+  // multiples of 32), so a group never straddles two launches.
+  const int G1 = (a.g_end + kMG - 1) / kMG;
+  for (int G = a.g_begin / kMG + blockIdx.x; G < G1; G += gridDim.x) {
+    const int g0 = G * kMG;
+    const int kn = min(kMG, a.g_end - g0);
+    for (int t = threadIdx.x; t < kState * kMG; t += blockDim.x) {
+      const int f = t / kMG, k = t - f * kMG;
+      st[t] = k < kn ? gstate[static_cast<int64_t>(f) * a.n_gp + g0 + k] : 0.0f;
+    }
+    __syncthreads();
+    if (threadIdx.x < kn) {
+      const int k = threadIdx.x;
+      fr[3 * k] = make_float4(st[(S_A1) * kMG + k], st[(S_A1 + 1) * kMG + k], st[(S_A1 + 2) * kMG + k], st[S_BV * kMG + k]);
+      fr[3 * k + 1] = make_float4(st[(S_A2) * kMG + k], st[(S_A2 + 1) * kMG + k], st[(S_A2 + 2) * kMG + k], 0.0f);
+      fr[3 * k + 2] = make_float4(st[(S_B) * kMG + k], st[(S_B + 1) * kMG + k], st[(S_B + 2) * kMG + k], 0.0f);
+    }
+    // Records of every (point, neighbour) of the group (the same formulas as phase2_group).
+    for (int t = threadIdx.x; t < kMG * nmax; t += blockDim.x) {
+      const int k = t / nmax, i = t - k * nmax;
+      if (k >= kn) continue;
+      const int64_t p0 = a.ptr[g0 + k];
+      if (i >= a.ptr[g0 + k + 1] - p0) continue;
+      const int64_t e = p0 + i;
+      const float a1t[3] = {st[S_A1 * kMG + k], st[(S_A1 + 1) * kMG + k], st[(S_A1 + 2) * kMG + k]};
+      const float a2t[3] = {st[S_A2 * kMG + k], st[(S_A2 + 1) * kMG + k], st[(S_A2 + 2) * kMG + k]};
+      const float bt[3] = {st[S_B * kMG + k], st[(S_B + 1) * kMG + k], st[(S_B + 2) * kMG + k]};
+      float rxx[3], ryy[3], rxy[3], Nt[3], Mt[3], Ci[4];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        rxx[c] = st[(S_RXX + c) * kMG + k]; ryy[c] = st[(S_RYY + c) * kMG + k]; rxy[c] = st[(S_RXY + c) * kMG + k];
+        Nt[c] = st[(S_N + c) * kMG + k]; Mt[c] = st[(S_M + c) * kMG + k];
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) Ci[c] = st[(S_CI + c) * kMG + k];
+      const float pX = st[S_P * kMG + k], pY = st[(S_P + 1) * kMG + k], Wt = st[S_W * kMG + k];
+      const float dx = dpsi_t[2 * e], dy = dpsi_t[2 * e + 1];
+      const float dxx = ddpsi_t[3 * e], dyy = ddpsi_t[3 * e + 1], dxy = ddpsi_t[3 * e + 2];
+      const float c0 = Ci[0] * dx + Ci[1] * dy, c1 = Ci[2] * dx + Ci[3] * dy;
+      float gI[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) gI[r] = a1t[r] * c0 + a2t[r] * c1;
+      const float b0 = -dxx + (rxx[0] * gI[0] + rxx[1] * gI[1] + rxx[2] * gI[2]);
+      const float b1 = -dyy + (ryy[0] * gI[0] + ryy[1] * gI[1] + ryy[2] * gI[2]);
+      const float b2 = 2.0f * (-dxy + (rxy[0] * gI[0] + rxy[1] * gI[1] + rxy[2] * gI[2]));
+      const float Tu = dx * pX + dy * pY - (dxx * Mt[0] + 2.0f * dxy * Mt[2] + dyy * Mt[1]);
+      float4* RI = ri + 3 * t;
+      RI[0] = make_float4(dx, dy, b0, b1);
+      RI[1] = make_float4(b2, Tu, gI[0], gI[1]);
+      RI[2] = make_float4(gI[2], 0.0f, 0.0f, 0.0f);
+      float4* RJ = rj + JW * t;
+      if constexpr (BZERO) {
+        float pa[3], pb[3], qc[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          pa[r] = (static_cast<float>(m.A[3 * r]) * dx + static_cast<float>(m.A[3 * r + 2]) * dy) * Wt;
+          pb[r] = (static_cast<float>(m.A[3 * r + 1]) * dy + static_cast<float>(m.A[3 * r + 2]) * dx) * Wt;
+          qc[r] = (static_cast<float>(m.D[3 * r]) * b0 + static_cast<float>(m.D[3 * r + 1]) * b1 +
+                   static_cast<float>(m.D[3 * r + 2]) * b2) * Wt;
+        }
+        RJ[0] = make_float4(pa[0], pa[1], pa[2], pb[0]);
+        RJ[1] = make_float4(pb[1], pb[2], qc[0], qc[1]);
+        RJ[2] = make_float4(qc[2], c0 * Wt, c1 * Wt, (Nt[0] * dx + Nt[2] * dy) * Wt);
+        RJ[3] = make_float4((Nt[2] * dx + Nt[1] * dy) * Wt, Tu * Wt, 0.0f, 0.0f);
+      } else {
+        float J[24];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          const float Ar0 = static_cast<float>(m.A[3 * r]), Ar1 = static_cast<float>(m.A[3 * r + 1]), Ar2 = static_cast<float>(m.A[3 * r + 2]);
+          const float Br0 = static_cast<float>(m.B[3 * r]), Br1 = static_cast<float>(m.B[3 * r + 1]), Br2 = static_cast<float>(m.B[3 * r + 2]);
+          const float Dr0 = static_cast<float>(m.D[3 * r]), Dr1 = static_cast<float>(m.D[3 * r + 1]), Dr2 = static_cast<float>(m.D[3 * r + 2]);
+          const float pa = (Ar0 * dx + Ar2 * dy) * Wt, pb = (Ar1 * dy + Ar2 * dx) * Wt, pc = (Br0 * b0 + Br1 * b1 + Br2 * b2) * Wt;
+          const float qa = (Br0 * dx + Br2 * dy) * Wt, qb = (Br1 * dy + Br2 * dx) * Wt, qc = (Dr0 * b0 + Dr1 * b1 + Dr2 * b2) * Wt;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            J[3 * r + c] = a1t[c] * pa + a2t[c] * pb + bt[c] * pc;
+            J[9 + 3 * r + c] = a1t[c] * qa + a2t[c] * qb + bt[c] * qc;
+          }
+        }
+        J[18] = c0 * Wt; J[19] = c1 * Wt;
+        J[20] = (Nt[0] * dx + Nt[2] * dy) * Wt; J[21] = (Nt[2] * dx + Nt[1] * dy) * Wt;
+        J[22] = Tu * Wt; J[23] = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) RJ[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
+      }
+      nid[t] = a.idx[e];
+    }
+    __syncthreads();
+    float4* acc4 = static_cast<float4*>(a.Kacc);
+    const int64_t cbase = a.map_ptr[g0];
+    if (mg.direct[G]) {
+      // Too many pairs for the setup's shared-memory sort: scatter pair by pair.
+      for (int k = 0; k < kn; ++k) {
+        const int n = static_cast<int>(a.ptr[g0 + k + 1] - a.ptr[g0 + k]);
+        const int np = n * (n + 1) / 2;
+        const int64_t m0 = a.map_ptr[g0 + k];
+        for (int p = threadIdx.x; p < np; p += blockDim.x) {
+          int i = 0, off = p;
+          while (off >= n - i) { off -= n - i; ++i; }
+          const int j = i + off;
+          float v[9];
+          merged_pair<BZERO>(fr + 3 * k, ri + 3 * (k * nmax + i), rj + JW * (k * nmax + j), v);
+          scatter_atomic<float>(a.Kacc, a.map_slot[m0 + p], nid[k * nmax + i] > nid[k * nmax + j], v);
+        }
+      }
+    } else {
+      const int64_t e0 = mg.ent_ptr[G];
+      const int ne = static_cast<int>(mg.ent_ptr[G + 1] - e0);
+      for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+        const int cs = mg.ent_cstart[e0 + e];
+        const int cnt = cs >> 16, c0 = cs & 0xffff;
+        float acc[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) acc[q] = 0.0f;
+        for (int c = 0; c < cnt; ++c) {
+          const unsigned code = mg.code[cbase + c0 + c];
+          const int k = code >> 12, i = (code >> 6) & 63, j = code & 63;
+          float v[9];
+          merged_pair<BZERO>(fr + 3 * k, ri + 3 * (k * nmax + i), rj + JW * (k * nmax + j), v);
+          if (nid[k * nmax + i] > nid[k * nmax + j]) {
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+              for (int q = 0; q < 3; ++q) acc[3 * r + q] += v[3 * q + r];
+          } else {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) acc[q] += v[q];
+          }
+        }
+        float4* d = acc4 + 3 * static_cast<int64_t>(mg.ent_slot[e0 + e]);
+        atomicAdd(d, make_float4(acc[0], acc[1], acc[2], acc[3]));
+        atomicAdd(d + 1, make_float4(acc[4], acc[5], acc[6], acc[7]));
+        atomicAdd(d + 2, make_float4(acc[8], 0.0f, 0.0f, 0.0f));
+      }
+    }
+    __syncthreads();
+  }
+}
+
 inline unsigned nb(int64_t n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
 
 int sm_count(int device) {
@@ -953,6 +1177,18 @@ void ensure_sell(cgb_assembler* a) {
   CGB_CUDA(cudaGetLastError());
 }
 
+constexpr int kChunks = 4;
+
+// The second stream and the events of the chunked face launch (created once per
+// assembler; the stream is non-blocking and joined back into the context stream).
+void ensure_side_stream(cgb_assembler* a) {
+  if (a->side) return;
+  CGB_CUDA(cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking));
+  CGB_CUDA(cudaEventCreateWithFlags(&a->ev_start, cudaEventDisableTiming));
+  CGB_CUDA(cudaEventCreateWithFlags(&a->ev_done, cudaEventDisableTiming));
+  for (int c = 0; c < kChunks; ++c) CGB_CUDA(cudaEventCreateWithFlags(&a->ev_chunk[c], cudaEventDisableTiming));
+}
+
 }  // namespace
 
 void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags) {
@@ -1001,6 +1237,8 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   // Face kernel.
   FaceArgs fa{};
   fa.n_gp = S->n_gp;
+  fa.g_begin = 0;
+  fa.g_end = S->n_gp;
   fa.nmax = std::max(S->max_n, 1);
   fa.ptr = S->nbr_ptr.p; fa.idx = S->nbr_idx.p; fa.dpsi = S->dpsi.p; fa.ddpsi = S->ddpsi.p;
   fa.weight = a->weight.p; fa.x = d_x;
@@ -1038,10 +1276,24 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   }
   float* st32 = a->state32.p;
   double* st64 = a->state64.p;
-  const unsigned rgrid = std::max(1u, std::min(nb(S->n_gp, 256), static_cast<unsigned>(sms * 16)));
+  // The residual kernel of chunk c + 1 (FP64 pipe) runs beside the tangent kernel of
+  // chunk c (FP32 pipe, L2 atomics) on a second stream; chunks are multiples of 32 points.
+  ensure_side_stream(a);
+  const int n_chunks = S->n_gp >= 65536 ? kChunks : 1;
+  const int chunk = ((S->n_gp + n_chunks - 1) / n_chunks + 31) / 32 * 32;
   prof_begin(ctx, CGB_PHASE_FACE);
   int nface = 0;
-  if (S->n_gp) {
+  const size_t tsm = static_cast<size_t>(kTanWarps) * ((kState * 32 + kRec * fa.nmax) * tk + fa.nmax * sizeof(int));
+  if (want_K) {
+    CGB_CUDA(cudaEventRecord(a->ev_start, st));
+    CGB_CUDA(cudaStreamWaitEvent(a->side, a->ev_start, 0));
+  }
+  for (int c = 0; c < n_chunks && S->n_gp > 0; ++c) {
+    fa.g_begin = c * chunk;
+    fa.g_end = std::min(S->n_gp, (c + 1) * chunk);
+    if (fa.g_begin >= fa.g_end) break;
+    const int ncg = fa.g_end - fa.g_begin;
+    const unsigned rgrid = std::max(1u, std::min(nb(ncg, 256), static_cast<unsigned>(sms * 16)));
     if (mixed) {
       if (det) { if (want_K) face_residual_kernel<float, true, true><<<rgrid, 256, 0, st>>>(fa, st32);
                  else face_residual_kernel<float, true, false><<<rgrid, 256, 0, st>>>(fa, st32); }
@@ -1055,23 +1307,41 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     }
     ++nface;
     CGB_CUDA(cudaGetLastError());
-    if (want_K) {
-      const size_t tsm = static_cast<size_t>(kTanWarps) * ((kState * 32 + kRec * fa.nmax) * tk + fa.nmax * sizeof(int));
-      const unsigned tgrid = std::max(1u, std::min(nb(S->n_gp, 32 * kTanWarps), static_cast<unsigned>(sms * 16)));
-      auto tl = [&](auto kern, auto* stp) {
-        if (tsm > 48 * 1024) CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tsm)));
-        kern<<<tgrid, 32 * kTanWarps, tsm, st>>>(fa, stp);
-      };
-      if (mixed) {
-        if (det) { if (bzero) tl(face_tangent_kernel<float, true, true>, st32); else tl(face_tangent_kernel<float, true, false>, st32); }
-        else { if (bzero) tl(face_tangent_kernel<float, false, true>, st32); else tl(face_tangent_kernel<float, false, false>, st32); }
-      } else {
-        if (det) { if (bzero) tl(face_tangent_kernel<double, true, true>, st64); else tl(face_tangent_kernel<double, true, false>, st64); }
-        else { if (bzero) tl(face_tangent_kernel<double, false, true>, st64); else tl(face_tangent_kernel<double, false, false>, st64); }
-      }
-      ++nface;
-      CGB_CUDA(cudaGetLastError());
+    if (!want_K) continue;
+    CGB_CUDA(cudaEventRecord(a->ev_chunk[c], st));
+    CGB_CUDA(cudaStreamWaitEvent(a->side, a->ev_chunk[c], 0));
+    const unsigned tgrid = std::max(1u, std::min(nb(ncg, 32 * kTanWarps), static_cast<unsigned>(sms * 16)));
+    auto tl = [&](auto kern, auto* stp) {
+      if (tsm > 48 * 1024) CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tsm)));
+      kern<<<tgrid, 32 * kTanWarps, tsm, a->side>>>(fa, stp);
+    };
+    if (mixed && !det) {
+      merge_prepare(a);
+      MergeArgs mg{a->mrg_ent_ptr.p, a->mrg_ent_slot.p, a->mrg_ent_cstart.p, a->mrg_direct.p, a->mrg_code.p};
+      const int JW = bzero ? 4 : 6;
+      const size_t msm = (static_cast<size_t>(kState) * kMG + 4 * 3 * kMG +
+                          4 * static_cast<size_t>(3 + JW) * kMG * fa.nmax) * sizeof(float) +
+                         static_cast<size_t>(kMG) * fa.nmax * sizeof(int);
+      if (msm > 220 * 1024) throw Error(CGB_ERR_CAPACITY, "assemble: neighbour lists too long for the merged tangent");
+      auto kern = bzero ? face_tangent_merged_kernel<true> : face_tangent_merged_kernel<false>;
+      CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(msm)));
+      int per_sm = 0;
+      CGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMrgThreads, msm));
+      const int groups = (fa.g_end + kMG - 1) / kMG - fa.g_begin / kMG;
+      const unsigned mgrid = static_cast<unsigned>(std::max(1, std::min(groups, std::max(per_sm, 1) * sms)));
+      kern<<<mgrid, kMrgThreads, msm, a->side>>>(fa, st32, mg);
+    } else if (mixed) {
+      if (bzero) tl(face_tangent_kernel<float, true, true>, st32); else tl(face_tangent_kernel<float, true, false>, st32);
+    } else {
+      if (det) { if (bzero) tl(face_tangent_kernel<double, true, true>, st64); else tl(face_tangent_kernel<double, true, false>, st64); }
+      else { if (bzero) tl(face_tangent_kernel<double, false, true>, st64); else tl(face_tangent_kernel<double, false, false>, st64); }
     }
+    ++nface;
+    CGB_CUDA(cudaGetLastError());
+  }
+  if (want_K) {
+    CGB_CUDA(cudaEventRecord(a->ev_done, a->side));
+    CGB_CUDA(cudaStreamWaitEvent(st, a->ev_done, 0));
   }
   prof_end(ctx, CGB_PHASE_FACE, nface);
 
@@ -1127,6 +1397,8 @@ void face_mixed_on_arrays(const cgb_face_problem& pr, const double* d_x, double*
                           float* kacc, cudaStream_t st) {
   FaceArgs fa{};
   fa.n_gp = pr.n_gp;
+  fa.g_begin = 0;
+  fa.g_end = pr.n_gp;
   fa.nmax = std::max(pr.max_neighbours, 1);
   fa.ptr = pr.nbr_ptr; fa.idx = pr.nbr_idx; fa.dpsi = pr.dpsi; fa.ddpsi = pr.ddpsi;
   fa.dpsi_t = pr.dpsi; fa.ddpsi_t = pr.ddpsi;

@@ -376,6 +376,12 @@ int cgb_assembler_destroy(cgb_assembler* a) {
     cudaStreamSynchronize(ctx->stream);
   }
   if (a->h_stage) cudaFreeHost(a->h_stage);
+  if (a->side) {
+    cudaStreamSynchronize(a->side);
+    cudaStreamDestroy(a->side);
+  }
+  for (cudaEvent_t e : {a->ev_start, a->ev_done}) if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : a->ev_chunk) if (e) cudaEventDestroy(e);
   delete a;
   if (ctx) cgb::ctx_release(ctx);
   return CGB_OK;

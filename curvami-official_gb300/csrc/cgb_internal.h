@@ -154,6 +154,17 @@ struct cgb_assembler {
   cgb::DevBuf<double> K;            // 9 n_blocks (device scratch for host-buffer calls)
   cgb::DevBuf<double> x;            // 3 n_nodes
   cgb::DevBuf<float> dpsi32, ddpsi32; // FP32 copies of the face shape derivatives (mixed mode)
+  // Merged contributions of the FP32 tangent: per group of 16 consecutive Gauss points the
+  // distinct blocks ("entries", count-descending) and every pair's code in entry order.
+  bool mrg_ready = false;
+  cgb::DevBuf<int64_t> mrg_ent_ptr;   // n_groups + 1
+  cgb::DevBuf<int32_t> mrg_ent_slot;  // block slot of each entry
+  cgb::DevBuf<int32_t> mrg_ent_cstart;// (count << 16) | first contribution within its group
+  cgb::DevBuf<int8_t> mrg_direct;     // 1: group too large, scatter directly
+  cgb::DevBuf<uint16_t> mrg_code;     // per pair: point | i | j, grouped by entry
+  // Second stream of the chunked face launch (tangent of chunk c beside residual of c+1).
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_done = nullptr, ev_chunk[8] = {nullptr};
   cgb::DevBuf<float> state32;         // per-point state between the residual and tangent kernels
   cgb::DevBuf<double> state64;
   cgb::DevBuf<int64_t> sell_ptr;      // sliced-ELL copy for the FP64 phase (groups of 32 points)
@@ -190,6 +201,7 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
 // pattern.cu
 void pattern_build(cgb_assembler* a);
 void deterministic_prepare(cgb_assembler* a);
+void merge_prepare(cgb_assembler* a);
 // assemble.cu
 void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags);
 void energies_device(cgb_assembler* a, const double* d_x, double* out3);

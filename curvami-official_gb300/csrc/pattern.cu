@@ -176,6 +176,122 @@ __global__ void sort_lists(int64_t n, const int64_t* __restrict__ lptr, int64_t*
   }
 }
 
+// ---- merged contributions for the FP32 tangent ---------------------------------------
+// A group is kMergeGroup consecutive face Gauss points (one quadrature cell with a 4x4 rule).
+// Its pairs are sorted by (block slot, point, i, j); each distinct slot is an entry whose
+// contributions are summed in registers before one scatter. Entries are ordered by
+// contribution count, descending (stable), so the threads of a warp get similar loops.
+// Contribution code: point k (4 bits) | local i (6 bits) | local j (6 bits).
+constexpr int kMergeGroup = 16;
+constexpr int kMergeItems = 16384;  // sortable pairs per group (8-byte keys, 128 KB)
+
+__global__ void __launch_bounds__(256) merge_groups_kernel(int n_gp, const int64_t* __restrict__ ptr,
+                                                          const int64_t* __restrict__ map_ptr,
+                                                          const int32_t* __restrict__ map_slot, int phase,
+                                                          int32_t* __restrict__ ent_count,
+                                                          const int64_t* __restrict__ ent_ptr,
+                                                          int32_t* __restrict__ ent_slot,
+                                                          int32_t* __restrict__ ent_cstart,
+                                                          uint16_t* __restrict__ con_code) {
+  extern __shared__ unsigned long long mkeys[];
+  __shared__ int hist[kMergeGroup + 2];
+  __shared__ int n_ent;
+  const int G = blockIdx.x;
+  const int g0 = G * kMergeGroup, g1 = min(n_gp, g0 + kMergeGroup);
+  const int64_t q0 = map_ptr[g0], q1 = map_ptr[g1];
+  const int items = static_cast<int>(q1 - q0);
+  bool ok = items <= kMergeItems;
+  for (int k = 0; k < g1 - g0; ++k) ok = ok && (ptr[g0 + k + 1] - ptr[g0 + k] <= 64);
+  if (!ok) {  // the group scatters directly (count -1)
+    if (phase == 0 && threadIdx.x == 0) ent_count[G] = -1;
+    return;
+  }
+  // Keys: slot (high 32 bits) | k i j (low 16 bits); pairs walked point by point.
+  for (int k = 0; k < g1 - g0; ++k) {
+    const int n = static_cast<int>(ptr[g0 + k + 1] - ptr[g0 + k]);
+    const int64_t m0 = map_ptr[g0 + k] - q0;
+    const int np = n * (n + 1) / 2;
+    for (int p = threadIdx.x; p < np; p += blockDim.x) {
+      int i = 0, off = p;
+      while (off >= n - i) { off -= n - i; ++i; }
+      const int j = i + off;
+      const unsigned code = (static_cast<unsigned>(k) << 12) | (static_cast<unsigned>(i) << 6) | static_cast<unsigned>(j);
+      mkeys[m0 + p] = (static_cast<unsigned long long>(static_cast<unsigned>(map_slot[q0 + m0 + p])) << 16) | code;
+    }
+  }
+  int n2 = 1;
+  while (n2 < items) n2 <<= 1;
+  for (int t = items + threadIdx.x; t < n2; t += blockDim.x) mkeys[t] = ~0ULL;
+  __syncthreads();
+  for (int k = 2; k <= n2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+        const int u = t ^ j;
+        if (u > t) {
+          const bool up = (t & k) == 0;
+          const unsigned long long a = mkeys[t], b = mkeys[u];
+          if ((a > b) == up) { mkeys[t] = b; mkeys[u] = a; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // Entry heads: position t starts an entry when its slot differs from t - 1.
+  if (threadIdx.x == 0) n_ent = 0;
+  __syncthreads();
+  for (int t = threadIdx.x; t < items; t += blockDim.x)
+    if (t == 0 || (mkeys[t] >> 16) != (mkeys[t - 1] >> 16)) atomicAdd(&n_ent, 1);
+  __syncthreads();
+  const int m = n_ent;
+  if (phase == 0) {
+    if (threadIdx.x == 0) ent_count[G] = m;
+    return;
+  }
+  if (ent_ptr[G + 1] - ent_ptr[G] != m) return;
+  // Per entry: start (rank among heads, by a serial scan over the sorted keys is avoided:
+  // each head counts the heads before it with a parallel prefix over positions).
+  // Reuse the key array's tail (beyond n2) is not possible in general, so write the codes
+  // in sorted order first, then the entry table.
+  const int64_t c0 = q0;  // contribution base of this group
+  for (int t = threadIdx.x; t < items; t += blockDim.x) con_code[c0 + t] = static_cast<uint16_t>(mkeys[t] & 0xffff);
+  // Entry start positions and counts, then a stable counting sort of the entries by count.
+  // Thread 0 walks the sorted keys (items <= 16384): the entry table is small.
+  if (threadIdx.x == 0) {
+    for (int c = 0; c < kMergeGroup + 2; ++c) hist[c] = 0;
+    int e = 0, start = 0;
+    for (int t = 1; t <= items; ++t) {
+      if (t == items || (mkeys[t] >> 16) != (mkeys[t - 1] >> 16)) {
+        const int cnt = t - start;
+        hist[cnt > kMergeGroup ? kMergeGroup : cnt]++;  // counts <= points per group
+        // temporarily store (start, slot) at the entry's unsorted index
+        ent_cstart[ent_ptr[G] + e] = start;
+        ent_slot[ent_ptr[G] + e] = static_cast<int32_t>(mkeys[start] >> 16);
+        ++e;
+        start = t;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // Descending count order: offsets for count = 16, 15, ..., 1.
+    int acc = 0;
+    int off[kMergeGroup + 1];
+    for (int c = kMergeGroup; c >= 1; --c) { off[c] = acc; acc += hist[c]; }
+    // Stable placement needs the unsorted table; copy it through the key array (no longer used).
+    int* tmp = reinterpret_cast<int*>(mkeys);
+    for (int e = 0; e < m; ++e) { tmp[2 * e] = ent_cstart[ent_ptr[G] + e]; tmp[2 * e + 1] = ent_slot[ent_ptr[G] + e]; }
+    for (int e = 0; e < m; ++e) {
+      const int start = tmp[2 * e];
+      const int end = (e + 1 < m) ? tmp[2 * e + 2] : items;
+      int cnt = end - start;
+      if (cnt > kMergeGroup) cnt = kMergeGroup;
+      const int at = off[cnt]++;
+      ent_cstart[ent_ptr[G] + at] = (cnt << 16) | start;  // count in the high half
+      ent_slot[ent_ptr[G] + at] = tmp[2 * e + 1];
+    }
+  }
+}
+
 inline unsigned nb(int64_t n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
 
 int read_err(cgb_context* ctx) {
@@ -343,6 +459,43 @@ void pattern_build(cgb_assembler* a) {
     }
   }
   CGB_CUDA(cudaStreamSynchronize(st));
+}
+
+void merge_prepare(cgb_assembler* a) {
+  if (a->mrg_ready) return;
+  cudaStream_t st = a->ctx->stream;
+  const cgb_shape* S = a->faces;
+  const int n_gp = S->n_gp;
+  const int ng = (n_gp + kMergeGroup - 1) / kMergeGroup;
+  const size_t smem = kMergeItems * sizeof(unsigned long long);
+  CGB_CUDA(cudaFuncSetAttribute(merge_groups_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(smem)));
+  DevBuf<int32_t> counts(ng);
+  if (ng > 0)
+    merge_groups_kernel<<<ng, 256, smem, st>>>(n_gp, S->nbr_ptr.p, a->map_ptr.p, a->map_slot.p, 0, counts.p,
+                                               nullptr, nullptr, nullptr, nullptr);
+  CGB_CUDA(cudaGetLastError());
+  std::vector<int32_t> hc(std::max(ng, 1));
+  if (ng > 0) CGB_CUDA(cudaMemcpyAsync(hc.data(), counts.p, ng * 4, cudaMemcpyDeviceToHost, st));
+  CGB_CUDA(cudaStreamSynchronize(st));
+  std::vector<int64_t> ep(ng + 1, 0);
+  std::vector<int8_t> direct(std::max(ng, 1), 0);
+  for (int G = 0; G < ng; ++G) {
+    if (hc[G] < 0) { direct[G] = 1; ep[G + 1] = ep[G]; }
+    else ep[G + 1] = ep[G] + hc[G];
+  }
+  upload(a->mrg_ent_ptr, ep.data(), ep.size(), st);
+  upload(a->mrg_direct, direct.data(), direct.size(), st);
+  a->mrg_ent_slot.alloc(ep[ng]);
+  a->mrg_ent_cstart.alloc(ep[ng]);
+  a->mrg_code.alloc(a->n_pairs);
+  if (ng > 0)
+    merge_groups_kernel<<<ng, 256, smem, st>>>(n_gp, S->nbr_ptr.p, a->map_ptr.p, a->map_slot.p, 1, nullptr,
+                                               a->mrg_ent_ptr.p, a->mrg_ent_slot.p, a->mrg_ent_cstart.p,
+                                               a->mrg_code.p);
+  CGB_CUDA(cudaGetLastError());
+  CGB_CUDA(cudaStreamSynchronize(st));
+  a->mrg_ready = true;
 }
 
 // Ordered lists for the deterministic scatter. Contribution ids: face pairs
