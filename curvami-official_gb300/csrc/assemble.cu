@@ -44,7 +44,24 @@ constexpr int kRecI = 9;   // dx dy beta0 beta1 beta2 Tu g0 g1 g2
 constexpr int kRecJ = 23;  // P(9) Q(9) cW0 cW1 nW0 nW1 TuW
 constexpr int kRec = kRecI + kRecJ;
 
-struct Material { double A[9], B[9], D[9]; };
+struct Material {
+  double A[9], B[9], D[9];
+  // FP32 copies for the FP32 tangent: a double -> float conversion issues on the FP64 pipe,
+  // which the records loop would otherwise pay for 9-27 times per record.
+  float Af[9], Bf[9], Df[9];
+  template <class T> __device__ __forceinline__ T Ai(int i) const { if constexpr (sizeof(T) == 4) return Af[i]; else return A[i]; }
+  template <class T> __device__ __forceinline__ T Bi(int i) const { if constexpr (sizeof(T) == 4) return Bf[i]; else return B[i]; }
+  template <class T> __device__ __forceinline__ T Di(int i) const { if constexpr (sizeof(T) == 4) return Df[i]; else return D[i]; }
+};
+
+inline Material make_material(const double* A, const double* B, const double* D) {
+  Material m;
+  for (int i = 0; i < 9; ++i) {
+    m.A[i] = A[i]; m.B[i] = B[i]; m.D[i] = D[i];
+    m.Af[i] = static_cast<float>(A[i]); m.Bf[i] = static_cast<float>(B[i]); m.Df[i] = static_cast<float>(D[i]);
+  }
+  return m;
+}
 
 struct FaceArgs {
   int n_gp;
@@ -334,8 +351,8 @@ __device__ __forceinline__ void phase2_group(const FaceArgs& a, int g0, int lane
         // J side: pa(3) pb(3) qc(3) cW(2) nW(2) TuW, all times W.
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-          const TK Ar0 = static_cast<TK>(m.A[3 * r]), Ar1 = static_cast<TK>(m.A[3 * r + 1]), Ar2 = static_cast<TK>(m.A[3 * r + 2]);
-          const TK Dr0 = static_cast<TK>(m.D[3 * r]), Dr1 = static_cast<TK>(m.D[3 * r + 1]), Dr2 = static_cast<TK>(m.D[3 * r + 2]);
+          const TK Ar0 = m.Ai<TK>(3 * r), Ar1 = m.Ai<TK>(3 * r + 1), Ar2 = m.Ai<TK>(3 * r + 2);
+          const TK Dr0 = m.Di<TK>(3 * r), Dr1 = m.Di<TK>(3 * r + 1), Dr2 = m.Di<TK>(3 * r + 2);
           R[(kRecI + r) * nmax] = (Ar0 * dx + Ar2 * dy) * Wt;
           R[(kRecI + 3 + r) * nmax] = (Ar1 * dy + Ar2 * dx) * Wt;
           R[(kRecI + 6 + r) * nmax] = (Dr0 * b0 + Dr1 * b1 + Dr2 * b2) * Wt;
@@ -350,9 +367,9 @@ __device__ __forceinline__ void phase2_group(const FaceArgs& a, int g0, int lane
       //   P(r,c) = a1_c pa_r + a2_c pb_r + b_c pc_r.
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
-        const TK Ar0 = static_cast<TK>(m.A[3 * r]), Ar1 = static_cast<TK>(m.A[3 * r + 1]), Ar2 = static_cast<TK>(m.A[3 * r + 2]);
-        const TK Br0 = static_cast<TK>(m.B[3 * r]), Br1 = static_cast<TK>(m.B[3 * r + 1]), Br2 = static_cast<TK>(m.B[3 * r + 2]);
-        const TK Dr0 = static_cast<TK>(m.D[3 * r]), Dr1 = static_cast<TK>(m.D[3 * r + 1]), Dr2 = static_cast<TK>(m.D[3 * r + 2]);
+        const TK Ar0 = m.Ai<TK>(3 * r), Ar1 = m.Ai<TK>(3 * r + 1), Ar2 = m.Ai<TK>(3 * r + 2);
+        const TK Br0 = m.Bi<TK>(3 * r), Br1 = m.Bi<TK>(3 * r + 1), Br2 = m.Bi<TK>(3 * r + 2);
+        const TK Dr0 = m.Di<TK>(3 * r), Dr1 = m.Di<TK>(3 * r + 1), Dr2 = m.Di<TK>(3 * r + 2);
         const TK pa = (Ar0 * dx + Ar2 * dy) * Wt;
         const TK pb = (Ar1 * dy + Ar2 * dx) * Wt;
         const TK pc = (Br0 * b0 + Br1 * b1 + Br2 * b2) * Wt;
@@ -927,7 +944,9 @@ __device__ __forceinline__ void merged_pair(const float4* fr, const float4* ri, 
     for (int c = 0; c < 3; ++c) v[3 * r + c] = a1t[r] * Y1[c] + a2t[r] * Y2[c] + bt[r] * Y3[c] + (r == c ? geo : 0.0f);
 }
 
-template <bool BZERO>
+// DET: every entry's sum is stored (9 floats at unit e0 + e of a.Kc) for the ordered
+// per-block reduction instead of being added atomically; it needs no direct group.
+template <bool BZERO, bool DET>
 __global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(FaceArgs a, const float* __restrict__ gstate,
                                                                             MergeArgs mg) {
   constexpr int JW = BZERO ? 4 : 6;  // float4 rows of a J-side record
@@ -996,10 +1015,10 @@ __global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(Fac
         float pa[3], pb[3], qc[3];
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-          pa[r] = (static_cast<float>(m.A[3 * r]) * dx + static_cast<float>(m.A[3 * r + 2]) * dy) * Wt;
-          pb[r] = (static_cast<float>(m.A[3 * r + 1]) * dy + static_cast<float>(m.A[3 * r + 2]) * dx) * Wt;
-          qc[r] = (static_cast<float>(m.D[3 * r]) * b0 + static_cast<float>(m.D[3 * r + 1]) * b1 +
-                   static_cast<float>(m.D[3 * r + 2]) * b2) * Wt;
+          pa[r] = (m.Ai<float>(3 * r) * dx + m.Ai<float>(3 * r + 2) * dy) * Wt;
+          pb[r] = (m.Ai<float>(3 * r + 1) * dy + m.Ai<float>(3 * r + 2) * dx) * Wt;
+          qc[r] = (m.Di<float>(3 * r) * b0 + m.Di<float>(3 * r + 1) * b1 +
+                   m.Di<float>(3 * r + 2) * b2) * Wt;
         }
         RJ[0] = make_float4(pa[0], pa[1], pa[2], pb[0]);
         RJ[1] = make_float4(pb[1], pb[2], qc[0], qc[1]);
@@ -1009,9 +1028,9 @@ __global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(Fac
         float J[24];
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-          const float Ar0 = static_cast<float>(m.A[3 * r]), Ar1 = static_cast<float>(m.A[3 * r + 1]), Ar2 = static_cast<float>(m.A[3 * r + 2]);
-          const float Br0 = static_cast<float>(m.B[3 * r]), Br1 = static_cast<float>(m.B[3 * r + 1]), Br2 = static_cast<float>(m.B[3 * r + 2]);
-          const float Dr0 = static_cast<float>(m.D[3 * r]), Dr1 = static_cast<float>(m.D[3 * r + 1]), Dr2 = static_cast<float>(m.D[3 * r + 2]);
+          const float Ar0 = m.Ai<float>(3 * r), Ar1 = m.Ai<float>(3 * r + 1), Ar2 = m.Ai<float>(3 * r + 2);
+          const float Br0 = m.Bi<float>(3 * r), Br1 = m.Bi<float>(3 * r + 1), Br2 = m.Bi<float>(3 * r + 2);
+          const float Dr0 = m.Di<float>(3 * r), Dr1 = m.Di<float>(3 * r + 1), Dr2 = m.Di<float>(3 * r + 2);
           const float pa = (Ar0 * dx + Ar2 * dy) * Wt, pb = (Ar1 * dy + Ar2 * dx) * Wt, pc = (Br0 * b0 + Br1 * b1 + Br2 * b2) * Wt;
           const float qa = (Br0 * dx + Br2 * dy) * Wt, qb = (Br1 * dy + Br2 * dx) * Wt, qc = (Dr0 * b0 + Dr1 * b1 + Dr2 * b2) * Wt;
 #pragma unroll
@@ -1031,7 +1050,7 @@ __global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(Fac
     __syncthreads();
     float4* acc4 = static_cast<float4*>(a.Kacc);
     const int64_t cbase = a.map_ptr[g0];
-    if (mg.direct[G]) {
+    if (!DET && mg.direct[G]) {
       // Too many pairs for the setup's shared-memory sort: scatter pair by pair.
       for (int k = 0; k < kn; ++k) {
         const int n = static_cast<int>(a.ptr[g0 + k + 1] - a.ptr[g0 + k]);
@@ -1070,10 +1089,16 @@ __global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(Fac
             for (int q = 0; q < 9; ++q) acc[q] += v[q];
           }
         }
-        float4* d = acc4 + 3 * static_cast<int64_t>(mg.ent_slot[e0 + e]);
-        atomicAdd(d, make_float4(acc[0], acc[1], acc[2], acc[3]));
-        atomicAdd(d + 1, make_float4(acc[4], acc[5], acc[6], acc[7]));
-        atomicAdd(d + 2, make_float4(acc[8], 0.0f, 0.0f, 0.0f));
+        if constexpr (DET) {
+          float* d = static_cast<float*>(a.Kc) + 9 * (e0 + e);
+#pragma unroll
+          for (int q = 0; q < 9; ++q) d[q] = acc[q];
+        } else {
+          float4* d = acc4 + 3 * static_cast<int64_t>(mg.ent_slot[e0 + e]);
+          atomicAdd(d, make_float4(acc[0], acc[1], acc[2], acc[3]));
+          atomicAdd(d + 1, make_float4(acc[4], acc[5], acc[6], acc[7]));
+          atomicAdd(d + 2, make_float4(acc[8], 0.0f, 0.0f, 0.0f));
+        }
       }
     }
     __syncthreads();
@@ -1202,6 +1227,18 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   if (!a->have_material) throw Error(CGB_ERR_INVALID, "assemble: material not set (cgb_set_material)");
   if (want_K && !d_K) throw Error(CGB_ERR_INVALID, "assemble: K output missing with CGB_TANGENT");
   if (det) deterministic_prepare(a);
+  // The FP32 tangent merges each group's contributions per block; in deterministic mode the
+  // merged sums become the K units, unless a group is too large to merge.
+  bool merged = false;
+  if (mixed && want_K) {
+    merge_prepare(a);
+    merged = !det || a->mrg_n_direct == 0;
+  }
+  if (det && want_K) {
+    if (merged) deterministic_entry_lists(a);
+    else deterministic_pair_lists(a);
+  }
+  const int64_t k_face_units = merged ? a->mrg_n_ent : a->n_pairs;
 
   const int64_t ndof = 3 * static_cast<int64_t>(a->n_nodes);
   // Accumulators.
@@ -1216,7 +1253,7 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
       CGB_CUDA(cudaMemsetAsync(a->kacc64.p, 0, 9 * a->n_blocks * sizeof(double), st));
     }
   }
-  const int64_t n_contrib = a->n_pairs + [&] { int64_t s = 0; for (auto& f : a->folds) s += f.n_pairs; return s; }();
+  const int64_t n_contrib = k_face_units + [&] { int64_t s = 0; for (auto& f : a->folds) s += f.n_pairs; return s; }();
   if (det) {
     a->fcontrib.ensure(3 * std::max<int64_t>(a->n_fcontrib, 1));
     if (want_K) {
@@ -1226,9 +1263,9 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     // Hinge entries of inactive crease points contribute zero.
     if (a->n_fcontrib > S->nnz)
       CGB_CUDA(cudaMemsetAsync(a->fcontrib.p + 3 * S->nnz, 0, 3 * (a->n_fcontrib - S->nnz) * sizeof(double), st));
-    if (want_K && n_contrib > a->n_pairs) {
-      if (mixed) CGB_CUDA(cudaMemsetAsync(a->contrib32.p + 9 * a->n_pairs, 0, 9 * (n_contrib - a->n_pairs) * sizeof(float), st));
-      else CGB_CUDA(cudaMemsetAsync(a->contrib64.p + 9 * a->n_pairs, 0, 9 * (n_contrib - a->n_pairs) * sizeof(double), st));
+    if (want_K && n_contrib > k_face_units) {
+      if (mixed) CGB_CUDA(cudaMemsetAsync(a->contrib32.p + 9 * k_face_units, 0, 9 * (n_contrib - k_face_units) * sizeof(float), st));
+      else CGB_CUDA(cudaMemsetAsync(a->contrib64.p + 9 * k_face_units, 0, 9 * (n_contrib - k_face_units) * sizeof(double), st));
     }
   }
 
@@ -1245,7 +1282,7 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   fa.map_ptr = a->map_ptr.p; fa.map_slot = a->map_slot.p;
   ensure_sell(a);
   fa.sell_ptr = a->sell_ptr.p; fa.sidx = a->sidx.p; fa.sdpsi = a->sdpsi.p; fa.sddpsi = a->sddpsi.p;
-  std::memcpy(fa.mat.A, a->A, sizeof a->A); std::memcpy(fa.mat.B, a->B, sizeof a->B); std::memcpy(fa.mat.D, a->D, sizeof a->D);
+  fa.mat = make_material(a->A, a->B, a->D);
   fa.F = d_F;
   fa.Fc = a->fcontrib.p;
   fa.Kacc = mixed ? static_cast<void*>(a->kacc32.p) : static_cast<void*>(a->kacc64.p);
@@ -1281,7 +1318,6 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   ensure_side_stream(a);
   const int n_chunks = S->n_gp >= 65536 ? kChunks : 1;
   const int chunk = ((S->n_gp + n_chunks - 1) / n_chunks + 31) / 32 * 32;
-  prof_begin(ctx, CGB_PHASE_FACE);
   int nface = 0;
   const size_t tsm = static_cast<size_t>(kTanWarps) * ((kState * 32 + kRec * fa.nmax) * tk + fa.nmax * sizeof(int));
   if (want_K) {
@@ -1294,6 +1330,7 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     if (fa.g_begin >= fa.g_end) break;
     const int ncg = fa.g_end - fa.g_begin;
     const unsigned rgrid = std::max(1u, std::min(nb(ncg, 256), static_cast<unsigned>(sms * 16)));
+    prof_begin(ctx, CGB_PHASE_FACE);
     if (mixed) {
       if (det) { if (want_K) face_residual_kernel<float, true, true><<<rgrid, 256, 0, st>>>(fa, st32);
                  else face_residual_kernel<float, true, false><<<rgrid, 256, 0, st>>>(fa, st32); }
@@ -1306,24 +1343,26 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
              else face_residual_kernel<double, false, false><<<rgrid, 256, 0, st>>>(fa, st64); }
     }
     ++nface;
+    prof_end(ctx, CGB_PHASE_FACE, 1);
     CGB_CUDA(cudaGetLastError());
     if (!want_K) continue;
     CGB_CUDA(cudaEventRecord(a->ev_chunk[c], st));
     CGB_CUDA(cudaStreamWaitEvent(a->side, a->ev_chunk[c], 0));
+    prof_begin(ctx, CGB_PHASE_TANGENT, a->side);
     const unsigned tgrid = std::max(1u, std::min(nb(ncg, 32 * kTanWarps), static_cast<unsigned>(sms * 16)));
     auto tl = [&](auto kern, auto* stp) {
       if (tsm > 48 * 1024) CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tsm)));
       kern<<<tgrid, 32 * kTanWarps, tsm, a->side>>>(fa, stp);
     };
-    if (mixed && !det) {
-      merge_prepare(a);
+    if (merged) {
       MergeArgs mg{a->mrg_ent_ptr.p, a->mrg_ent_slot.p, a->mrg_ent_cstart.p, a->mrg_direct.p, a->mrg_code.p};
       const int JW = bzero ? 4 : 6;
       const size_t msm = (static_cast<size_t>(kState) * kMG + 4 * 3 * kMG +
                           4 * static_cast<size_t>(3 + JW) * kMG * fa.nmax) * sizeof(float) +
                          static_cast<size_t>(kMG) * fa.nmax * sizeof(int);
       if (msm > 220 * 1024) throw Error(CGB_ERR_CAPACITY, "assemble: neighbour lists too long for the merged tangent");
-      auto kern = bzero ? face_tangent_merged_kernel<true> : face_tangent_merged_kernel<false>;
+      auto kern = det ? (bzero ? face_tangent_merged_kernel<true, true> : face_tangent_merged_kernel<false, true>)
+                      : (bzero ? face_tangent_merged_kernel<true, false> : face_tangent_merged_kernel<false, false>);
       CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(msm)));
       int per_sm = 0;
       CGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMrgThreads, msm));
@@ -1337,19 +1376,20 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
       else { if (bzero) tl(face_tangent_kernel<double, false, true>, st64); else tl(face_tangent_kernel<double, false, false>, st64); }
     }
     ++nface;
+    prof_end(ctx, CGB_PHASE_TANGENT, 1, a->side);
     CGB_CUDA(cudaGetLastError());
   }
   if (want_K) {
     CGB_CUDA(cudaEventRecord(a->ev_done, a->side));
     CGB_CUDA(cudaStreamWaitEvent(st, a->ev_done, 0));
   }
-  prof_end(ctx, CGB_PHASE_FACE, nface);
+  (void)nface;
 
   // Hinge.
   if (hinge) {
     prof_begin(ctx, CGB_PHASE_HINGE);
     int nl = 0;
-    int64_t kb = a->hinge_pair_base, fb = a->hinge_f_base;
+    int64_t kb = k_face_units, fb = a->hinge_f_base;
     for (auto& f : a->folds) {
       if (f.n_gp == 0) continue;
       HingeArgs h = hinge_args(a, f, d_x, flags);
@@ -1379,7 +1419,8 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     nred = want_K ? 2 : 1;
     det_reduce_F<<<nb(a->n_nodes, 128), 128, 0, st>>>(a->n_nodes, a->node_list_ptr.p, a->node_list.p, a->fcontrib.p, d_F);
     if (want_K) {
-      if (mixed) det_reduce_blocks<float><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->blk_list_ptr.p, a->blk_list.p, a->contrib32.p, d_K);
+      if (merged) det_reduce_blocks<float><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->ent_list_ptr.p, a->ent_list.p, a->contrib32.p, d_K);
+      else if (mixed) det_reduce_blocks<float><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->blk_list_ptr.p, a->blk_list.p, a->contrib32.p, d_K);
       else det_reduce_blocks<double><<<cg, 128, 0, st>>>(a->n_nodes, a->col_ptr.p, a->blk_list_ptr.p, a->blk_list.p, a->contrib64.p, d_K);
     }
   } else if (want_K) {
@@ -1404,8 +1445,7 @@ void face_mixed_on_arrays(const cgb_face_problem& pr, const double* d_x, double*
   fa.dpsi_t = pr.dpsi; fa.ddpsi_t = pr.ddpsi;
   fa.weight = pr.weight; fa.x = d_x;
   fa.map_ptr = pr.map_ptr; fa.map_slot = pr.csr_map; fa.outer = pr.outer;
-  std::memcpy(fa.mat.A, pr.A, sizeof fa.mat.A); std::memcpy(fa.mat.B, pr.B, sizeof fa.mat.B);
-  std::memcpy(fa.mat.D, pr.D, sizeof fa.mat.D);
+  fa.mat = make_material(pr.A, pr.B, pr.D);
   fa.F = d_F;
   fa.Kacc = kacc;
   const int64_t n_blocks = static_cast<int64_t>(pr.nnz / 9);
@@ -1432,8 +1472,7 @@ void energies_device(cgb_assembler* a, const double* d_x, double* out3) {
   cudaStream_t st = ctx->stream;
   a->energy.ensure(3);
   CGB_CUDA(cudaMemsetAsync(a->energy.p, 0, 3 * sizeof(double), st));
-  Material m;
-  std::memcpy(m.A, a->A, sizeof m.A); std::memcpy(m.B, a->B, sizeof m.B); std::memcpy(m.D, a->D, sizeof m.D);
+  const Material m = make_material(a->A, a->B, a->D);
   const cgb_shape* S = a->faces;
   if (S->n_gp)
     face_energy_kernel<<<std::max(1u, std::min(nb(S->n_gp, 4), 152u * 32u)), 128, 0, st>>>(

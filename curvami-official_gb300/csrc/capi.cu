@@ -66,19 +66,21 @@ void collect_marks(cgb_context* ctx) {
 }  // namespace
 
 namespace cgb {
-void prof_begin(cgb_context* ctx, int phase) {
+void prof_begin(cgb_context* ctx, int phase, cudaStream_t stream) {
   if (!ctx->profile) return;
-  cgb_context::Mark m{phase, take_event(ctx), nullptr, 0};
-  CGB_CUDA(cudaEventRecord(m.start, ctx->stream));
+  if (!stream) stream = ctx->stream;
+  cgb_context::Mark m{phase, take_event(ctx), nullptr, 0, stream};
+  CGB_CUDA(cudaEventRecord(m.start, stream));
   ctx->marks.push_back(m);
 }
-void prof_end(cgb_context* ctx, int phase, int launches) {
+void prof_end(cgb_context* ctx, int phase, int launches, cudaStream_t stream) {
   if (!ctx->profile) return;
+  if (!stream) stream = ctx->stream;
   for (auto it = ctx->marks.rbegin(); it != ctx->marks.rend(); ++it) {
-    if (it->phase == phase && !it->stop) {
+    if (it->phase == phase && !it->stop && it->stream == stream) {
       it->stop = take_event(ctx);
       it->launches = launches;
-      CGB_CUDA(cudaEventRecord(it->stop, ctx->stream));
+      CGB_CUDA(cudaEventRecord(it->stop, stream));
       break;
     }
   }

@@ -88,7 +88,7 @@ struct cgb_context {
   int* h_err = nullptr;  // pinned mirror
   // Tracing: event pairs per phase, summed when read.
   bool profile = false;
-  struct Mark { int phase; cudaEvent_t start, stop; int launches; };
+  struct Mark { int phase; cudaEvent_t start, stop; int launches; cudaStream_t stream; };
   std::vector<Mark> marks;
   std::vector<cudaEvent_t> event_pool;
   double prof_ms[CGB_N_PHASES] = {0};
@@ -162,6 +162,8 @@ struct cgb_assembler {
   cgb::DevBuf<int32_t> mrg_ent_cstart;// (count << 16) | first contribution within its group
   cgb::DevBuf<int8_t> mrg_direct;     // 1: group too large, scatter directly
   cgb::DevBuf<uint16_t> mrg_code;     // per pair: point | i | j, grouped by entry
+  int64_t mrg_n_ent = 0;              // entries over all groups
+  int mrg_n_direct = 0;               // groups scattered pair by pair
   // Second stream of the chunked face launch (tangent of chunk c beside residual of c+1).
   cudaStream_t side = nullptr;
   cudaEvent_t ev_start = nullptr, ev_done = nullptr, ev_chunk[8] = {nullptr};
@@ -170,17 +172,22 @@ struct cgb_assembler {
   cgb::DevBuf<int64_t> sell_ptr;      // sliced-ELL copy for the FP64 phase (groups of 32 points)
   cgb::DevBuf<int32_t> sidx;
   cgb::DevBuf<double> sdpsi, sddpsi;
-  // Deterministic scatter: per pair contributions and per-block ordered lists.
-  bool det_ready = false;
-  cgb::DevBuf<int64_t> blk_list_ptr;  // n_blocks + 1
-  cgb::DevBuf<int64_t> blk_list;      // global contribution ids, ascending
+  // Deterministic scatter: contributions ("units") and per-block / per-node ordered lists.
+  // K units are either every pair (FP64, or groups the merge cannot take) or, for the FP32
+  // tangent, every merged entry (one fixed-order sum per group and block); hinge pairs follow.
+  bool det_ready = false;             // F lists
+  bool det_pairs_ready = false;       // K lists over pairs
+  bool det_entries_ready = false;     // K lists over merged entries
+  cgb::DevBuf<int64_t> blk_list_ptr;  // n_blocks + 1 (pair units)
+  cgb::DevBuf<int64_t> blk_list;      // pair unit ids, ascending
+  cgb::DevBuf<int64_t> ent_list_ptr;  // n_blocks + 1 (entry units)
+  cgb::DevBuf<int64_t> ent_list;      // entry unit ids, ascending
   cgb::DevBuf<int64_t> node_list_ptr; // n_nodes + 1
   cgb::DevBuf<int64_t> node_list;     // F contribution ids, ascending
   cgb::DevBuf<double> contrib64;      // 9 per contribution
   cgb::DevBuf<float> contrib32;
   cgb::DevBuf<double> fcontrib;       // 3 per F contribution
   int64_t n_fcontrib = 0;
-  int64_t hinge_pair_base = 0;        // first contribution id of hinge pairs
   int64_t hinge_f_base = 0;
   // Energies.
   cgb::DevBuf<double> energy;       // 3
@@ -193,14 +200,18 @@ namespace cgb {
 void ctx_retain(cgb_context* ctx);
 void ctx_release(cgb_context* ctx);
 // Tracing helpers (capi.cu): no-ops unless profiling is enabled on the context.
-void prof_begin(cgb_context* ctx, int phase);
-void prof_end(cgb_context* ctx, int phase, int launches);
+void prof_begin(cgb_context* ctx, int phase, cudaStream_t stream = nullptr);
+void prof_end(cgb_context* ctx, int phase, int launches, cudaStream_t stream = nullptr);
 // shape.cu
 void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shape_params& prm,
                  const std::vector<Crease>& creases, cgb_shape* out);
 // pattern.cu
 void pattern_build(cgb_assembler* a);
 void deterministic_prepare(cgb_assembler* a);
+// Per-block lists of K units: pairs (units [0, n_pairs) then hinge pairs) or merged entries
+// (units [0, mrg_n_ent) then hinge pairs; needs merge_prepare and no direct group).
+void deterministic_pair_lists(cgb_assembler* a);
+void deterministic_entry_lists(cgb_assembler* a);
 void merge_prepare(cgb_assembler* a);
 // assemble.cu
 void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags);

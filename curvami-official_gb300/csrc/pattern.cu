@@ -489,6 +489,9 @@ void merge_prepare(cgb_assembler* a) {
   a->mrg_ent_slot.alloc(ep[ng]);
   a->mrg_ent_cstart.alloc(ep[ng]);
   a->mrg_code.alloc(a->n_pairs);
+  a->mrg_n_ent = ep[ng];
+  a->mrg_n_direct = 0;
+  for (int G = 0; G < ng; ++G) a->mrg_n_direct += direct[G];
   if (ng > 0)
     merge_groups_kernel<<<ng, 256, smem, st>>>(n_gp, S->nbr_ptr.p, a->map_ptr.p, a->map_slot.p, 1, nullptr,
                                                a->mrg_ent_ptr.p, a->mrg_ent_slot.p, a->mrg_ent_cstart.p,
@@ -498,31 +501,23 @@ void merge_prepare(cgb_assembler* a) {
   a->mrg_ready = true;
 }
 
-// Ordered lists for the deterministic scatter. Contribution ids: face pairs
-// [0, n_pairs), then hinge pairs fold by fold. F contribution ids: face entries
-// [0, nnz_face), then hinge merged-node entries fold by fold. Each K block and each
-// node sums its contributions in ascending id order, i.e. Gauss point by Gauss point
-// in the reference's loop order.
-void deterministic_prepare(cgb_assembler* a) {
-  if (a->det_ready) return;
-  cgb_context* ctx = a->ctx;
-  cudaStream_t st = ctx->stream;
-  int64_t n_hp = 0, n_hf = 0;
-  std::vector<int64_t> fnum;  // merged-node entries per fold
-  for (auto& f : a->folds) {
-    n_hp += f.n_pairs;
-    fnum.push_back(f.n_u);
-    n_hf += f.n_u;
-  }
-  const int64_t nq = a->n_pairs + n_hp;
-  a->hinge_pair_base = a->n_pairs;
-  a->hinge_f_base = a->faces->nnz;
-  a->n_fcontrib = a->faces->nnz + n_hf;
+// Ordered lists for the deterministic scatter. F contribution ids: face entries
+// [0, nnz_face), then hinge merged-node entries fold by fold. K unit ids: the face units
+// (pairs, or merged entries), then hinge pairs fold by fold. Each K block and each node sums
+// its units in ascending id order, i.e. Gauss point (or group of Gauss points) by Gauss
+// point in the reference's loop order.
+namespace {
 
-  // K lists.
+// Per-block ascending lists of K units: n_face face units whose block slots are face_slot,
+// then every fold's pairs.
+void block_lists(cgb_assembler* a, int64_t n_face, const int32_t* face_slot, DevBuf<int64_t>& ptr,
+                 DevBuf<int64_t>& list) {
+  cudaStream_t st = a->ctx->stream;
+  int64_t nq = n_face;
+  for (auto& f : a->folds) nq += f.n_pairs;
   DevBuf<int64_t> cnt(a->n_blocks + 1);
   CGB_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes(), st));
-  if (a->n_pairs) count_slots<<<nb(a->n_pairs, 256), 256, 0, st>>>(a->n_pairs, a->map_slot.p, cnt.p);
+  if (n_face) count_slots<<<nb(n_face, 256), 256, 0, st>>>(n_face, face_slot, cnt.p);
   for (auto& f : a->folds)
     if (f.n_pairs) count_slots<<<nb(f.n_pairs, 256), 256, 0, st>>>(f.n_pairs, f.pair_slot.p, cnt.p);
   std::vector<int64_t> hc(a->n_blocks);
@@ -530,18 +525,49 @@ void deterministic_prepare(cgb_assembler* a) {
   CGB_CUDA(cudaStreamSynchronize(st));
   std::vector<int64_t> lp(a->n_blocks + 1, 0);
   for (int64_t b = 0; b < a->n_blocks; ++b) lp[b + 1] = lp[b] + hc[b];
-  upload(a->blk_list_ptr, lp.data(), lp.size(), st);
+  upload(ptr, lp.data(), lp.size(), st);
   DevBuf<int64_t> cur;
   upload(cur, lp.data(), a->n_blocks, st);
-  a->blk_list.alloc(nq);
-  if (a->n_pairs) fill_slots<<<nb(a->n_pairs, 256), 256, 0, st>>>(a->n_pairs, 0, a->map_slot.p, cur.p, a->blk_list.p);
-  int64_t base = a->n_pairs;
+  list.alloc(std::max<int64_t>(nq, 1));
+  if (n_face) fill_slots<<<nb(n_face, 256), 256, 0, st>>>(n_face, 0, face_slot, cur.p, list.p);
+  int64_t base = n_face;
   for (auto& f : a->folds) {
-    if (f.n_pairs) fill_slots<<<nb(f.n_pairs, 256), 256, 0, st>>>(f.n_pairs, base, f.pair_slot.p, cur.p, a->blk_list.p);
+    if (f.n_pairs) fill_slots<<<nb(f.n_pairs, 256), 256, 0, st>>>(f.n_pairs, base, f.pair_slot.p, cur.p, list.p);
     base += f.n_pairs;
   }
-  sort_lists<<<nb(a->n_blocks, 128), 128, 0, st>>>(a->n_blocks, a->blk_list_ptr.p, a->blk_list.p);
+  sort_lists<<<nb(a->n_blocks, 128), 128, 0, st>>>(a->n_blocks, ptr.p, list.p);
   CGB_CUDA(cudaGetLastError());
+  CGB_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace
+
+void deterministic_pair_lists(cgb_assembler* a) {
+  if (a->det_pairs_ready) return;
+  block_lists(a, a->n_pairs, a->map_slot.p, a->blk_list_ptr, a->blk_list);
+  a->det_pairs_ready = true;
+}
+
+void deterministic_entry_lists(cgb_assembler* a) {
+  if (a->det_entries_ready) return;
+  merge_prepare(a);
+  if (a->mrg_n_direct) throw Error(CGB_ERR_INVALID, "deterministic entry lists need every group merged");
+  block_lists(a, a->mrg_n_ent, a->mrg_ent_slot.p, a->ent_list_ptr, a->ent_list);
+  a->det_entries_ready = true;
+}
+
+void deterministic_prepare(cgb_assembler* a) {
+  if (a->det_ready) return;
+  cgb_context* ctx = a->ctx;
+  cudaStream_t st = ctx->stream;
+  int64_t n_hf = 0;
+  std::vector<int64_t> fnum;  // merged-node entries per fold
+  for (auto& f : a->folds) {
+    fnum.push_back(f.n_u);
+    n_hf += f.n_u;
+  }
+  a->hinge_f_base = a->faces->nnz;
+  a->n_fcontrib = a->faces->nnz + n_hf;
 
   // F lists (node of each contribution: face entries then hinge merged nodes).
   DevBuf<int64_t> fc(a->n_nodes + 1);
@@ -560,7 +586,7 @@ void deterministic_prepare(cgb_assembler* a) {
   a->node_list.alloc(a->n_fcontrib);
   if (a->faces->nnz)
     fill_slots<<<nb(a->faces->nnz, 256), 256, 0, st>>>(a->faces->nnz, 0, a->faces->nbr_idx.p, fcur.p, a->node_list.p);
-  base = a->faces->nnz;
+  int64_t base = a->faces->nnz;
   for (size_t k = 0; k < a->folds.size(); ++k) {
     if (fnum[k]) fill_slots<<<nb(fnum[k], 256), 256, 0, st>>>(fnum[k], base, a->folds[k].u_node.p, fcur.p, a->node_list.p);
     base += fnum[k];

@@ -55,7 +55,7 @@ SIGNATURES = {
     "cgb_profile_read": (i32, [vp, vp, vp, i32]),
 }
 
-PHASES = ("h2d", "zero", "face", "hinge", "reduce", "d2h")
+PHASES = ("h2d", "zero", "face", "hinge", "reduce", "d2h", "tangent")
 
 
 class Crease(C.Structure):

@@ -204,11 +204,12 @@ int cgb_assemble_face_noalloc(cgb_context* ctx, const cgb_face_problem* prob, co
 enum {
   CGB_PHASE_H2D = 0,    /* x host -> device (cgb_assemble only) */
   CGB_PHASE_ZERO = 1,   /* clearing of the accumulators */
-  CGB_PHASE_FACE = 2,   /* face Gauss points: residual, tangent, scatter */
-  CGB_PHASE_HINGE = 3,  /* elastic hinge */
-  CGB_PHASE_REDUCE = 4, /* block -> CSC output, or the deterministic reductions */
-  CGB_PHASE_D2H = 5,    /* K, F device -> host (cgb_assemble only) */
-  CGB_N_PHASES = 6
+  CGB_PHASE_FACE = 2,    /* face Gauss points: kinematics, resultants, residual (FP64 kernels) */
+  CGB_PHASE_HINGE = 3,   /* elastic hinge */
+  CGB_PHASE_REDUCE = 4,  /* block -> CSC output, or the deterministic reductions */
+  CGB_PHASE_D2H = 5,     /* K, F device -> host (cgb_assemble only) */
+  CGB_PHASE_TANGENT = 6, /* face tangent and its scatter (second stream, overlaps FACE) */
+  CGB_N_PHASES = 7
 };
 int cgb_profile_enable(cgb_context* ctx, int on);
 /* ms[CGB_N_PHASES] summed device time, launches[CGB_N_PHASES] kernels launched by the

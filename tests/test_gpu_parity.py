@@ -187,9 +187,10 @@ def test_fp64_assembly(which, det, arc_case, row_case):
     assert rel(F, Fo) < 1e-13
 
 
+@pytest.mark.parametrize("which", ["arc", "row"])
 @pytest.mark.parametrize("det", [False, True])
-def test_mixed_assembly(det, arc_case):
-    c = arc_case
+def test_mixed_assembly(which, det, arc_case, row_case):
+    c = arc_case if which == "arc" else row_case
     Ko, Fo = c.oracle(c.x)
     fl = cg.TANGENT | cg.HINGE | cg.MIXED | (cg.DETERMINISTIC if det else 0)
     K, F = c.asm.assemble(c.x, fl)
@@ -225,12 +226,37 @@ def test_exact_hinge_tangent(arc_case):
     assert rel(K, Ko) < 1e-9 and rel(F, Fo) < 1e-13
 
 
-def test_deterministic_bitwise(arc_case):
+def test_deterministic_bitwise(ctx, arc_case):
     c = arc_case
+    # a second assembler over the same inputs builds the same ordered lists (an assembler
+    # takes its node count from the context's nodes when it is created)
+    ctx.set_nodes(c.p.node_xy)
+    other = cg.NonLinearAssembler(ctx, c.faces_o, c.p.faces.weight, c.model.fold_specs)
+    other.set_material(*cg.abd_isotropic(c.p.E, c.p.nu, c.p.thickness))
     for fl in (cg.TANGENT | cg.HINGE | cg.DETERMINISTIC, cg.TANGENT | cg.HINGE | cg.MIXED | cg.DETERMINISTIC):
         K1, F1 = c.asm.assemble(c.x, fl)
         K2, F2 = c.asm.assemble(c.x, fl)
+        K3, F3 = other.assemble(c.x, fl)
         assert np.array_equal(K1, K2) and np.array_equal(F1, F2)
+        assert np.array_equal(K1, K3) and np.array_equal(F1, F3)
+
+
+def test_mixed_wide_supports(o, ctx):
+    """About 60 neighbours per point: a group of 16 points has more pairs than the merge
+    setup sorts, so the FP32 tangent scatters those groups pair by pair and the
+    deterministic mode keeps one unit per pair."""
+    p = synth.square_plate(17, 0.5, 3, jitter=0.05, seed=31, crease="arc", rho_factor=4.5)
+    x = 0.3 * synth.fourier_field(p.node_xy, np.random.default_rng(32), lam=(3.0, 10.0))
+    c = Case(o, ctx, p, x)
+    assert int(np.diff(c.ref["ptr"]).max()) >= 45
+    Ko, Fo = c.oracle(c.x)
+    for det in (0, cg.DETERMINISTIC):
+        K, F = c.asm.assemble(c.x, cg.TANGENT | cg.HINGE | cg.MIXED | det)
+        assert rel(F, Fo) < 1e-12
+        assert rel(K, Ko) < 1e-5
+    K1, F1 = c.asm.assemble(c.x, cg.TANGENT | cg.HINGE | cg.MIXED | cg.DETERMINISTIC)
+    K2, F2 = c.asm.assemble(c.x, cg.TANGENT | cg.HINGE | cg.MIXED | cg.DETERMINISTIC)
+    assert np.array_equal(K1, K2) and np.array_equal(F1, F2)
 
 
 def test_tangent_check_on_gpu(arc_case):
