@@ -38,6 +38,9 @@ for _p in (ROOT, PKG_DIR):
 METRIC = "Gauss-pt residual+tangent evals/s, mixed vs FP64 GPU at stated error"
 UNIT = "GP evals/s"
 SEED = 1003
+# DRAM bytes (read + write) per Gauss point of one face_tangent_merged_kernel launch, from
+# ncu on the 101 x 101 plate (profiles/face_tangent_merged_kernel_101.md).
+TANGENT_DRAM_BYTES_PER_GP = (85.999616e6 + 1.660928e6) / 40000
 WORKLOAD = ("single-plate assembly at scale: 201x201 jittered nodes, 4x4 Gauss rule (640,000 "
             "Gauss points), quadratic RKPM, quartic window, rho = 3h, circular-arc crease R = 60 "
             "with elastic hinge Kt = 1e-3, seeded 8-mode Fourier displacement (rotations up to 60 "
@@ -337,8 +340,16 @@ def run_gpu(args):
     res_ms = ph_ms["face"] / steps
     # Compulsory bytes of the tangent per step: per-point state (32 floats), per neighbour
     # the FP32 grad / Hessian Phi and its id (24 B), per pair its 2-byte contribution code,
-    # and the FP32 block accumulator written once (36 B per block).
-    alg_bytes = float((128 + 24 * n + n * (n + 1)).sum() + 36.0 * asm.nnz / 9.0)
+    # per merged entry its block slot and contribution range (8 B), and the FP32 block
+    # accumulator once (48 B per block: three 16-byte vectors).
+    work = asm.stats()
+    alg_bytes = float((128 + 24 * n + n * (n + 1)).sum() + 8.0 * work["entries"] + 48.0 * work["blocks"])
+    tan_launches = max(int(ph_n["tangent"]) // steps, 1)
+    # DRAM traffic of one tangent launch, from the ncu capture of the 101 x 101 plate
+    # (profiles/face_tangent_merged_kernel_101.md: 87.66 MB read + write for a launch of
+    # 40,000 Gauss points), scaled by the Gauss points of this launch; the traffic per point
+    # is the same at both sizes (the same n, the same per-point records).
+    traffic = TANGENT_DRAM_BYTES_PER_GP * len(n) / tan_launches
     flops_fp64 = float((121 * n + 200).sum())                 # residual path (FP64)
     flops_total = float((181 * n * (n + 1) / 2 + 364 * n + 200).sum())
     flops_fp32 = flops_total - flops_fp64
@@ -347,12 +358,14 @@ def run_gpu(args):
     achieved_gbs = alg_bytes / (tan_ms * 1e-3) / 1e9
     roofline = {
         "bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-        "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,
+        "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": traffic,
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, 101x101 plate, scaled per Gauss point",
         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
         "kernel": "face_tangent_merged_kernel (FP32 tangent, merged contributions)",
-        "launch_ms": tan_ms / max(ph_n["tangent"] // steps, 1), "launches_per_step": int(ph_n["tangent"] // steps),
-        "step_ms": tan_ms, "algorithmic_bytes_per_step": alg_bytes,
-        "binding_unit": "L1 / shared-memory data pipe (ncu: ~82% of peak, records read per contribution)",
+        "launch_ms": tan_ms / tan_launches, "launches_per_step": tan_launches,
+        "algorithmic_bytes_per_launch": alg_bytes / tan_launches,
+        "step_ms": tan_ms, "algorithmic_bytes_per_step": alg_bytes, "work": work,
+        "binding_unit": "L1 / shared-memory data pipe (ncu: 90% of peak, records read per contribution)",
         "pipes": {
             "fp32_tangent": {"achieved_tflops": flops_fp32 / (tan_ms * 1e-3) / 1e12, "peak_tflops": p32,
                              "frac": flops_fp32 / (tan_ms * 1e-3) / 1e12 / p32 if p32 > 0 else None,

@@ -421,6 +421,19 @@ int cgb_assembler_download_pattern(const cgb_assembler* a, int32_t* outer, int32
   });
 }
 
+int cgb_assembler_stats(cgb_assembler* a, int64_t out[4]) {
+  if (!a) return CGB_ERR_INVALID;
+  return guarded(a->ctx, [&] {
+    need(out != nullptr, "cgb_assembler_stats: out is NULL");
+    bind_device(a->ctx);
+    cgb::merge_prepare(a);
+    out[0] = a->n_pairs;
+    out[1] = a->n_blocks;
+    out[2] = a->mrg_n_ent;
+    out[3] = a->mrg_n_direct;
+  });
+}
+
 int cgb_assembler_download_map(const cgb_assembler* a, int32_t* map, int64_t n_entries) {
   if (!a || !map) return CGB_ERR_INVALID;
   cgb_context* ctx = a->ctx;

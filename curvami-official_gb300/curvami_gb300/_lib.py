@@ -46,6 +46,7 @@ SIGNATURES = {
     "cgb_assembler_pattern": (i32, [vp, C.POINTER(i32), C.POINTER(i64)]),
     "cgb_assembler_download_pattern": (i32, [vp, vp, vp]),
     "cgb_assembler_download_map": (i32, [vp, vp, i64]),
+    "cgb_assembler_stats": (i32, [vp, vp]),
     "cgb_set_material": (i32, [vp, vp, vp, vp]),
     "cgb_assemble": (i32, [vp, vp, vp, vp, i32]),
     "cgb_assemble_device": (i32, [vp, vp, vp, vp, i32]),

@@ -203,6 +203,12 @@ class NonLinearAssembler:
         self.ctx.check(self.ctx.lib.cgb_assembler_download_pattern(self.h, _p(outer), _p(inner)))
         return outer, inner[: self.nnz]
 
+    def stats(self):
+        """{"pairs", "blocks", "entries", "direct_groups"}: sizes of the assembler's work."""
+        out = np.zeros(4, np.int64)
+        self.ctx.check(self.ctx.lib.cgb_assembler_stats(self.h, _p(out)))
+        return dict(zip(("pairs", "blocks", "entries", "direct_groups"), (int(v) for v in out)))
+
     def csr_mapping(self):
         n = np.diff(self.faces.download()["ptr"])
         total = int((n * (n + 1) // 2).sum())

@@ -142,6 +142,11 @@ int cgb_assembler_download_pattern(const cgb_assembler* a, int32_t* outer, int32
  * concatenated: n(n+1)/2 entries per point, the position of min(ni, nj) among the
  * block rows of column max(ni, nj). */
 int cgb_assembler_download_map(const cgb_assembler* a, int32_t* map, int64_t n_entries);
+/* Sizes of the assembler's work (no reference counterpart; for measurement): out[0] local
+ * pairs over all face Gauss points (sum n(n+1)/2), out[1] 3x3 blocks of K, out[2] merged
+ * entries of the FP32 tangent (distinct blocks per group of 16 consecutive Gauss points),
+ * out[3] groups too large to merge. The first call builds the merge tables. */
+int cgb_assembler_stats(cgb_assembler* a, int64_t out[4]);
 /* LaminateProperties A, B, D (plate/PlateData.h:20-35), row-major 3x3 each. */
 int cgb_set_material(cgb_assembler* a, const double* A, const double* B, const double* D);
 

@@ -241,6 +241,15 @@ def test_deterministic_bitwise(ctx, arc_case):
         assert np.array_equal(K1, K3) and np.array_equal(F1, F3)
 
 
+def test_assembler_stats(arc_case):
+    c = arc_case
+    n = np.diff(c.ref["ptr"])
+    st = c.asm.stats()
+    assert st["pairs"] == int((n * (n + 1) // 2).sum())
+    assert st["blocks"] == c.asm.nnz // 9
+    assert 0 < st["entries"] < st["pairs"] and st["direct_groups"] == 0
+
+
 def test_mixed_wide_supports(o, ctx):
     """About 60 neighbours per point: a group of 16 points has more pairs than the merge
     setup sorts, so the FP32 tangent scatters those groups pair by pair and the
@@ -249,6 +258,7 @@ def test_mixed_wide_supports(o, ctx):
     x = 0.3 * synth.fourier_field(p.node_xy, np.random.default_rng(32), lam=(3.0, 10.0))
     c = Case(o, ctx, p, x)
     assert int(np.diff(c.ref["ptr"]).max()) >= 45
+    assert c.asm.stats()["direct_groups"] > 0
     Ko, Fo = c.oracle(c.x)
     for det in (0, cg.DETERMINISTIC):
         K, F = c.asm.assemble(c.x, cg.TANGENT | cg.HINGE | cg.MIXED | det)
