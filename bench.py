@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n-side", type=int, default=201, help="nodes per side (201 = the workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="assembly", choices=["assembly", "batched"],
+                    help="assembly: the single-plate assembly at scale (the metric's workload); "
+                         "batched: 64 uneven plates in one graph launch per step")
+    ap.add_argument("--plates", type=int, default=64, help="plates of the batched workload")
     ap.add_argument("--cpu-sample-rows", type=int, default=20,
                     help="cell rows of the plate in the CPU sample (200 rows = the whole plate)")
     return ap.parse_args()
@@ -389,6 +393,8 @@ def run_gpu(args):
 
     v_mix = world * n_gp / (ms_mix * 1e-3)
     v_f64 = world * n_gp / (ms_f64 * 1e-3)
+    shape = shape_stage(cg, ctx, args, rank == 0 and not args.no_cpu_baseline)
+
     line = {
         "metric": METRIC, "value": v_mix, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": W, "ms_per_step": ms_mix, "higher_is_better": True, "scaling": "weak",
@@ -412,6 +418,7 @@ def run_gpu(args):
         "roofline": roofline,
         "cpu_baseline": cpu,
         "clocks": clocks,
+        "shape_stage": shape,
     }
     if rank == 0:
         print(json.dumps(line))
@@ -420,10 +427,188 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------------
+# Shape-function stage alone (1,000,000 points over a 401 x 401 jittered node grid)
+# ---------------------------------------------------------------------------------
+
+SHAPE_SEED = 1002
+
+
+def reproducing_error(d, node_xy, pts, scale):
+    """max over points of |scale^|a| sum_I D^a Phi_I t_I^b - a! delta_ab|, t_I = (X_I - x) /
+    scale, for the quadratic monomials b and the jets a = value, x, y, xx, yy, xy (the RKPM
+    reproducing conditions, GlobalRKPM.h:361-397), per derivative order 0 / 1 / 2."""
+    import torch
+
+    dev = torch.device("cuda")
+    ptr = torch.from_numpy(d["ptr"]).to(dev)
+    n = len(ptr) - 1
+    row = torch.repeat_interleave(torch.arange(n, device=dev), ptr[1:] - ptr[:-1])
+    idx = torch.from_numpy(d["idx"].astype(np.int64)).to(dev)
+    X = torch.from_numpy(node_xy).to(dev)[idx]
+    P = torch.from_numpy(pts).to(dev)[row]
+    t = (X - P) / scale
+    tx, ty = t[:, 0], t[:, 1]
+    mono = [torch.ones_like(tx), tx, ty, tx * tx, tx * ty, ty * ty]
+    dp = torch.from_numpy(d["dpsi"].reshape(-1, 2)).to(dev)
+    ddp = torch.from_numpy(d["ddpsi"].reshape(-1, 3)).to(dev)
+    jets = [torch.from_numpy(d["psi"]).to(dev), dp[:, 0] * scale, dp[:, 1] * scale,
+            ddp[:, 0] * scale ** 2, ddp[:, 1] * scale ** 2, ddp[:, 2] * scale ** 2]
+    expect = {(0, 0): 1.0, (1, 1): 1.0, (2, 2): 1.0, (3, 3): 2.0, (4, 5): 2.0, (5, 4): 1.0}
+    worst = [0.0, 0.0, 0.0]
+    for a, J in enumerate(jets):
+        for b, m in enumerate(mono):
+            acc = torch.zeros(n, dtype=torch.float64, device=dev).index_add_(0, row, J * m)
+            acc -= expect.get((a, b), 0.0)
+            order = 0 if a == 0 else (1 if a < 3 else 2)
+            worst[order] = max(worst[order], float(acc.abs().max()))
+    return {"order0": worst[0], "order1": worst[1], "order2": worst[2]}
+
+
+def shape_stage(cg, ctx, args, with_cpu):
+    from curvami_gb300 import synth
+
+    plate, pts = synth.config_shape_points(seed=SHAPE_SEED)
+    ctx.set_nodes(plate.node_xy)
+    kw = dict(rho=plate.rho, order=plate.order, creases=plate.creases, rho_node=plate.rho_node,
+              kernel=plate.kernel)
+    steps = max(3, args.steps // 4)
+    for _ in range(max(args.warmup, 3)):
+        cg.shape_functions(ctx, pts, **kw)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sh = cg.shape_functions(ctx, pts, **kw)
+    wall = (time.perf_counter() - t0) / steps
+    ctx.profile(True)
+    ctx.profile_read(reset=True)
+    sh = cg.shape_functions(ctx, pts, **kw)
+    ph, _ = ctx.profile_read(reset=True)
+    ctx.profile(False)
+    d = sh.download()
+    nnz = int(d["ptr"][-1])
+    n = np.diff(d["ptr"])
+    out = {
+        "workload": ("1,000,000 uniform points in [0,200]^2 over 401x401 jittered nodes (+/-0.2h), quadratic "
+                     "basis, cubic B-spline window, per-node support radius U[2.5h, 3.5h], one straight cut "
+                     "along the node row y = 100; outputs Phi, grad Phi, Hessian Phi (FP64)"),
+        "seed": SHAPE_SEED, "n_points": len(pts), "pairs": nnz, "neighbours_min_mean_max":
+            [int(n.min()), float(n.mean()), int(n.max())],
+        "value": len(pts) / wall, "unit": "points/s", "ms_per_build": wall * 1e3,
+        "phases_ms": {k: ph[k] for k in ("frnn", "crease", "rkpm")},
+        "rkpm_points_per_s": len(pts) / (ph["rkpm"] * 1e-3) if ph["rkpm"] > 0 else None,
+        "reproducing_error": reproducing_error(d, plate.node_xy, pts, 1.5),
+        "precision": "fp64",
+    }
+    if with_cpu:
+        # The oracle's restatement of GlobalFRNN::execute + GlobalRKPM::solve (OpenMP, all
+        # host threads) on the first 20,000 points, and the GPU's difference from it there.
+        from oracle import Oracle
+
+        o = Oracle(native=True)
+        m = 20000
+        t0 = time.perf_counter()
+        ptr, idx, sdist = o.frnn(plate.node_xy, pts[:m], plate.rho, plate.rho_node)
+        psi, dpsi, ddpsi, bad, rc = o.rkpm(plate.node_xy, pts[:m], ptr, idx, sdist, plate.rho, plate.order,
+                                           plate.creases, plate.rho_node, plate.kernel)
+        t_cpu = time.perf_counter() - t0
+        e = int(ptr[-1])
+        same = bool(np.array_equal(ptr, d["ptr"][: m + 1]) and np.array_equal(idx, d["idx"][:e]))
+
+        def rel(a, b):
+            return float(np.abs(a - b).max() / np.abs(b).max())
+
+        out["cpu_baseline"] = {"value": m / t_cpu, "unit": "points/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": f"first {m} points (FRNN + RKPM)"}
+        out["error_vs_oracle"] = {
+            "neighbours_bit_exact": same,
+            "psi": rel(d["psi"][:e], psi), "dpsi": rel(d["dpsi"][:e].reshape(-1), dpsi.reshape(-1)),
+            "ddpsi": rel(d["ddpsi"][:e].reshape(-1), ddpsi.reshape(-1)), "sample_points": m}
+    return out
+
+
+# ---------------------------------------------------------------------------------
+# Batched uneven plates: one assembler over all plates, one CUDA-graph launch per step
+# ---------------------------------------------------------------------------------
+
+BATCH_SEED = 1004
+
+
+def run_batched(args):
+    import torch
+
+    import curvami_gb300 as cg
+    from curvami_gb300 import autotune as at
+    from curvami_gb300 import synth
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    plates, xs = synth.config_batched(args.plates, seed=BATCH_SEED + rank)
+    gen_s = time.perf_counter() - t0
+    ctx = cg.Context(local)
+    t0 = time.perf_counter()
+    batch = cg.PlateBatch(plates, ctx)
+    setup_s = time.perf_counter() - t0
+    asm = batch.asm
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    x_d = torch.from_numpy(np.concatenate(xs)).to("cuda")
+    K_d = torch.empty(asm.nnz, dtype=torch.float64, device="cuda")
+    F_d = torch.empty(asm.n_dofs, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    MIX = cg.TANGENT | cg.HINGE | cg.MIXED
+    F64 = cg.TANGENT | cg.HINGE
+    name = torch.cuda.get_device_name(local).replace(" ", "_")
+    tune = at.autotune(asm, x_d.data_ptr(), K_d.data_ptr(), F_d.data_ptr(), MIX, device_name=name)
+
+    def timed_graph(flags, steps, warmup):
+        g = asm.graph(x_d.data_ptr(), K_d.data_ptr(), F_d.data_ptr(), flags)
+        for _ in range(warmup):
+            g.launch()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            g.launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        g.close()
+        return e0.elapsed_time(e1) / steps
+
+    W = max(args.warmup, 3)
+    with ClockSampler(local) as clk:
+        ms_mix = timed_graph(MIX, args.steps, W)
+    ms_f64 = timed_graph(F64, max(3, args.steps // 4), 3)
+    n = np.diff(batch.faces.download()["ptr"])
+    sides = [int(p.meta["n_side"]) for p in plates]
+    line = {
+        "metric": METRIC, "value": world * batch.n_gp / (ms_mix * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": W, "ms_per_step": ms_mix, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp64 residual + fp32 tangent", "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": (f"batched uneven plates: {len(plates)} independent plates, node side U{{21..161}}, "
+                                "4x4 rule, 1-3 non-crossing straight or arc creases, Kt log-uniform [1e-4, 1e-1], "
+                                "seeded smooth displacement per plate; all plates in one assembler, one CUDA-graph "
+                                "launch per step"),
+                   "seed": BATCH_SEED, "plates": len(plates), "n_gauss_points": batch.n_gp,
+                   "n_nodes": int(batch.node_offset[-1]), "nnz_K": asm.nnz, "sides_min_max": [min(sides), max(sides)],
+                   "creases": int(sum(len(p.creases) for p in plates)), "mean_neighbours": float(n.mean()),
+                   "generate_s": gen_s, "setup_s": setup_s},
+        "fp64": {"value": world * batch.n_gp / (ms_f64 * 1e-3), "ms_per_step": ms_f64, "mixed_over_fp64": ms_f64 / ms_mix},
+        "autotune": {"tuning": list(tune["tuning"]), "cached": tune["cached"], "key": tune["key"],
+                     "ms": tune["ms"], "tried_ms": tune["tried"]},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
     else:
         run_gpu(args)
 

@@ -16,7 +16,7 @@ LIB = os.path.join(OUT_DIR, "libcurvami_gb300.so")
 PEAKS = os.path.join(OUT_DIR, "libcgb_peaks.so")
 OBJ = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-UNITS = ["shape", "pattern", "assemble", "capi", "noalloc"]
+UNITS = ["shape", "pattern", "assemble", "capi", "noalloc", "batch"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
 

@@ -894,16 +894,22 @@ struct MergeArgs {
   const uint16_t* code;       // point (4) | i (6) | j (6)
 };
 
-// The block of the local pair (i, j) of one point from the frame (fr[0..2]), the
-// I-side record (ri[0..2]) and the J-side record (rj), as in phase2_group.
+// The block of the local pair (i, j) of one point from the frame (fr[0..1]: a1 | b.v,
+// a2), the I-side record (ri[0..1]) and the J-side record (rj), as in phase2_group. The
+// unit normal b = a1 x a2 / |a1 x a2| and g_I = a1 c0_I + a2 c1_I are rebuilt from the
+// frame here rather than read: the kernel is bound by shared-memory wavefronts, not FMAs.
 template <bool BZERO>
 __device__ __forceinline__ void merged_pair(const float4* fr, const float4* ri, const float4* rj, float v[9]) {
-  const float4 f0 = fr[0], f1 = fr[1], f2 = fr[2];
-  const float a1t[3] = {f0.x, f0.y, f0.z}, a2t[3] = {f1.x, f1.y, f1.z}, bt[3] = {f2.x, f2.y, f2.z};
+  const float4 f0 = fr[0], f1 = fr[1];
+  const float a1t[3] = {f0.x, f0.y, f0.z}, a2t[3] = {f1.x, f1.y, f1.z};
+  float bt[3] = {a1t[1] * a2t[2] - a1t[2] * a2t[1], a1t[2] * a2t[0] - a1t[0] * a2t[2],
+                 a1t[0] * a2t[1] - a1t[1] * a2t[0]};
+  const float rn = rsqrtf(bt[0] * bt[0] + bt[1] * bt[1] + bt[2] * bt[2]);
+  bt[0] *= rn; bt[1] *= rn; bt[2] *= rn;
   const float bv = f0.w;
-  const float4 i0 = ri[0], i1 = ri[1], i2 = ri[2];
+  const float4 i0 = ri[0], i1 = ri[1];
   const float dxi = i0.x, dyi = i0.y, be0 = i0.z, be1 = i0.w, be2 = i1.x, Tui = i1.y;
-  const float gi[3] = {i1.z, i1.w, i2.x};
+  const float gi[3] = {a1t[0] * i1.z + a2t[0] * i1.w, a1t[1] * i1.z + a2t[1] * i1.w, a1t[2] * i1.z + a2t[2] * i1.w};
   float Y1[3], Y2[3], Y3[3], geo;
   if constexpr (BZERO) {
     const float4 j0 = rj[0], j1 = rj[1], j2 = rj[2], j3 = rj[3];
@@ -949,13 +955,19 @@ __device__ __forceinline__ void merged_pair(const float4* fr, const float4* ri, 
 template <bool BZERO, bool DET>
 __global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(FaceArgs a, const float* __restrict__ gstate,
                                                                             MergeArgs mg) {
-  constexpr int JW = BZERO ? 4 : 6;  // float4 rows of a J-side record
+  // Record strides in float4 are odd (one padding row where needed): a warp reads the
+  // records of 32 different (point, neighbour) pairs at once, and with an even stride of
+  // 2^m float4 those addresses fall into only 8 / 2^m of the 8 four-bank groups (a stride
+  // of 4 serialises a float4 load into ~16 wavefronts instead of ~4).
+  constexpr int JW = BZERO ? 5 : 7;  // float4 rows of a J-side record (4 or 6 used)
+  constexpr int IW = 3;              // float4 rows of an I-side record (2 used)
+  constexpr int FW = 3;              // float4 rows of a point frame (2 used)
   extern __shared__ __align__(16) float msm[];
   const int nmax = a.nmax;
   float* st = msm;                                          // [kState][kMG]
-  float4* fr = reinterpret_cast<float4*>(st + kState * kMG); // [kMG][3]
-  float4* ri = fr + 3 * kMG;                                // [kMG * nmax][3]
-  float4* rj = ri + 3 * kMG * nmax;                         // [kMG * nmax][JW]
+  float4* fr = reinterpret_cast<float4*>(st + kState * kMG); // [kMG][2]
+  float4* ri = fr + FW * kMG;                               // [kMG * nmax][IW]
+  float4* rj = ri + IW * kMG * nmax;                        // [kMG * nmax][JW]
   int* nid = reinterpret_cast<int*>(rj + JW * kMG * nmax);  // [kMG * nmax]
   const float* dpsi_t = static_cast<const float*>(a.dpsi_t);
   const float* ddpsi_t = static_cast<const float*>(a.ddpsi_t);
@@ -973,9 +985,8 @@ __global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(Fac
     __syncthreads();
     if (threadIdx.x < kn) {
       const int k = threadIdx.x;
-      fr[3 * k] = make_float4(st[(S_A1) * kMG + k], st[(S_A1 + 1) * kMG + k], st[(S_A1 + 2) * kMG + k], st[S_BV * kMG + k]);
-      fr[3 * k + 1] = make_float4(st[(S_A2) * kMG + k], st[(S_A2 + 1) * kMG + k], st[(S_A2 + 2) * kMG + k], 0.0f);
-      fr[3 * k + 2] = make_float4(st[(S_B) * kMG + k], st[(S_B + 1) * kMG + k], st[(S_B + 2) * kMG + k], 0.0f);
+      fr[FW * k] = make_float4(st[(S_A1) * kMG + k], st[(S_A1 + 1) * kMG + k], st[(S_A1 + 2) * kMG + k], st[S_BV * kMG + k]);
+      fr[FW * k + 1] = make_float4(st[(S_A2) * kMG + k], st[(S_A2 + 1) * kMG + k], st[(S_A2 + 2) * kMG + k], 0.0f);
     }
     // Records of every (point, neighbour) of the group (the same formulas as phase2_group).
     for (int t = threadIdx.x; t < kMG * nmax; t += blockDim.x) {
@@ -1006,10 +1017,9 @@ __global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(Fac
       const float b1 = -dyy + (ryy[0] * gI[0] + ryy[1] * gI[1] + ryy[2] * gI[2]);
       const float b2 = 2.0f * (-dxy + (rxy[0] * gI[0] + rxy[1] * gI[1] + rxy[2] * gI[2]));
       const float Tu = dx * pX + dy * pY - (dxx * Mt[0] + 2.0f * dxy * Mt[2] + dyy * Mt[1]);
-      float4* RI = ri + 3 * t;
+      float4* RI = ri + IW * t;
       RI[0] = make_float4(dx, dy, b0, b1);
-      RI[1] = make_float4(b2, Tu, gI[0], gI[1]);
-      RI[2] = make_float4(gI[2], 0.0f, 0.0f, 0.0f);
+      RI[1] = make_float4(b2, Tu, c0, c1);
       float4* RJ = rj + JW * t;
       if constexpr (BZERO) {
         float pa[3], pb[3], qc[3];
@@ -1061,7 +1071,7 @@ __global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(Fac
           while (off >= n - i) { off -= n - i; ++i; }
           const int j = i + off;
           float v[9];
-          merged_pair<BZERO>(fr + 3 * k, ri + 3 * (k * nmax + i), rj + JW * (k * nmax + j), v);
+          merged_pair<BZERO>(fr + FW * k, ri + IW * (k * nmax + i), rj + JW * (k * nmax + j), v);
           scatter_atomic<float>(a.Kacc, a.map_slot[m0 + p], nid[k * nmax + i] > nid[k * nmax + j], v);
         }
       }
@@ -1078,7 +1088,7 @@ __global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(Fac
           const unsigned code = mg.code[cbase + c0 + c];
           const int k = code >> 12, i = (code >> 6) & 63, j = code & 63;
           float v[9];
-          merged_pair<BZERO>(fr + 3 * k, ri + 3 * (k * nmax + i), rj + JW * (k * nmax + j), v);
+          merged_pair<BZERO>(fr + FW * k, ri + IW * (k * nmax + i), rj + JW * (k * nmax + j), v);
           if (nid[k * nmax + i] > nid[k * nmax + j]) {
 #pragma unroll
             for (int r = 0; r < 3; ++r)
@@ -1211,7 +1221,7 @@ void ensure_side_stream(cgb_assembler* a) {
   CGB_CUDA(cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking));
   CGB_CUDA(cudaEventCreateWithFlags(&a->ev_start, cudaEventDisableTiming));
   CGB_CUDA(cudaEventCreateWithFlags(&a->ev_done, cudaEventDisableTiming));
-  for (int c = 0; c < kChunks; ++c) CGB_CUDA(cudaEventCreateWithFlags(&a->ev_chunk[c], cudaEventDisableTiming));
+  for (int c = 0; c < 8; ++c) CGB_CUDA(cudaEventCreateWithFlags(&a->ev_chunk[c], cudaEventDisableTiming));
 }
 
 }  // namespace
@@ -1316,7 +1326,8 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   // The residual kernel of chunk c + 1 (FP64 pipe) runs beside the tangent kernel of
   // chunk c (FP32 pipe, L2 atomics) on a second stream; chunks are multiples of 32 points.
   ensure_side_stream(a);
-  const int n_chunks = S->n_gp >= 65536 ? kChunks : 1;
+  const int n_chunks = a->tuning.n_chunks > 0 ? a->tuning.n_chunks : (S->n_gp >= 65536 ? kChunks : 1);
+  const int rthreads = a->tuning.residual_threads > 0 ? a->tuning.residual_threads : 256;
   const int chunk = ((S->n_gp + n_chunks - 1) / n_chunks + 31) / 32 * 32;
   int nface = 0;
   const size_t tsm = static_cast<size_t>(kTanWarps) * ((kState * 32 + kRec * fa.nmax) * tk + fa.nmax * sizeof(int));
@@ -1329,18 +1340,18 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     fa.g_end = std::min(S->n_gp, (c + 1) * chunk);
     if (fa.g_begin >= fa.g_end) break;
     const int ncg = fa.g_end - fa.g_begin;
-    const unsigned rgrid = std::max(1u, std::min(nb(ncg, 256), static_cast<unsigned>(sms * 16)));
+    const unsigned rgrid = std::max(1u, std::min(nb(ncg, rthreads), static_cast<unsigned>(sms * 16 * (256 / rthreads))));
     prof_begin(ctx, CGB_PHASE_FACE);
     if (mixed) {
-      if (det) { if (want_K) face_residual_kernel<float, true, true><<<rgrid, 256, 0, st>>>(fa, st32);
-                 else face_residual_kernel<float, true, false><<<rgrid, 256, 0, st>>>(fa, st32); }
-      else { if (want_K) face_residual_kernel<float, false, true><<<rgrid, 256, 0, st>>>(fa, st32);
-             else face_residual_kernel<float, false, false><<<rgrid, 256, 0, st>>>(fa, st32); }
+      if (det) { if (want_K) face_residual_kernel<float, true, true><<<rgrid, rthreads, 0, st>>>(fa, st32);
+                 else face_residual_kernel<float, true, false><<<rgrid, rthreads, 0, st>>>(fa, st32); }
+      else { if (want_K) face_residual_kernel<float, false, true><<<rgrid, rthreads, 0, st>>>(fa, st32);
+             else face_residual_kernel<float, false, false><<<rgrid, rthreads, 0, st>>>(fa, st32); }
     } else {
-      if (det) { if (want_K) face_residual_kernel<double, true, true><<<rgrid, 256, 0, st>>>(fa, st64);
-                 else face_residual_kernel<double, true, false><<<rgrid, 256, 0, st>>>(fa, st64); }
-      else { if (want_K) face_residual_kernel<double, false, true><<<rgrid, 256, 0, st>>>(fa, st64);
-             else face_residual_kernel<double, false, false><<<rgrid, 256, 0, st>>>(fa, st64); }
+      if (det) { if (want_K) face_residual_kernel<double, true, true><<<rgrid, rthreads, 0, st>>>(fa, st64);
+                 else face_residual_kernel<double, true, false><<<rgrid, rthreads, 0, st>>>(fa, st64); }
+      else { if (want_K) face_residual_kernel<double, false, true><<<rgrid, rthreads, 0, st>>>(fa, st64);
+             else face_residual_kernel<double, false, false><<<rgrid, rthreads, 0, st>>>(fa, st64); }
     }
     ++nface;
     prof_end(ctx, CGB_PHASE_FACE, 1);
@@ -1356,9 +1367,9 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     };
     if (merged) {
       MergeArgs mg{a->mrg_ent_ptr.p, a->mrg_ent_slot.p, a->mrg_ent_cstart.p, a->mrg_direct.p, a->mrg_code.p};
-      const int JW = bzero ? 4 : 6;
-      const size_t msm = (static_cast<size_t>(kState) * kMG + 4 * 3 * kMG +
-                          4 * static_cast<size_t>(3 + JW) * kMG * fa.nmax) * sizeof(float) +
+      const int JW = bzero ? 5 : 7, IW = 3, FW = 3;  // record strides of the kernel
+      const size_t msm = (static_cast<size_t>(kState) * kMG + 4 * FW * kMG +
+                          4 * static_cast<size_t>(IW + JW) * kMG * fa.nmax) * sizeof(float) +
                          static_cast<size_t>(kMG) * fa.nmax * sizeof(int);
       if (msm > 220 * 1024) throw Error(CGB_ERR_CAPACITY, "assemble: neighbour lists too long for the merged tangent");
       auto kern = det ? (bzero ? face_tangent_merged_kernel<true, true> : face_tangent_merged_kernel<false, true>)
@@ -1367,6 +1378,7 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
       int per_sm = 0;
       CGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMrgThreads, msm));
       const int groups = (fa.g_end + kMG - 1) / kMG - fa.g_begin / kMG;
+      if (a->tuning.tangent_ctas_per_sm > 0) per_sm = std::min(per_sm, a->tuning.tangent_ctas_per_sm);
       const unsigned mgrid = static_cast<unsigned>(std::max(1, std::min(groups, std::max(per_sm, 1) * sms)));
       kern<<<mgrid, kMrgThreads, msm, a->side>>>(fa, st32, mg);
     } else if (mixed) {

@@ -372,6 +372,10 @@ int cgb_assembler_create(cgb_context* ctx, const cgb_shape* faces, const double*
 
 int cgb_assembler_destroy(cgb_assembler* a) {
   if (!a) return CGB_OK;
+  if (a->n_graphs > 0) {
+    if (a->ctx) a->ctx->last_error = "cgb_assembler_destroy: destroy its graphs first";
+    return CGB_ERR_INVALID;
+  }
   cgb_context* ctx = a->ctx;
   if (ctx) {
     cudaSetDevice(ctx->device);

@@ -162,6 +162,8 @@ struct cgb_assembler {
   cgb::DevBuf<int32_t> mrg_ent_cstart;// (count << 16) | first contribution within its group
   cgb::DevBuf<int8_t> mrg_direct;     // 1: group too large, scatter directly
   cgb::DevBuf<uint16_t> mrg_code;     // per pair: point | i | j, grouped by entry
+  cgb_tuning tuning{};                // launch shape (0 = library default)
+  int n_graphs = 0;                   // live cgb_graph objects on this assembler
   int64_t mrg_n_ent = 0;              // entries over all groups
   int mrg_n_direct = 0;               // groups scattered pair by pair
   // Second stream of the chunked face launch (tangent of chunk c beside residual of c+1).
@@ -208,6 +210,8 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
 // pattern.cu
 void pattern_build(cgb_assembler* a);
 void deterministic_prepare(cgb_assembler* a);
+void shape_concat(cgb_context* ctx, const cgb_shape* const* sets, const int32_t* node_offset, int n_sets,
+                  cgb_shape* out);
 // Per-block lists of K units: pairs (units [0, n_pairs) then hinge pairs) or merged entries
 // (units [0, mrg_n_ent) then hinge pairs; needs merge_prepare and no direct group).
 void deterministic_pair_lists(cgb_assembler* a);

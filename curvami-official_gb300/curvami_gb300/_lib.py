@@ -47,6 +47,11 @@ SIGNATURES = {
     "cgb_assembler_download_pattern": (i32, [vp, vp, vp]),
     "cgb_assembler_download_map": (i32, [vp, vp, i64]),
     "cgb_assembler_stats": (i32, [vp, vp]),
+    "cgb_shape_concat": (i32, [vp, vp, vp, i32, vp]),
+    "cgb_assembler_set_tuning": (i32, [vp, vp]),
+    "cgb_graph_create": (i32, [vp, vp, vp, vp, i32, vp]),
+    "cgb_graph_launch": (i32, [vp]),
+    "cgb_graph_destroy": (i32, [vp]),
     "cgb_set_material": (i32, [vp, vp, vp, vp]),
     "cgb_assemble": (i32, [vp, vp, vp, vp, i32]),
     "cgb_assemble_device": (i32, [vp, vp, vp, vp, i32]),
@@ -56,7 +61,7 @@ SIGNATURES = {
     "cgb_profile_read": (i32, [vp, vp, vp, i32]),
 }
 
-PHASES = ("h2d", "zero", "face", "hinge", "reduce", "d2h", "tangent")
+PHASES = ("h2d", "zero", "face", "hinge", "reduce", "d2h", "tangent", "frnn", "crease", "rkpm")
 
 
 class Crease(C.Structure):
@@ -66,6 +71,10 @@ class Crease(C.Structure):
 
 class ShapeParams(C.Structure):
     _fields_ = [("rho", dbl), ("rho_node", vp), ("order", i32), ("kernel", i32)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("n_chunks", i32), ("residual_threads", i32), ("tangent_ctas_per_sm", i32)]
 
 
 class Fold(C.Structure):

@@ -126,6 +126,16 @@ class ShapeSet:
             pass
 
 
+def concat_shapes(ctx: Context, sets, node_offsets) -> ShapeSet:
+    """cgb_shape_concat: the union of several shape sets, set k's neighbour indices shifted
+    by node_offsets[k] (independent plates stacked over the union of their nodes)."""
+    arr = (C.c_void_p * len(sets))(*[st.h for st in sets])
+    off = _c(node_offsets, np.int32)
+    h = C.c_void_p()
+    ctx.check(ctx.lib.cgb_shape_concat(ctx.h, arr, _p(off), len(sets), C.byref(h)))
+    return ShapeSet(ctx, h)
+
+
 def shape_functions(ctx: Context, gp_xy, rho, order=2, creases=(), rho_node=None, kernel=0) -> ShapeSet:
     """GlobalFRNN::execute + GlobalRKPM::solve for one set of Gauss points. Raises
     CGBError (CGB_ERR_SINGULAR / CGB_ERR_PIVOT) with the reference's message on a
@@ -232,6 +242,16 @@ class NonLinearAssembler:
                                                         C.c_void_p(d_K) if d_K else None,
                                                         C.c_void_p(d_F), int(flags)))
 
+    def set_tuning(self, n_chunks=0, residual_threads=0, tangent_ctas_per_sm=0):
+        """cgb_assembler_set_tuning (0 = the library's default)."""
+        t = L.Tuning(int(n_chunks), int(residual_threads), int(tangent_ctas_per_sm))
+        self.ctx.check(self.ctx.lib.cgb_assembler_set_tuning(self.h, C.byref(t)))
+        self.tuning = (int(n_chunks), int(residual_threads), int(tangent_ctas_per_sm))
+
+    def graph(self, d_x: int, d_K: int | None, d_F: int, flags) -> "AssemblyGraph":
+        """One cgb_assemble_device call on these device buffers captured as a CUDA graph."""
+        return AssemblyGraph(self, d_x, d_K, d_F, flags)
+
     def energies(self, x):
         x = _c(x, np.float64)
         em = C.c_double(); eb = C.c_double(); eh = C.c_double()
@@ -241,6 +261,32 @@ class NonLinearAssembler:
     def close(self):
         if getattr(self, "h", None):
             self.ctx.lib.cgb_assembler_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class AssemblyGraph:
+    """cgb_graph: replay of one captured assembly with a single graph launch."""
+
+    def __init__(self, asm: NonLinearAssembler, d_x, d_K, d_F, flags):
+        self.asm = asm
+        self.ctx = asm.ctx
+        h = C.c_void_p()
+        self.ctx.check(self.ctx.lib.cgb_graph_create(asm.h, C.c_void_p(d_x), C.c_void_p(d_K) if d_K else None,
+                                                     C.c_void_p(d_F), int(flags), C.byref(h)))
+        self.h = h
+
+    def launch(self):
+        self.ctx.check(self.ctx.lib.cgb_graph_launch(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.cgb_graph_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -289,3 +335,54 @@ class PlateModel:
 
     def assemble_internal_only(self, x, flags=L.HINGE):
         return self.asm.assemble(x, flags & ~L.TANGENT)[1]
+
+
+class PlateBatch:
+    """Independent plates of uneven size assembled as one problem: each plate's shape
+    functions are built over its own nodes and creases, then stacked (concat_shapes) over
+    the union of all nodes, so one assembler — one set of launches, or one graph launch —
+    covers every plate's Gauss points. The union K is block diagonal: plate k owns dofs
+    [3 o_k, 3 o_{k+1}) and the K values [outer[3 o_k], outer[3 o_{k+1}])."""
+
+    def __init__(self, plates, ctx: Context | None = None):
+        self.plates = list(plates)
+        self.ctx = ctx or Context(0)
+        p0 = self.plates[0]
+        for p in self.plates:
+            if (p.E, p.nu, p.thickness) != (p0.E, p0.nu, p0.thickness):
+                raise ValueError("PlateBatch: every plate needs the same laminate (one material per assembler)")
+        sizes = [len(p.node_xy) for p in self.plates]
+        self.node_offset = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        faces, weights, folds, self._keep = [], [], [], []
+        for k, p in enumerate(self.plates):
+            self.ctx.set_nodes(p.node_xy)
+            kw = dict(rho=p.rho, order=p.order, creases=p.creases, rho_node=p.rho_node, kernel=p.kernel)
+            faces.append(shape_functions(self.ctx, p.faces.xy, **kw))
+            weights.append(p.faces.weight)
+            for f in p.folds:
+                folds.append((k, f, shape_functions(self.ctx, f.left.xy, **kw),
+                              shape_functions(self.ctx, f.right.xy, **kw)))
+        self.node_xy = np.concatenate([p.node_xy for p in self.plates])
+        self.ctx.set_nodes(self.node_xy)
+        off = self.node_offset[:-1]
+        self.faces = concat_shapes(self.ctx, faces, off)
+        specs = []
+        for k, f, Ls, Rs in folds:
+            L_ = concat_shapes(self.ctx, [Ls], [off[k]])
+            R_ = concat_shapes(self.ctx, [Rs], [off[k]])
+            self._keep += [L_, R_]
+            specs.append({"left": L_, "right": R_, "weight": f.left.weight, "tangent": f.left.tangent,
+                          "Kt": f.Kt, "theta0": f.theta0})
+        self.fold_specs = specs
+        self.weight = np.concatenate(weights)
+        self.asm = NonLinearAssembler(self.ctx, self.faces, self.weight, specs)
+        self.asm.set_material(*abd_isotropic(p0.E, p0.nu, p0.thickness))
+        outer, _ = self.asm.pattern()
+        self.outer = outer
+        self.n_gp = self.faces.n_gp
+
+    def dofs(self, k):
+        return slice(3 * int(self.node_offset[k]), 3 * int(self.node_offset[k + 1]))
+
+    def k_values(self, k):
+        return slice(int(self.outer[3 * self.node_offset[k]]), int(self.outer[3 * self.node_offset[k + 1]]))

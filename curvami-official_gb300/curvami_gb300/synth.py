@@ -211,6 +211,12 @@ def split_on_creases(faces: PointSet, creases, eps=1e-9, s=1e-7) -> tuple[PointS
     xy = faces.xy.copy(); w = faces.weight.copy()
     best_d = np.full(len(xy), np.inf)
     best_n = np.zeros_like(xy)
+    # Only a point within eps of a segment can be split, so each segment is tested against
+    # the points inside its bounding box grown by eps (found on the x-sorted order); the
+    # nearest segment of such a point is among those tested (ties: lower index, as before).
+    order = np.argsort(xy[:, 0], kind="stable")
+    xs = xy[order, 0]
+    pad = 2.0 * eps
     for cr in creases:
         V = np.asarray(cr["vertices"], np.float64)
         for i in range(len(V) - 1):
@@ -219,12 +225,19 @@ def split_on_creases(faces: PointSet, creases, eps=1e-9, s=1e-7) -> tuple[PointS
             v2 = float(v @ v)
             if v2 == 0.0:
                 continue
-            t = np.clip(((xy - A) @ v) / v2, 0.0, 1.0)
+            lo = np.searchsorted(xs, min(A[0], B[0]) - pad, "left")
+            hi = np.searchsorted(xs, max(A[0], B[0]) + pad, "right")
+            cand = order[lo:hi]
+            cand = cand[(xy[cand, 1] >= min(A[1], B[1]) - pad) & (xy[cand, 1] <= max(A[1], B[1]) + pad)]
+            if len(cand) == 0:
+                continue
+            P = xy[cand]
+            t = np.clip(((P - A) @ v) / v2, 0.0, 1.0)
             C = A[None, :] + t[:, None] * v[None, :]
-            d = np.linalg.norm(xy - C, axis=1)
-            better = d < best_d
-            best_d[better] = d[better]
-            best_n[better] = np.array([-v[1], v[0]]) / math.sqrt(v2)
+            d = np.linalg.norm(P - C, axis=1)
+            better = d < best_d[cand]
+            best_d[cand[better]] = d[better]
+            best_n[cand[better]] = np.array([-v[1], v[0]]) / math.sqrt(v2)
     hit = np.nonzero((best_d < eps) & ((best_n ** 2).sum(1) > 0))[0]
     if len(hit) == 0:
         return faces, 0
@@ -325,11 +338,11 @@ def config_assembly(rule: int = 4, n_side: int = 201, kernel: int = 0, seed: int
 
 
 def config_shape_points(n_points: int = 1_000_000, n_side: int = 401, per_node_rho: bool = True,
-                        seed: int = 1002) -> tuple[Plate, np.ndarray]:
+                        seed: int = 1002, kernel: int = 1) -> tuple[Plate, np.ndarray]:
     """Shape-function stage alone: n_points uniform points in [0,200]^2 over a 401x401
-    jittered node grid (+/-0.2h), quadratic basis, per-node support radius
-    U[2.5h, 3.5h] (extension) or the global 3h, one straight cut along the node row
-    y = 100 extended to the hull."""
+    jittered node grid (+/-0.2h), quadratic basis, cubic B-spline window (kernel 1; 0 is the
+    reference's quartic), per-node support radius U[2.5h, 3.5h] (extension) or the global
+    3h, one straight cut along the node row y = 100 extended to the hull."""
     rng = np.random.default_rng(seed)
     h = 0.5
     nodes = grid_nodes(n_side, n_side, h, 0.2 * h, rng)
@@ -341,6 +354,69 @@ def config_shape_points(n_points: int = 1_000_000, n_side: int = 401, per_node_r
     creases = [make_crease(verts, nodes, hull)]
     rho_node = rng.uniform(2.5 * h, 3.5 * h, size=len(nodes)) if per_node_rho else None
     plate = Plate(name=f"points{n_points}", node_xy=nodes, faces=PointSet(pts, np.ones(n_points)),
-                  creases=creases, rho=3.0 * h, rho_node=rho_node, order=2, seed=seed,
+                  creases=creases, rho=3.0 * h, rho_node=rho_node, order=2, kernel=kernel, seed=seed,
                   meta={"n_side": n_side, "h": h})
     return plate, pts
+
+
+def batched_plate(n_side: int, rng, h: float = 0.5, rule: int = 4, jitter: float = 0.1,
+                  name: str = "plate") -> Plate:
+    """One plate of the batched workload: n_side x n_side jittered nodes, 1-3 creases that
+    do not cross — either straight cuts parallel to y placed half-way between node columns
+    and at least 6h apart, or concentric circular arcs about the origin at least 6h apart —
+    each an elastic hinge with Kt log-uniform in [1e-4, 1e-1]."""
+    nodes = grid_nodes(n_side, n_side, h, jitter, rng)
+    faces = quad_gauss_points(nodes, n_side, n_side, rule)
+    hull = convex_hull(_hull_candidates(nodes))
+    side = (n_side - 1) * h
+    k = int(rng.integers(1, 4))
+    creases, folds = [], []
+    if rng.random() < 0.5:
+        lo, hi = 4, n_side - 5                      # columns with room for a support on both sides
+        cols = []
+        for c in rng.permutation(np.arange(lo, max(lo + 1, hi))):
+            if all(abs(c - d) >= 6 for d in cols):
+                cols.append(int(c))
+            if len(cols) == k:
+                break
+        for c in sorted(cols):
+            x0 = (c + 0.5) * h
+            nseg = max(4, int(math.ceil(side / h)))
+            verts = np.stack([np.full(nseg + 1, x0), np.linspace(0.0, side, nseg + 1)], axis=1)
+            creases.append(make_crease(verts, nodes, hull))
+            folds.append(make_fold(verts, 10.0 ** rng.uniform(-4, -1)))
+    else:
+        radii = []
+        for R in rng.permutation(np.linspace(0.25 * side, 0.85 * side, 16)):
+            if all(abs(R - S) >= 6 * h for S in radii):
+                radii.append(float(R))
+            if len(radii) == k:
+                break
+        for R in sorted(radii):
+            nseg = max(8, int(math.ceil(R * math.pi / 2 / (0.5 * h))))
+            ang = np.linspace(0.0, math.pi / 2, nseg + 1)
+            verts = np.stack([R * np.cos(ang), R * np.sin(ang)], axis=1)
+            verts[0, 1] = 0.0; verts[-1, 0] = 0.0
+            creases.append(make_crease(verts, nodes, hull))
+            folds.append(make_fold(verts, 10.0 ** rng.uniform(-4, -1)))
+    faces, nsplit = split_on_creases(faces, creases)
+    return Plate(name=name, node_xy=nodes, faces=faces, creases=creases, folds=folds, rho=3.0 * h, order=2,
+                 kernel=0, seed=0, meta={"n_side": n_side, "h": h, "rule": rule, "jitter": jitter,
+                                         "creases": len(creases), "split": nsplit})
+
+
+def config_batched(n_plates: int = 64, side_range=(21, 161), seed: int = 1004, rule: int = 4):
+    """Batched uneven plates: n_plates independent plates with node sides drawn uniformly
+    from side_range (the config's "21^2 to 161^2" read as the side), 1-3 non-crossing
+    straight or arc creases each, Kt log-uniform in [1e-4, 1e-1]; with every plate's seeded
+    smooth displacement field (fourier_field, wavelengths scaled to the plate)."""
+    rng = np.random.default_rng(seed)
+    plates, xs = [], []
+    for k in range(n_plates):
+        n = int(rng.integers(side_range[0], side_range[1] + 1))
+        p = batched_plate(n, rng, rule=rule, name=f"batch{k}_n{n}")
+        side = (n - 1) * 0.5
+        x = fourier_field(p.node_xy, rng, lam=(0.2 * side + 1.0, 2.0 * side + 1.0))
+        plates.append(p)
+        xs.append(x)
+    return plates, xs

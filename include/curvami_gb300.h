@@ -203,9 +203,40 @@ typedef struct {
 int cgb_assemble_face_noalloc(cgb_context* ctx, const cgb_face_problem* prob, const double* d_x,
                               double* d_K, double* d_F);
 
+/* ---- batching and graphs (no reference counterpart: the reference assembles one plate
+ * per call on the host) ------------------------------------------------------------ */
+/* The union of n_sets shape sets with the neighbour indices of set k shifted by
+ * node_offset[k]: independent plates become one set over the union of their nodes
+ * (call cgb_set_nodes with the union before building the assembler on it). The inputs
+ * stay valid and owned by the caller. */
+int cgb_shape_concat(cgb_context* ctx, const cgb_shape* const* sets, const int32_t* node_offset, int n_sets,
+                     cgb_shape** out);
+
+/* Launch shape of an assembly; 0 keeps the library's choice. n_chunks (1..8): Gauss-point
+ * chunks whose residual and tangent kernels overlap on two streams (default 4 from 65,536
+ * points, else 1); residual_threads (64, 128, 256): block size of the residual kernel
+ * (default 256); tangent_ctas_per_sm (1..3): resident CTAs per SM of the merged FP32
+ * tangent (default: as many as fit). */
+typedef struct cgb_tuning {
+  int n_chunks;
+  int residual_threads;
+  int tangent_ctas_per_sm;
+} cgb_tuning;
+int cgb_assembler_set_tuning(cgb_assembler* a, const cgb_tuning* t);
+
+/* One cgb_assemble_device call (the given device buffers and flags) captured as a CUDA
+ * graph on the context's stream; cgb_graph_launch replays it (the buffers are read and
+ * written at replay time). Creation runs the call once directly first. A graph must be
+ * destroyed before its assembler (cgb_assembler_destroy refuses while graphs exist). */
+typedef struct cgb_graph cgb_graph;
+int cgb_graph_create(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags, cgb_graph** out);
+int cgb_graph_launch(cgb_graph* g);
+int cgb_graph_destroy(cgb_graph* g);
+
 /* ---- tracing (library extension; the reference only prints wall-clock times) ------ */
-/* CUDA events around every phase of cgb_assemble / cgb_assemble_device, summed per
- * phase until read. Off by default; costs two event records per phase when on. */
+/* CUDA events around every phase of cgb_assemble / cgb_assemble_device and of
+ * cgb_shape_build, summed per phase until read. Off by default; costs two event records
+ * per phase when on. */
 enum {
   CGB_PHASE_H2D = 0,    /* x host -> device (cgb_assemble only) */
   CGB_PHASE_ZERO = 1,   /* clearing of the accumulators */
@@ -214,7 +245,10 @@ enum {
   CGB_PHASE_REDUCE = 4,  /* block -> CSC output, or the deterministic reductions */
   CGB_PHASE_D2H = 5,     /* K, F device -> host (cgb_assemble only) */
   CGB_PHASE_TANGENT = 6, /* face tangent and its scatter (second stream, overlaps FACE) */
-  CGB_N_PHASES = 7
+  CGB_PHASE_FRNN = 7,    /* shape build: neighbour count and fill (FRNN.h:23-78) */
+  CGB_PHASE_CREASE = 8,  /* shape build: node sides and Gauss-point crease indicators */
+  CGB_PHASE_RKPM = 9,    /* shape build: moments, inverse, Phi / grad / Hessian */
+  CGB_N_PHASES = 10
 };
 int cgb_profile_enable(cgb_context* ctx, int on);
 /* ms[CGB_N_PHASES] summed device time, launches[CGB_N_PHASES] kernels launched by the

@@ -84,7 +84,7 @@ def test_shape_functions(o, ctx, name):
 def test_shape_functions_per_node_radius(o, ctx):
     plate, pts = synth.config_shape_points(n_points=20000, n_side=61, per_node_rho=True, seed=11)
     ctx.set_nodes(plate.node_xy)
-    sh = cg.shape_functions(ctx, pts, plate.rho, 2, plate.creases, plate.rho_node, 0).download()
+    sh = cg.shape_functions(ctx, pts, plate.rho, 2, plate.creases, plate.rho_node, plate.kernel).download()
     ref = oracle_shapes(o, plate, pts)
     assert np.array_equal(sh["ptr"], ref["ptr"]) and np.array_equal(sh["idx"], ref["idx"])
     assert np.array_equal(sh["s"], ref["s"])
