@@ -1084,20 +1084,18 @@ __global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(Fac
         float acc[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) acc[q] = 0.0f;
+        // Codes are in the block's stored orientation (row node first); the next code is
+        // fetched while the current contribution is computed.
+        const uint16_t* codes = mg.code + cbase + c0;
+        unsigned next = cnt > 0 ? codes[0] : 0u;
         for (int c = 0; c < cnt; ++c) {
-          const unsigned code = mg.code[cbase + c0 + c];
+          const unsigned code = next;
+          if (c + 1 < cnt) next = codes[c + 1];
           const int k = code >> 12, i = (code >> 6) & 63, j = code & 63;
           float v[9];
           merged_pair<BZERO>(fr + FW * k, ri + IW * (k * nmax + i), rj + JW * (k * nmax + j), v);
-          if (nid[k * nmax + i] > nid[k * nmax + j]) {
 #pragma unroll
-            for (int r = 0; r < 3; ++r)
-#pragma unroll
-              for (int q = 0; q < 3; ++q) acc[3 * r + q] += v[3 * q + r];
-          } else {
-#pragma unroll
-            for (int q = 0; q < 9; ++q) acc[q] += v[q];
-          }
+          for (int q = 0; q < 9; ++q) acc[q] += v[q];
         }
         if constexpr (DET) {
           float* d = static_cast<float*>(a.Kc) + 9 * (e0 + e);

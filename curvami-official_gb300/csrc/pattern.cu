@@ -186,6 +186,7 @@ constexpr int kMergeGroup = 16;
 constexpr int kMergeItems = 16384;  // sortable pairs per group (8-byte keys, 128 KB)
 
 __global__ void __launch_bounds__(256) merge_groups_kernel(int n_gp, const int64_t* __restrict__ ptr,
+                                                          const int32_t* __restrict__ idx,
                                                           const int64_t* __restrict__ map_ptr,
                                                           const int32_t* __restrict__ map_slot, int phase,
                                                           int32_t* __restrict__ ent_count,
@@ -206,16 +207,22 @@ __global__ void __launch_bounds__(256) merge_groups_kernel(int n_gp, const int64
     if (phase == 0 && threadIdx.x == 0) ent_count[G] = -1;
     return;
   }
-  // Keys: slot (high 32 bits) | k i j (low 16 bits); pairs walked point by point.
+  // Keys: slot (high 32 bits) | k i j (low 16 bits); pairs walked point by point. The
+  // local pair is written row node first (i and j swapped when node(i) > node(j)), so the
+  // tangent evaluates the block in its stored orientation, K_{min,max}, and needs no
+  // transpose (the pair blocks are symmetric: K_ji = K_ij^T).
   for (int k = 0; k < g1 - g0; ++k) {
-    const int n = static_cast<int>(ptr[g0 + k + 1] - ptr[g0 + k]);
+    const int64_t p0 = ptr[g0 + k];
+    const int n = static_cast<int>(ptr[g0 + k + 1] - p0);
     const int64_t m0 = map_ptr[g0 + k] - q0;
     const int np = n * (n + 1) / 2;
     for (int p = threadIdx.x; p < np; p += blockDim.x) {
       int i = 0, off = p;
       while (off >= n - i) { off -= n - i; ++i; }
-      const int j = i + off;
-      const unsigned code = (static_cast<unsigned>(k) << 12) | (static_cast<unsigned>(i) << 6) | static_cast<unsigned>(j);
+      int j = i + off;
+      int ii = i;
+      if (idx[p0 + i] > idx[p0 + j]) { ii = j; j = i; }
+      const unsigned code = (static_cast<unsigned>(k) << 12) | (static_cast<unsigned>(ii) << 6) | static_cast<unsigned>(j);
       mkeys[m0 + p] = (static_cast<unsigned long long>(static_cast<unsigned>(map_slot[q0 + m0 + p])) << 16) | code;
     }
   }
@@ -472,7 +479,7 @@ void merge_prepare(cgb_assembler* a) {
                                 static_cast<int>(smem)));
   DevBuf<int32_t> counts(ng);
   if (ng > 0)
-    merge_groups_kernel<<<ng, 256, smem, st>>>(n_gp, S->nbr_ptr.p, a->map_ptr.p, a->map_slot.p, 0, counts.p,
+    merge_groups_kernel<<<ng, 256, smem, st>>>(n_gp, S->nbr_ptr.p, S->nbr_idx.p, a->map_ptr.p, a->map_slot.p, 0, counts.p,
                                                nullptr, nullptr, nullptr, nullptr);
   CGB_CUDA(cudaGetLastError());
   std::vector<int32_t> hc(std::max(ng, 1));
@@ -493,7 +500,7 @@ void merge_prepare(cgb_assembler* a) {
   a->mrg_n_direct = 0;
   for (int G = 0; G < ng; ++G) a->mrg_n_direct += direct[G];
   if (ng > 0)
-    merge_groups_kernel<<<ng, 256, smem, st>>>(n_gp, S->nbr_ptr.p, a->map_ptr.p, a->map_slot.p, 1, nullptr,
+    merge_groups_kernel<<<ng, 256, smem, st>>>(n_gp, S->nbr_ptr.p, S->nbr_idx.p, a->map_ptr.p, a->map_slot.p, 1, nullptr,
                                                a->mrg_ent_ptr.p, a->mrg_ent_slot.p, a->mrg_ent_cstart.p,
                                                a->mrg_code.p);
   CGB_CUDA(cudaGetLastError());
