@@ -953,7 +953,7 @@ __device__ __forceinline__ void merged_pair(const float4* fr, const float4* ri, 
 // DET: every entry's sum is stored (9 floats at unit e0 + e of a.Kc) for the ordered
 // per-block reduction instead of being added atomically; it needs no direct group.
 template <bool BZERO, bool DET>
-__global__ void __launch_bounds__(kMrgThreads, 3) face_tangent_merged_kernel(FaceArgs a, const float* __restrict__ gstate,
+__global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(FaceArgs a, const float* __restrict__ gstate,
                                                                             MergeArgs mg) {
   // Record strides in float4 are odd (one padding row where needed): a warp reads the
   // records of 32 different (point, neighbour) pairs at once, and with an even stride of
