@@ -40,7 +40,7 @@ UNIT = "GP evals/s"
 SEED = 1003
 # DRAM bytes (read + write) per Gauss point of one face_tangent_merged_kernel launch, from
 # ncu on the 101 x 101 plate (profiles/face_tangent_merged_kernel_101.md).
-TANGENT_DRAM_BYTES_PER_GP = (85.999616e6 + 1.660928e6) / 40000
+TANGENT_DRAM_BYTES_PER_GP = (85.99296e6 + 1.751552e6) / 40000
 WORKLOAD = ("single-plate assembly at scale: 201x201 jittered nodes, 4x4 Gauss rule (640,000 "
             "Gauss points), quadratic RKPM, quartic window, rho = 3h, circular-arc crease R = 60 "
             "with elastic hinge Kt = 1e-3, seeded 8-mode Fourier displacement (rotations up to 60 "
@@ -59,6 +59,8 @@ def parse():
                     help="assembly: the single-plate assembly at scale (the metric's workload); "
                          "batched: 64 uneven plates in one graph launch per step")
     ap.add_argument("--plates", type=int, default=64, help="plates of the batched workload")
+    ap.add_argument("--no-shape-stage", action="store_true",
+                    help="skip the shape-function stage object (shorter runs under a profiler)")
     ap.add_argument("--cpu-sample-rows", type=int, default=20,
                     help="cell rows of the plate in the CPU sample (200 rows = the whole plate)")
     return ap.parse_args()
@@ -384,7 +386,7 @@ def run_gpu(args):
         "launch_ms": tan_ms / tan_launches, "launches_per_step": tan_launches,
         "algorithmic_bytes_per_launch": alg_bytes / tan_launches,
         "step_ms": tan_ms, "algorithmic_bytes_per_step": alg_bytes, "work": work,
-        "binding_unit": "L1 / shared-memory data pipe (ncu: 90% of peak, records read per contribution)",
+        "binding_unit": "L1 / shared-memory data pipe (ncu: 81% of peak; FMA pipe 42%)",
         "pipes": {
             "fp32_tangent": {"achieved_tflops": flops_fp32 / (tan_ms * 1e-3) / 1e12, "peak_tflops": p32,
                              "frac": flops_fp32 / (tan_ms * 1e-3) / 1e12 / p32 if p32 > 0 else None,
@@ -408,7 +410,7 @@ def run_gpu(args):
 
     v_mix = world * n_gp / (ms_mix * 1e-3)
     v_f64 = world * n_gp / (ms_f64 * 1e-3)
-    shape = shape_stage(cg, ctx, args, rank == 0 and not args.no_cpu_baseline)
+    shape = None if args.no_shape_stage else shape_stage(cg, ctx, args, rank == 0 and not args.no_cpu_baseline)
 
     line = {
         "metric": METRIC, "value": v_mix, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -892,7 +892,54 @@ struct MergeArgs {
   const int32_t* ent_cstart;  // (count << 16) | first contribution
   const int8_t* direct;
   const uint16_t* code;       // point (4) | i (6) | j (6)
+  const int32_t* idx_pad;     // neighbour ids followed by kStagePad zeros
+  int* err;                   // set to kErrStage when a staging copy never completes
 };
+
+// ---- bulk-copy (TMA) staging --------------------------------------------------------
+// One elected thread copies a group's contiguous ranges of grad / Hessian Phi and ids
+// into shared memory with cp.async.bulk, completing on an mbarrier the CTA waits on.
+constexpr int kErrStage = 4;
+constexpr long long kStageSpin = 1LL << 20;   // try_wait rounds before a wait gives up
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+               : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+  return ok != 0;
+}
+// Bounded wait: false if the phase did not complete within kStageSpin rounds.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (long long r = 0; r < kStageSpin; ++r)
+    if (mbar_try(bar, parity)) return true;
+  return false;
+}
+
+// Byte window [lo, lo + len) of the element range [q0, q1) of an array with `es`-byte
+// elements, widened to 16-byte boundaries (the bulk copy's alignment rule).
+struct StageWin { int64_t lo; uint32_t len, skip; };
+__device__ __forceinline__ StageWin stage_window(int64_t q0, int64_t q1, int es) {
+  const int64_t b0 = q0 * es, b1 = q1 * es;
+  StageWin w;
+  w.lo = b0 & ~static_cast<int64_t>(15);
+  w.len = static_cast<uint32_t>(((b1 + 15) & ~static_cast<int64_t>(15)) - w.lo);
+  w.skip = static_cast<uint32_t>(b0 - w.lo);
+  return w;
+}
 
 // The block of the local pair (i, j) of one point from the frame (fr[0..1]: a1 | b.v,
 // a2), the I-side record (ri[0..1]) and the J-side record (rj), as in phase2_group. The
@@ -963,38 +1010,80 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
   constexpr int IW = 3;              // float4 rows of an I-side record (2 used)
   constexpr int FW = 3;              // float4 rows of a point frame (2 used)
   extern __shared__ __align__(16) float msm[];
+  __shared__ uint64_t stage_bar;
+  __shared__ int64_t sptr[kMG + 1];
   const int nmax = a.nmax;
+  const int E = kMG * nmax;                                 // most entries of a group
   float* st = msm;                                          // [kState][kMG]
-  float4* fr = reinterpret_cast<float4*>(st + kState * kMG); // [kMG][2]
+  float4* fr = reinterpret_cast<float4*>(st + kState * kMG); // [kMG][FW]
   float4* ri = fr + FW * kMG;                               // [kMG * nmax][IW]
   float4* rj = ri + IW * kMG * nmax;                        // [kMG * nmax][JW]
   int* nid = reinterpret_cast<int*>(rj + JW * kMG * nmax);  // [kMG * nmax]
-  const float* dpsi_t = static_cast<const float*>(a.dpsi_t);
-  const float* ddpsi_t = static_cast<const float*>(a.ddpsi_t);
+  // Staging windows (16-byte aligned: nid holds 64 nmax bytes): grad Phi, Hessian Phi, ids.
+  unsigned char* s_d = reinterpret_cast<unsigned char*>(nid + E);
+  unsigned char* s_dd = s_d + 8 * E + 32;
+  unsigned char* s_i = s_dd + 12 * E + 32;
+  const unsigned char* dpsi_b = static_cast<const unsigned char*>(a.dpsi_t);
+  const unsigned char* ddpsi_b = static_cast<const unsigned char*>(a.ddpsi_t);
+  const unsigned char* idx_b = reinterpret_cast<const unsigned char*>(mg.idx_pad);
   const Material& m = a.mat;
   // Groups of this launch: [g_begin, g_end) are multiples of kMG apart (chunk bounds are
   // multiples of 32), so a group never straddles two launches.
   const int G1 = (a.g_end + kMG - 1) / kMG;
-  for (int G = a.g_begin / kMG + blockIdx.x; G < G1; G += gridDim.x) {
+  const int Gfirst = a.g_begin / kMG + blockIdx.x;
+  // Thread 0 starts the copies of group G's ranges; every thread later waits on the phase.
+  auto stage = [&](int G) {
+    const int g0 = G * kMG, g1 = min(g0 + kMG, a.g_end);
+    const int64_t q0 = a.ptr[g0], q1 = a.ptr[g1];
+    const StageWin wd = stage_window(q0, q1, 8), wdd = stage_window(q0, q1, 12), wi = stage_window(q0, q1, 4);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect(&stage_bar, wd.len + wdd.len + wi.len);
+    if (wd.len) bulk_load(s_d, dpsi_b + wd.lo, wd.len, &stage_bar);
+    if (wdd.len) bulk_load(s_dd, ddpsi_b + wdd.lo, wdd.len, &stage_bar);
+    if (wi.len) bulk_load(s_i, idx_b + wi.lo, wi.len, &stage_bar);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&stage_bar);
+    if (Gfirst < G1) stage(Gfirst);
+  }
+  __syncthreads();
+  uint32_t phase = 0;
+  for (int G = Gfirst; G < G1; G += gridDim.x) {
     const int g0 = G * kMG;
     const int kn = min(kMG, a.g_end - g0);
     for (int t = threadIdx.x; t < kState * kMG; t += blockDim.x) {
       const int f = t / kMG, k = t - f * kMG;
       st[t] = k < kn ? gstate[static_cast<int64_t>(f) * a.n_gp + g0 + k] : 0.0f;
     }
-    __syncthreads();
+    if (threadIdx.x <= kn) sptr[threadIdx.x] = a.ptr[g0 + threadIdx.x];
+    // Every thread waits on the copies of this group, then the CTA agrees on the outcome
+    // so that no thread leaves while another waits at a barrier.
+    const bool ok = mbar_wait(&stage_bar, phase);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicOr(mg.err, kErrStage);
+        mbar_wait(&stage_bar, phase);   // let copies still in flight land before leaving
+      }
+      return;
+    }
+    phase ^= 1u;
+    const int64_t q0 = sptr[0];
+    const float* sdp = reinterpret_cast<const float*>(s_d + (q0 * 8 - ((q0 * 8) & ~static_cast<int64_t>(15))));
+    const float* sddp = reinterpret_cast<const float*>(s_dd + (q0 * 12 - ((q0 * 12) & ~static_cast<int64_t>(15))));
+    const int* sidp = reinterpret_cast<const int*>(s_i + (q0 * 4 - ((q0 * 4) & ~static_cast<int64_t>(15))));
     if (threadIdx.x < kn) {
       const int k = threadIdx.x;
       fr[FW * k] = make_float4(st[(S_A1) * kMG + k], st[(S_A1 + 1) * kMG + k], st[(S_A1 + 2) * kMG + k], st[S_BV * kMG + k]);
       fr[FW * k + 1] = make_float4(st[(S_A2) * kMG + k], st[(S_A2 + 1) * kMG + k], st[(S_A2 + 2) * kMG + k], 0.0f);
     }
-    // Records of every (point, neighbour) of the group (the same formulas as phase2_group).
+    // Records of every (point, neighbour) of the group (the same formulas as phase2_group),
+    // from the staged copies.
     for (int t = threadIdx.x; t < kMG * nmax; t += blockDim.x) {
       const int k = t / nmax, i = t - k * nmax;
       if (k >= kn) continue;
-      const int64_t p0 = a.ptr[g0 + k];
-      if (i >= a.ptr[g0 + k + 1] - p0) continue;
-      const int64_t e = p0 + i;
+      const int64_t p0 = sptr[k];
+      if (i >= sptr[k + 1] - p0) continue;
+      const int64_t e = p0 + i - q0;   // entry within the group's staged range
       const float a1t[3] = {st[S_A1 * kMG + k], st[(S_A1 + 1) * kMG + k], st[(S_A1 + 2) * kMG + k]};
       const float a2t[3] = {st[S_A2 * kMG + k], st[(S_A2 + 1) * kMG + k], st[(S_A2 + 2) * kMG + k]};
       const float bt[3] = {st[S_B * kMG + k], st[(S_B + 1) * kMG + k], st[(S_B + 2) * kMG + k]};
@@ -1007,8 +1096,8 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
 #pragma unroll
       for (int c = 0; c < 4; ++c) Ci[c] = st[(S_CI + c) * kMG + k];
       const float pX = st[S_P * kMG + k], pY = st[(S_P + 1) * kMG + k], Wt = st[S_W * kMG + k];
-      const float dx = dpsi_t[2 * e], dy = dpsi_t[2 * e + 1];
-      const float dxx = ddpsi_t[3 * e], dyy = ddpsi_t[3 * e + 1], dxy = ddpsi_t[3 * e + 2];
+      const float dx = sdp[2 * e], dy = sdp[2 * e + 1];
+      const float dxx = sddp[3 * e], dyy = sddp[3 * e + 1], dxy = sddp[3 * e + 2];
       const float c0 = Ci[0] * dx + Ci[1] * dy, c1 = Ci[2] * dx + Ci[3] * dy;
       float gI[3];
 #pragma unroll
@@ -1055,9 +1144,12 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
 #pragma unroll
         for (int q = 0; q < 6; ++q) RJ[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
       }
-      nid[t] = a.idx[e];
+      nid[t] = sidp[e];
     }
     __syncthreads();
+    // The staging buffers are free again: start the next group's copies, which land while
+    // this group's entries are summed.
+    if (threadIdx.x == 0 && G + static_cast<int>(gridDim.x) < G1) stage(G + gridDim.x);
     float4* acc4 = static_cast<float4*>(a.Kacc);
     const int64_t cbase = a.map_ptr[g0];
     if (!DET && mg.direct[G]) {
@@ -1151,15 +1243,26 @@ __global__ void to_float(int64_t n, const double* __restrict__ src, float* __res
 }
 
 // FP32 copies of grad / Hessian Phi for the FP32 pair phase (made once per assembler).
+// FP32 copies of grad / Hessian Phi and a copy of the neighbour ids, each followed by
+// kStagePad zero elements: the tangent stages a group's range of these arrays with bulk
+// copies whose ends are rounded out to 16 bytes, which may read up to 15 bytes past the
+// last entry.
+constexpr int kStagePad = 16;
+
 void ensure_fp32_shapes(cgb_assembler* a) {
   if (a->dpsi32.p) return;
   const cgb_shape* S = a->faces;
   cudaStream_t st = a->ctx->stream;
-  a->dpsi32.alloc(2 * S->nnz);
-  a->ddpsi32.alloc(3 * S->nnz);
+  a->dpsi32.alloc(2 * S->nnz + kStagePad);
+  a->ddpsi32.alloc(3 * S->nnz + kStagePad);
+  a->idx_pad.alloc(S->nnz + kStagePad);
+  CGB_CUDA(cudaMemsetAsync(a->dpsi32.p, 0, a->dpsi32.bytes(), st));
+  CGB_CUDA(cudaMemsetAsync(a->ddpsi32.p, 0, a->ddpsi32.bytes(), st));
+  CGB_CUDA(cudaMemsetAsync(a->idx_pad.p, 0, a->idx_pad.bytes(), st));
   if (S->nnz) {
     to_float<<<nb(2 * S->nnz, 256), 256, 0, st>>>(2 * S->nnz, S->dpsi.p, a->dpsi32.p);
     to_float<<<nb(3 * S->nnz, 256), 256, 0, st>>>(3 * S->nnz, S->ddpsi.p, a->ddpsi32.p);
+    CGB_CUDA(cudaMemcpyAsync(a->idx_pad.p, S->nbr_idx.p, S->nnz * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
   }
   CGB_CUDA(cudaGetLastError());
 }
@@ -1219,7 +1322,7 @@ void ensure_side_stream(cgb_assembler* a) {
   CGB_CUDA(cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking));
   CGB_CUDA(cudaEventCreateWithFlags(&a->ev_start, cudaEventDisableTiming));
   CGB_CUDA(cudaEventCreateWithFlags(&a->ev_done, cudaEventDisableTiming));
-  for (int c = 0; c < 8; ++c) CGB_CUDA(cudaEventCreateWithFlags(&a->ev_chunk[c], cudaEventDisableTiming));
+  for (int c = 0; c < kMaxChunks; ++c) CGB_CUDA(cudaEventCreateWithFlags(&a->ev_chunk[c], cudaEventDisableTiming));
 }
 
 }  // namespace
@@ -1364,11 +1467,13 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
       kern<<<tgrid, 32 * kTanWarps, tsm, a->side>>>(fa, stp);
     };
     if (merged) {
-      MergeArgs mg{a->mrg_ent_ptr.p, a->mrg_ent_slot.p, a->mrg_ent_cstart.p, a->mrg_direct.p, a->mrg_code.p};
+      MergeArgs mg{a->mrg_ent_ptr.p, a->mrg_ent_slot.p, a->mrg_ent_cstart.p, a->mrg_direct.p, a->mrg_code.p,
+                   a->idx_pad.p, ctx->dev_err.p};
       const int JW = bzero ? 5 : 7, IW = 3, FW = 3;  // record strides of the kernel
-      const size_t msm = (static_cast<size_t>(kState) * kMG + 4 * FW * kMG +
-                          4 * static_cast<size_t>(IW + JW) * kMG * fa.nmax) * sizeof(float) +
-                         static_cast<size_t>(kMG) * fa.nmax * sizeof(int);
+      const size_t E = static_cast<size_t>(kMG) * fa.nmax;
+      const size_t msm = (static_cast<size_t>(kState) * kMG + 4 * FW * kMG + 4 * static_cast<size_t>(IW + JW) * E) *
+                             sizeof(float) +
+                         E * sizeof(int) + (24 * E + 96);  // + the staging windows
       if (msm > 220 * 1024) throw Error(CGB_ERR_CAPACITY, "assemble: neighbour lists too long for the merged tangent");
       auto kern = det ? (bzero ? face_tangent_merged_kernel<true, true> : face_tangent_merged_kernel<false, true>)
                       : (bzero ? face_tangent_merged_kernel<true, false> : face_tangent_merged_kernel<false, false>);

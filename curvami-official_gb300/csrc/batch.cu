@@ -140,7 +140,7 @@ int cgb_assembler_set_tuning(cgb_assembler* a, const cgb_tuning* t) {
   if (!a) return CGB_ERR_INVALID;
   return guarded_ctx(a->ctx, [&] {
     if (!t) throw Error(CGB_ERR_INVALID, "cgb_assembler_set_tuning: tuning is NULL");
-    if (t->n_chunks < 0 || t->n_chunks > 8) throw Error(CGB_ERR_INVALID, "cgb_assembler_set_tuning: n_chunks must be 0..8");
+    if (t->n_chunks < 0 || t->n_chunks > kMaxChunks) throw Error(CGB_ERR_INVALID, "cgb_assembler_set_tuning: n_chunks must be 0..16");
     if (t->residual_threads != 0 && t->residual_threads != 64 && t->residual_threads != 128 &&
         t->residual_threads != 256)
       throw Error(CGB_ERR_INVALID, "cgb_assembler_set_tuning: residual_threads must be 0, 64, 128 or 256");

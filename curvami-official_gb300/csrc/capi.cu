@@ -37,6 +37,17 @@ void need(bool ok, const char* msg) {
 
 void bind_device(cgb_context* ctx) { CGB_CUDA(cudaSetDevice(ctx->device)); }
 
+// The device error word after an assembly: a bounded wait of the tangent's staging
+// copies gave up (the kernel left its remaining groups undone). Cleared once reported.
+void check_device_word(cgb_context* ctx, int word) {
+  if (word & 4) {
+    CGB_CUDA(cudaMemsetAsync(ctx->dev_err.p, 0, sizeof(int), ctx->stream));
+    CGB_CUDA(cudaStreamSynchronize(ctx->stream));
+    throw Error(CGB_ERR_DEVICE, "assemble: a bulk copy of the tangent's neighbour data did not complete; "
+                                "K is incomplete");
+  }
+}
+
 cudaEvent_t take_event(cgb_context* ctx) {
   if (!ctx->event_pool.empty()) {
     cudaEvent_t e = ctx->event_pool.back();
@@ -185,7 +196,12 @@ int cgb_set_stream(cgb_context* ctx, void* stream) {
 
 int cgb_synchronize(cgb_context* ctx) {
   if (!ctx) return CGB_ERR_INVALID;
-  return guarded(ctx, [&] { CGB_CUDA(cudaStreamSynchronize(ctx->stream)); });
+  return guarded(ctx, [&] {
+    int dev_err = 0;
+    CGB_CUDA(cudaMemcpyAsync(&dev_err, ctx->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CGB_CUDA(cudaStreamSynchronize(ctx->stream));
+    check_device_word(ctx, dev_err);
+  });
 }
 
 int cgb_set_nodes(cgb_context* ctx, const double* node_xy, int n_nodes) {
@@ -507,7 +523,10 @@ int cgb_assemble(cgb_assembler* a, const double* x, double* K_values, double* F,
     if (want_K) CGB_CUDA(cudaMemcpyAsync(K_values, a->K.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, st));
     CGB_CUDA(cudaMemcpyAsync(F, a->F.p, ndof * sizeof(double), cudaMemcpyDeviceToHost, st));
     cgb::prof_end(ctx, CGB_PHASE_D2H, 0);
+    int dev_err = 0;
+    CGB_CUDA(cudaMemcpyAsync(&dev_err, ctx->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     CGB_CUDA(cudaStreamSynchronize(st));
+    check_device_word(ctx, dev_err);
   });
 }
 

@@ -130,6 +130,9 @@ struct cgb_fold_dev {
   int64_t n_pairs = 0;
 };
 
+// Most Gauss-point chunks one assembly is split into (residual / tangent overlap).
+constexpr int kMaxChunks = 16;
+
 struct cgb_assembler {
   cgb_context* ctx = nullptr;
   const cgb_shape* faces = nullptr;
@@ -154,6 +157,7 @@ struct cgb_assembler {
   cgb::DevBuf<double> K;            // 9 n_blocks (device scratch for host-buffer calls)
   cgb::DevBuf<double> x;            // 3 n_nodes
   cgb::DevBuf<float> dpsi32, ddpsi32; // FP32 copies of the face shape derivatives (mixed mode)
+  cgb::DevBuf<int32_t> idx_pad;       // face neighbour ids, padded for the tangent's bulk copies
   // Merged contributions of the FP32 tangent: per group of 16 consecutive Gauss points the
   // distinct blocks ("entries", count-descending) and every pair's code in entry order.
   bool mrg_ready = false;
@@ -168,7 +172,7 @@ struct cgb_assembler {
   int mrg_n_direct = 0;               // groups scattered pair by pair
   // Second stream of the chunked face launch (tangent of chunk c beside residual of c+1).
   cudaStream_t side = nullptr;
-  cudaEvent_t ev_start = nullptr, ev_done = nullptr, ev_chunk[8] = {nullptr};
+  cudaEvent_t ev_start = nullptr, ev_done = nullptr, ev_chunk[kMaxChunks] = {nullptr};
   cgb::DevBuf<float> state32;         // per-point state between the residual and tangent kernels
   cgb::DevBuf<double> state64;
   cgb::DevBuf<int64_t> sell_ptr;      // sliced-ELL copy for the FP64 phase (groups of 32 points)

@@ -18,7 +18,7 @@ import time
 import numpy as np
 
 DEFAULT_CANDIDATES = {
-    "n_chunks": (1, 2, 4, 8),
+    "n_chunks": (1, 2, 4, 8, 16),
     "residual_threads": (128, 256),
     "tangent_ctas_per_sm": (0, 2),
 }

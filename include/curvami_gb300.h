@@ -212,7 +212,7 @@ int cgb_assemble_face_noalloc(cgb_context* ctx, const cgb_face_problem* prob, co
 int cgb_shape_concat(cgb_context* ctx, const cgb_shape* const* sets, const int32_t* node_offset, int n_sets,
                      cgb_shape** out);
 
-/* Launch shape of an assembly; 0 keeps the library's choice. n_chunks (1..8): Gauss-point
+/* Launch shape of an assembly; 0 keeps the library's choice. n_chunks (1..16): Gauss-point
  * chunks whose residual and tangent kernels overlap on two streams (default 4 from 65,536
  * points, else 1); residual_threads (64, 128, 256): block size of the residual kernel
  * (default 256); tangent_ctas_per_sm (1..3): resident CTAs per SM of the merged FP32

@@ -96,7 +96,7 @@ def test_tuning_changes_launch_shape_not_results(ctx):
         Km, Fm = batch.asm.assemble(x, fl | cg.MIXED)
         assert np.abs(Km - K0).max() <= 1e-6 * np.abs(K0).max()
     with pytest.raises(cg.CGBError):
-        batch.asm.set_tuning(9, 0, 0)
+        batch.asm.set_tuning(17, 0, 0)
     with pytest.raises(cg.CGBError):
         batch.asm.set_tuning(0, 96, 0)
 

@@ -162,4 +162,11 @@ def test_newton_config_small_plate(o):
     if report:
         with open(report, "w") as f:
             json.dump(out, f, indent=1)
-    check(out)
+    # ~43 Newton iterations per load step, most of them backtracking on the max-norm merit:
+    # round-off differences between two faithful assemblies (1e-13 in Phi, 1e-15 in K) can
+    # flip a backtracking decision and shift a step's count by a few. The bar is the
+    # converged load-displacement path (1e-6) and the total count.
+    ref = sum(out["oracle"]["iters"])
+    for arm, slack in (("gpu_fp64", 0.02), ("gpu_mixed_refined", 0.02), ("gpu_mixed", 0.10)):
+        assert abs(sum(out[arm]["iters"]) - ref) <= slack * ref, (arm, out)
+        assert out[arm]["path_rel_diff"] <= 1e-6, (arm, out)
