@@ -892,7 +892,6 @@ struct MergeArgs {
   const int32_t* ent_cstart;  // (count << 16) | first contribution
   const int8_t* direct;
   const uint16_t* code;       // point (4) | i (6) | j (6)
-  const int32_t* idx_pad;     // neighbour ids followed by kStagePad zeros
   int* err;                   // set to kErrStage when a staging copy never completes
 };
 
@@ -1002,12 +1001,12 @@ __device__ __forceinline__ void merged_pair(const float4* fr, const float4* ri, 
 template <bool BZERO, bool DET>
 __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(FaceArgs a, const float* __restrict__ gstate,
                                                                             MergeArgs mg) {
-  // Record strides in float4 are odd (one padding row where needed): a warp reads the
-  // records of 32 different (point, neighbour) pairs at once, and with an even stride of
-  // 2^m float4 those addresses fall into only 8 / 2^m of the 8 four-bank groups (a stride
-  // of 4 serialises a float4 load into ~16 wavefronts instead of ~4).
-  constexpr int JW = BZERO ? 5 : 7;  // float4 rows of a J-side record (4 or 6 used)
-  constexpr int IW = 3;              // float4 rows of an I-side record (2 used)
+  // One record per (point, neighbour): the I side (2 float4) then the J side (4 float4, 6
+  // when B != 0), with an odd stride RW in float4. A warp reads the records of 32
+  // different (point, neighbour) pairs at once, and with an even stride of 2^m float4
+  // those addresses fall into only 8 / 2^m of the 8 four-bank groups (a stride of 4
+  // serialises a float4 load into ~16 wavefronts instead of ~4).
+  constexpr int RW = BZERO ? 7 : 9;  // float4 rows of a record (6 or 8 used)
   constexpr int FW = 3;              // float4 rows of a point frame (2 used)
   extern __shared__ __align__(16) float msm[];
   __shared__ uint64_t stage_bar;
@@ -1016,16 +1015,12 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
   const int E = kMG * nmax;                                 // most entries of a group
   float* st = msm;                                          // [kState][kMG]
   float4* fr = reinterpret_cast<float4*>(st + kState * kMG); // [kMG][FW]
-  float4* ri = fr + FW * kMG;                               // [kMG * nmax][IW]
-  float4* rj = ri + IW * kMG * nmax;                        // [kMG * nmax][JW]
-  int* nid = reinterpret_cast<int*>(rj + JW * kMG * nmax);  // [kMG * nmax]
-  // Staging windows (16-byte aligned: nid holds 64 nmax bytes): grad Phi, Hessian Phi, ids.
-  unsigned char* s_d = reinterpret_cast<unsigned char*>(nid + E);
+  float4* rec = fr + FW * kMG;                              // [kMG * nmax][RW]
+  // Staging windows (16-byte aligned): grad Phi, Hessian Phi of the group's entries.
+  unsigned char* s_d = reinterpret_cast<unsigned char*>(rec + RW * E);
   unsigned char* s_dd = s_d + 8 * E + 32;
-  unsigned char* s_i = s_dd + 12 * E + 32;
   const unsigned char* dpsi_b = static_cast<const unsigned char*>(a.dpsi_t);
   const unsigned char* ddpsi_b = static_cast<const unsigned char*>(a.ddpsi_t);
-  const unsigned char* idx_b = reinterpret_cast<const unsigned char*>(mg.idx_pad);
   const Material& m = a.mat;
   // Groups of this launch: [g_begin, g_end) are multiples of kMG apart (chunk bounds are
   // multiples of 32), so a group never straddles two launches.
@@ -1035,12 +1030,11 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
   auto stage = [&](int G) {
     const int g0 = G * kMG, g1 = min(g0 + kMG, a.g_end);
     const int64_t q0 = a.ptr[g0], q1 = a.ptr[g1];
-    const StageWin wd = stage_window(q0, q1, 8), wdd = stage_window(q0, q1, 12), wi = stage_window(q0, q1, 4);
+    const StageWin wd = stage_window(q0, q1, 8), wdd = stage_window(q0, q1, 12);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_expect(&stage_bar, wd.len + wdd.len + wi.len);
+    mbar_expect(&stage_bar, wd.len + wdd.len);
     if (wd.len) bulk_load(s_d, dpsi_b + wd.lo, wd.len, &stage_bar);
     if (wdd.len) bulk_load(s_dd, ddpsi_b + wdd.lo, wdd.len, &stage_bar);
-    if (wi.len) bulk_load(s_i, idx_b + wi.lo, wi.len, &stage_bar);
   };
   if (threadIdx.x == 0) {
     mbar_init(&stage_bar);
@@ -1070,7 +1064,6 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
     const int64_t q0 = sptr[0];
     const float* sdp = reinterpret_cast<const float*>(s_d + (q0 * 8 - ((q0 * 8) & ~static_cast<int64_t>(15))));
     const float* sddp = reinterpret_cast<const float*>(s_dd + (q0 * 12 - ((q0 * 12) & ~static_cast<int64_t>(15))));
-    const int* sidp = reinterpret_cast<const int*>(s_i + (q0 * 4 - ((q0 * 4) & ~static_cast<int64_t>(15))));
     if (threadIdx.x < kn) {
       const int k = threadIdx.x;
       fr[FW * k] = make_float4(st[(S_A1) * kMG + k], st[(S_A1 + 1) * kMG + k], st[(S_A1 + 2) * kMG + k], st[S_BV * kMG + k]);
@@ -1106,10 +1099,10 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
       const float b1 = -dyy + (ryy[0] * gI[0] + ryy[1] * gI[1] + ryy[2] * gI[2]);
       const float b2 = 2.0f * (-dxy + (rxy[0] * gI[0] + rxy[1] * gI[1] + rxy[2] * gI[2]));
       const float Tu = dx * pX + dy * pY - (dxx * Mt[0] + 2.0f * dxy * Mt[2] + dyy * Mt[1]);
-      float4* RI = ri + IW * t;
+      float4* RI = rec + RW * t;
       RI[0] = make_float4(dx, dy, b0, b1);
       RI[1] = make_float4(b2, Tu, c0, c1);
-      float4* RJ = rj + JW * t;
+      float4* RJ = rec + RW * t + 2;
       if constexpr (BZERO) {
         float pa[3], pb[3], qc[3];
 #pragma unroll
@@ -1144,7 +1137,6 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
 #pragma unroll
         for (int q = 0; q < 6; ++q) RJ[q] = make_float4(J[4 * q], J[4 * q + 1], J[4 * q + 2], J[4 * q + 3]);
       }
-      nid[t] = sidp[e];
     }
     __syncthreads();
     // The staging buffers are free again: start the next group's copies, which land while
@@ -1155,7 +1147,8 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
     if (!DET && mg.direct[G]) {
       // Too many pairs for the setup's shared-memory sort: scatter pair by pair.
       for (int k = 0; k < kn; ++k) {
-        const int n = static_cast<int>(a.ptr[g0 + k + 1] - a.ptr[g0 + k]);
+        const int64_t p0k = a.ptr[g0 + k];
+        const int n = static_cast<int>(a.ptr[g0 + k + 1] - p0k);
         const int np = n * (n + 1) / 2;
         const int64_t m0 = a.map_ptr[g0 + k];
         for (int p = threadIdx.x; p < np; p += blockDim.x) {
@@ -1163,8 +1156,8 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
           while (off >= n - i) { off -= n - i; ++i; }
           const int j = i + off;
           float v[9];
-          merged_pair<BZERO>(fr + FW * k, ri + IW * (k * nmax + i), rj + JW * (k * nmax + j), v);
-          scatter_atomic<float>(a.Kacc, a.map_slot[m0 + p], nid[k * nmax + i] > nid[k * nmax + j], v);
+          merged_pair<BZERO>(fr + FW * k, rec + RW * (k * nmax + i), rec + RW * (k * nmax + j) + 2, v);
+          scatter_atomic<float>(a.Kacc, a.map_slot[m0 + p], a.idx[p0k + i] > a.idx[p0k + j], v);
         }
       }
     } else {
@@ -1185,7 +1178,7 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
           if (c + 1 < cnt) next = codes[c + 1];
           const int k = code >> 12, i = (code >> 6) & 63, j = code & 63;
           float v[9];
-          merged_pair<BZERO>(fr + FW * k, ri + IW * (k * nmax + i), rj + JW * (k * nmax + j), v);
+          merged_pair<BZERO>(fr + FW * k, rec + RW * (k * nmax + i), rec + RW * (k * nmax + j) + 2, v);
 #pragma unroll
           for (int q = 0; q < 9; ++q) acc[q] += v[q];
         }
@@ -1243,10 +1236,9 @@ __global__ void to_float(int64_t n, const double* __restrict__ src, float* __res
 }
 
 // FP32 copies of grad / Hessian Phi for the FP32 pair phase (made once per assembler).
-// FP32 copies of grad / Hessian Phi and a copy of the neighbour ids, each followed by
-// kStagePad zero elements: the tangent stages a group's range of these arrays with bulk
-// copies whose ends are rounded out to 16 bytes, which may read up to 15 bytes past the
-// last entry.
+// FP32 copies of grad / Hessian Phi, each followed by kStagePad zero elements: the
+// tangent stages a group's range of these arrays with bulk copies whose ends are rounded
+// out to 16 bytes, which may read up to 15 bytes past the last entry.
 constexpr int kStagePad = 16;
 
 void ensure_fp32_shapes(cgb_assembler* a) {
@@ -1255,14 +1247,11 @@ void ensure_fp32_shapes(cgb_assembler* a) {
   cudaStream_t st = a->ctx->stream;
   a->dpsi32.alloc(2 * S->nnz + kStagePad);
   a->ddpsi32.alloc(3 * S->nnz + kStagePad);
-  a->idx_pad.alloc(S->nnz + kStagePad);
   CGB_CUDA(cudaMemsetAsync(a->dpsi32.p, 0, a->dpsi32.bytes(), st));
   CGB_CUDA(cudaMemsetAsync(a->ddpsi32.p, 0, a->ddpsi32.bytes(), st));
-  CGB_CUDA(cudaMemsetAsync(a->idx_pad.p, 0, a->idx_pad.bytes(), st));
   if (S->nnz) {
     to_float<<<nb(2 * S->nnz, 256), 256, 0, st>>>(2 * S->nnz, S->dpsi.p, a->dpsi32.p);
     to_float<<<nb(3 * S->nnz, 256), 256, 0, st>>>(3 * S->nnz, S->ddpsi.p, a->ddpsi32.p);
-    CGB_CUDA(cudaMemcpyAsync(a->idx_pad.p, S->nbr_idx.p, S->nnz * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
   }
   CGB_CUDA(cudaGetLastError());
 }
@@ -1468,12 +1457,12 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     };
     if (merged) {
       MergeArgs mg{a->mrg_ent_ptr.p, a->mrg_ent_slot.p, a->mrg_ent_cstart.p, a->mrg_direct.p, a->mrg_code.p,
-                   a->idx_pad.p, ctx->dev_err.p};
-      const int JW = bzero ? 5 : 7, IW = 3, FW = 3;  // record strides of the kernel
+                   ctx->dev_err.p};
+      const int RW = bzero ? 7 : 9, FW = 3;  // record and frame strides of the kernel (float4)
       const size_t E = static_cast<size_t>(kMG) * fa.nmax;
-      const size_t msm = (static_cast<size_t>(kState) * kMG + 4 * FW * kMG + 4 * static_cast<size_t>(IW + JW) * E) *
+      const size_t msm = (static_cast<size_t>(kState) * kMG + 4 * FW * kMG + 4 * static_cast<size_t>(RW) * E) *
                              sizeof(float) +
-                         E * sizeof(int) + (24 * E + 96);  // + the staging windows
+                         (20 * E + 64);  // + the staging windows
       if (msm > 220 * 1024) throw Error(CGB_ERR_CAPACITY, "assemble: neighbour lists too long for the merged tangent");
       auto kern = det ? (bzero ? face_tangent_merged_kernel<true, true> : face_tangent_merged_kernel<false, true>)
                       : (bzero ? face_tangent_merged_kernel<true, false> : face_tangent_merged_kernel<false, false>);

@@ -157,7 +157,6 @@ struct cgb_assembler {
   cgb::DevBuf<double> K;            // 9 n_blocks (device scratch for host-buffer calls)
   cgb::DevBuf<double> x;            // 3 n_nodes
   cgb::DevBuf<float> dpsi32, ddpsi32; // FP32 copies of the face shape derivatives (mixed mode)
-  cgb::DevBuf<int32_t> idx_pad;       // face neighbour ids, padded for the tangent's bulk copies
   // Merged contributions of the FP32 tangent: per group of 16 consecutive Gauss points the
   // distinct blocks ("entries", count-descending) and every pair's code in entry order.
   bool mrg_ready = false;
