@@ -233,24 +233,13 @@ def run_gpu(args):
 
     import curvami_gb300 as cg
 
+    from curvami_gb300.replicas import Replicas
+
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-
-    def max_over_ranks(v):
-        if world == 1:
-            return v
-        import torch.distributed as dist
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    reps = Replicas()
+    barrier = reps.barrier
+    max_over_ranks = reps.max
 
     plate, x = build_workload(args.n_side)
     ctx = cg.Context(local)
@@ -442,9 +431,7 @@ def run_gpu(args):
     }
     if rank == 0:
         print(json.dumps(line))
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    reps.close()
 
 
 # ---------------------------------------------------------------------------------
@@ -560,10 +547,13 @@ def run_batched(args):
     from curvami_gb300 import autotune as at
     from curvami_gb300 import synth
 
+    from curvami_gb300.replicas import Replicas
+
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
+    reps = Replicas()
     t0 = time.perf_counter()
-    plates, xs = synth.config_batched(args.plates, seed=BATCH_SEED + rank)
+    plates, xs = synth.config_batched(args.plates, seed=BATCH_SEED)   # the same batch on every rank
     gen_s = time.perf_counter() - t0
     ctx = cg.Context(local)
     t0 = time.perf_counter()
@@ -585,6 +575,7 @@ def run_batched(args):
         g = asm.graph(x_d.data_ptr(), K_d.data_ptr(), F_d.data_ptr(), flags)
         for _ in range(warmup):
             g.launch()
+        reps.barrier()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -593,8 +584,9 @@ def run_batched(args):
             g.launch()
         e1.record(stream)
         torch.cuda.synchronize()
+        reps.barrier()
         g.close()
-        return e0.elapsed_time(e1) / steps
+        return reps.max(e0.elapsed_time(e1) / steps)
 
     W = max(args.warmup, 3)
     with ClockSampler(local) as clk:
@@ -621,6 +613,7 @@ def run_batched(args):
     }
     if rank == 0:
         print(json.dumps(line))
+    reps.close()
 
 
 def main():
