@@ -150,6 +150,12 @@ int cgb_assembler_set_tuning(cgb_assembler* a, const cgb_tuning* t) {
   });
 }
 
+int cgb_test_stage_timeout(cgb_assembler* a, int on) {
+  if (!a) return CGB_ERR_INVALID;
+  a->test_stage_extra_tx = on ? 16u : 0u;
+  return CGB_OK;
+}
+
 int cgb_graph_create(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags, cgb_graph** out) {
   if (!a || !out) return CGB_ERR_INVALID;
   *out = nullptr;

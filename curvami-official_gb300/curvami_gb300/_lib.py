@@ -52,6 +52,7 @@ SIGNATURES = {
     "cgb_graph_create": (i32, [vp, vp, vp, vp, i32, vp]),
     "cgb_graph_launch": (i32, [vp]),
     "cgb_graph_destroy": (i32, [vp]),
+    "cgb_test_stage_timeout": (i32, [vp, i32]),
     "cgb_set_material": (i32, [vp, vp, vp, vp]),
     "cgb_assemble": (i32, [vp, vp, vp, vp, i32]),
     "cgb_assemble_device": (i32, [vp, vp, vp, vp, i32]),

@@ -233,6 +233,13 @@ int cgb_graph_create(cgb_assembler* a, const double* d_x, double* d_K, double* d
 int cgb_graph_launch(cgb_graph* g);
 int cgb_graph_destroy(cgb_graph* g);
 
+/* Failure-detection test hook (no reference counterpart): on != 0 makes every staging
+ * wait of the FP32 tangent expect 16 bytes that never arrive, so the bounded wait (about
+ * one second of SM clock per launch) gives up; the kernel leaves its remaining work undone
+ * and the next synchronising call returns CGB_ERR_DEVICE. No fault and no hang: the
+ * copies that were issued complete, only the expected count is never reached. */
+int cgb_test_stage_timeout(cgb_assembler* a, int on);
+
 /* ---- tracing (library extension; the reference only prints wall-clock times) ------ */
 /* CUDA events around every phase of cgb_assemble / cgb_assemble_device and of
  * cgb_shape_build, summed per phase until read. Off by default; costs two event records
