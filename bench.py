@@ -40,7 +40,7 @@ UNIT = "GP evals/s"
 SEED = 1003
 # DRAM bytes (read + write) per Gauss point of one face_tangent_merged_kernel launch, from
 # ncu on the 101 x 101 plate (profiles/face_tangent_merged_kernel_101.md).
-TANGENT_DRAM_BYTES_PER_GP = (85.99296e6 + 1.751552e6) / 40000
+TANGENT_DRAM_BYTES_PER_GP = (81.53728e6 + 1.746432e6) / 40000
 WORKLOAD = ("single-plate assembly at scale: 201x201 jittered nodes, 4x4 Gauss rule (640,000 "
             "Gauss points), quadratic RKPM, quartic window, rho = 3h, circular-arc crease R = 60 "
             "with elastic hinge Kt = 1e-3, seeded 8-mode Fourier displacement (rotations up to 60 "
