@@ -375,7 +375,7 @@ def run_gpu(args):
         "launch_ms": tan_ms / tan_launches, "launches_per_step": tan_launches,
         "algorithmic_bytes_per_launch": alg_bytes / tan_launches,
         "step_ms": tan_ms, "algorithmic_bytes_per_step": alg_bytes, "work": work,
-        "binding_unit": "L1 / shared-memory data pipe (ncu: 81% of peak; FMA pipe 42%)",
+        "binding_unit": "L1 / shared-memory data pipe (ncu: 82% of peak; FMA pipe 44%)",
         "pipes": {
             "fp32_tangent": {"achieved_tflops": flops_fp32 / (tan_ms * 1e-3) / 1e12, "peak_tflops": p32,
                              "frac": flops_fp32 / (tan_ms * 1e-3) / 1e12 / p32 if p32 > 0 else None,
