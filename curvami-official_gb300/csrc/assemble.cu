@@ -494,14 +494,22 @@ __global__ void __launch_bounds__(32 * kFaceWarps, sizeof(TK) == 4 ? 5 : 3) face
 // (phase 1, one Gauss point per thread, FP64 bound) writes the per-point state to
 // global memory ([field][n_gp]); the tangent kernel (phase 2) stages 32 points' states
 // in shared memory and runs the pair loop.
+// Work is handed out 32 points at a time from a counter (zeroed per assembly), so the
+// warps of a launch finish together whatever the grid: when the tangent kernel of the
+// previous chunk holds most of each SM, only one residual CTA fits beside it, and a
+// fixed split into CTAs would leave a partial last wave.
 template <typename TK, bool DET, bool STORE>
-__global__ void __launch_bounds__(256) face_residual_kernel(FaceArgs a, TK* gstate) {
+__global__ void __launch_bounds__(256) face_residual_kernel(FaceArgs a, TK* gstate, int* __restrict__ work) {
   const int lane = threadIdx.x & 31;
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t g = a.g_begin + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g - lane < a.g_end;
-       g += stride)
-    phase1_point<TK, DET>(a, static_cast<int>(g - lane), lane, STORE ? gstate : static_cast<TK*>(nullptr),
-                          a.n_gp, g);
+  for (;;) {
+    int unit = 0;
+    if (lane == 0) unit = atomicAdd(work, 1);
+    unit = __shfl_sync(0xffffffffu, unit, 0);
+    const int64_t g0 = a.g_begin + 32 * static_cast<int64_t>(unit);
+    if (g0 >= a.g_end) break;
+    phase1_point<TK, DET>(a, static_cast<int>(g0), lane, STORE ? gstate : static_cast<TK*>(nullptr), a.n_gp,
+                          g0 + lane);
+  }
 }
 
 constexpr int kTanWarps = 4;
@@ -1423,11 +1431,15 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   const int chunk = ((S->n_gp + n_chunks - 1) / n_chunks + 31) / 32 * 32;
   int nface = 0;
   const size_t tsm = static_cast<size_t>(kTanWarps) * ((kState * 32 + kRec * fa.nmax) * tk + fa.nmax * sizeof(int));
+  // Work counters of the chunks' residual launches.
+  a->work_ctr.ensure(kMaxChunks);
+  CGB_CUDA(cudaMemsetAsync(a->work_ctr.p, 0, kMaxChunks * sizeof(int), st));
   if (want_K) {
     CGB_CUDA(cudaEventRecord(a->ev_start, st));
     CGB_CUDA(cudaStreamWaitEvent(a->side, a->ev_start, 0));
   }
   for (int c = 0; c < n_chunks && S->n_gp > 0; ++c) {
+    int* work = a->work_ctr.p + c;
     fa.g_begin = c * chunk;
     fa.g_end = std::min(S->n_gp, (c + 1) * chunk);
     if (fa.g_begin >= fa.g_end) break;
@@ -1435,15 +1447,15 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     const unsigned rgrid = std::max(1u, std::min(nb(ncg, rthreads), static_cast<unsigned>(sms * 16 * (256 / rthreads))));
     prof_begin(ctx, CGB_PHASE_FACE);
     if (mixed) {
-      if (det) { if (want_K) face_residual_kernel<float, true, true><<<rgrid, rthreads, 0, st>>>(fa, st32);
-                 else face_residual_kernel<float, true, false><<<rgrid, rthreads, 0, st>>>(fa, st32); }
-      else { if (want_K) face_residual_kernel<float, false, true><<<rgrid, rthreads, 0, st>>>(fa, st32);
-             else face_residual_kernel<float, false, false><<<rgrid, rthreads, 0, st>>>(fa, st32); }
+      if (det) { if (want_K) face_residual_kernel<float, true, true><<<rgrid, rthreads, 0, st>>>(fa, st32, work);
+                 else face_residual_kernel<float, true, false><<<rgrid, rthreads, 0, st>>>(fa, st32, work); }
+      else { if (want_K) face_residual_kernel<float, false, true><<<rgrid, rthreads, 0, st>>>(fa, st32, work);
+             else face_residual_kernel<float, false, false><<<rgrid, rthreads, 0, st>>>(fa, st32, work); }
     } else {
-      if (det) { if (want_K) face_residual_kernel<double, true, true><<<rgrid, rthreads, 0, st>>>(fa, st64);
-                 else face_residual_kernel<double, true, false><<<rgrid, rthreads, 0, st>>>(fa, st64); }
-      else { if (want_K) face_residual_kernel<double, false, true><<<rgrid, rthreads, 0, st>>>(fa, st64);
-             else face_residual_kernel<double, false, false><<<rgrid, rthreads, 0, st>>>(fa, st64); }
+      if (det) { if (want_K) face_residual_kernel<double, true, true><<<rgrid, rthreads, 0, st>>>(fa, st64, work);
+                 else face_residual_kernel<double, true, false><<<rgrid, rthreads, 0, st>>>(fa, st64, work); }
+      else { if (want_K) face_residual_kernel<double, false, true><<<rgrid, rthreads, 0, st>>>(fa, st64, work);
+             else face_residual_kernel<double, false, false><<<rgrid, rthreads, 0, st>>>(fa, st64, work); }
     }
     ++nface;
     prof_end(ctx, CGB_PHASE_FACE, 1);

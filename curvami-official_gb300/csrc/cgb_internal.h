@@ -166,6 +166,7 @@ struct cgb_assembler {
   cgb::DevBuf<int8_t> mrg_direct;     // 1: group too large, scatter directly
   cgb::DevBuf<uint16_t> mrg_code;     // per pair: point | i | j, grouped by entry
   cgb_tuning tuning{};                // launch shape (0 = library default)
+  cgb::DevBuf<int> work_ctr;          // per-chunk work counters of the residual kernel
   uint32_t test_stage_extra_tx = 0;   // failure-detection test only: bytes the staging never gets
   int n_graphs = 0;                   // live cgb_graph objects on this assembler
   int64_t mrg_n_ent = 0;              // entries over all groups
