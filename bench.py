@@ -412,6 +412,7 @@ def run_gpu(args):
                    "l2": "inputs larger than L2 every step (grad/Hessian Phi 0.73 GB + slot map 1.0 GB)",
                    "setup_s": setup_s,
                    "launch_shape": {"mixed": list(tune_mix["tuning"]), "fp64": list(tune_f64["tuning"]),
+                                    "mixed_tried_ms": tune_mix["tried"], "fp64_tried_ms": tune_f64["tried"],
                                     "note": "(chunks, residual threads, tangent CTAs/SM; 0 = default) "
                                             "picked by curvami_gb300/autotune.py on this problem"}},
         "fp64": {"value": v_f64, "ms_per_step": ms_f64, "mixed_over_fp64": ms_f64 / ms_mix,

@@ -144,8 +144,8 @@ int cgb_assembler_set_tuning(cgb_assembler* a, const cgb_tuning* t) {
     if (t->residual_threads != 0 && t->residual_threads != 64 && t->residual_threads != 128 &&
         t->residual_threads != 256)
       throw Error(CGB_ERR_INVALID, "cgb_assembler_set_tuning: residual_threads must be 0, 64, 128 or 256");
-    if (t->tangent_ctas_per_sm < 0 || t->tangent_ctas_per_sm > 3)
-      throw Error(CGB_ERR_INVALID, "cgb_assembler_set_tuning: tangent_ctas_per_sm must be 0..3");
+    if (t->tangent_ctas_per_sm < 0 || t->tangent_ctas_per_sm > 4)
+      throw Error(CGB_ERR_INVALID, "cgb_assembler_set_tuning: tangent_ctas_per_sm must be 0..4");
     a->tuning = *t;
   });
 }

@@ -49,15 +49,19 @@ def _load(path):
 
 
 def _time(asm, d_x, d_K, d_F, flags, repeats):
+    """Seconds per assembly in steady state: `repeats` back-to-back calls (as a Newton loop
+    or the benchmark issues them, so one call's tail overlaps the next one's start) between
+    two synchronisations; the best of three such runs."""
     ctx = asm.ctx
     asm.assemble_device(d_x, d_K, d_F, flags)        # warm-up (and any first-call set-up)
     ctx.synchronize()
     best = float("inf")
-    for _ in range(repeats):
+    for _ in range(3):
         t0 = time.perf_counter()
-        asm.assemble_device(d_x, d_K, d_F, flags)
+        for _ in range(repeats):
+            asm.assemble_device(d_x, d_K, d_F, flags)
         ctx.synchronize()
-        best = min(best, time.perf_counter() - t0)
+        best = min(best, (time.perf_counter() - t0) / repeats)
     return best
 
 

@@ -215,7 +215,7 @@ int cgb_shape_concat(cgb_context* ctx, const cgb_shape* const* sets, const int32
 /* Launch shape of an assembly; 0 keeps the library's choice. n_chunks (1..16): Gauss-point
  * chunks whose residual and tangent kernels overlap on two streams (default 4 from 65,536
  * points, else 1); residual_threads (64, 128, 256): block size of the residual kernel
- * (default 256); tangent_ctas_per_sm (1..3): resident CTAs per SM of the merged FP32
+ * (default 256); tangent_ctas_per_sm (1..4): resident CTAs per SM of the merged FP32
  * tangent (default: as many as fit). */
 typedef struct cgb_tuning {
   int n_chunks;
