@@ -306,6 +306,37 @@ def abd_isotropic(E: float, nu: float, h: float):
     return Q * (z1 - z0), 0.5 * Q * (z1 * z1 - z0 * z0), (1.0 / 3.0) * Q * (z1 ** 3 - z0 ** 3)
 
 
+def abd_laminate(plies):
+    """A, B, D of a laminate by classical lamination theory (Constitutive::computeABD,
+    plate/Constitutive.h:10-50): plies = [(E1, E2, nu12, G12, angle_deg, thickness), ...]
+    from the bottom face up, the mid-plane at half the total thickness. Each ply's reduced
+    stiffness Q is rotated to Q-bar by the ply angle and integrated through its thickness
+    (A: 1, B: z, D: z^2). An unsymmetric layup gives B != 0 (membrane-bending coupling)."""
+    h = float(sum(p[5] for p in plies))
+    z = -h / 2.0
+    A = np.zeros((3, 3)); B = np.zeros((3, 3)); D = np.zeros((3, 3))
+    for E1, E2, nu12, G12, angle, t in plies:
+        nu21 = (E2 / E1) * nu12
+        den = 1.0 - nu12 * nu21
+        Q11, Q22, Q12, Q66 = E1 / den, E2 / den, nu12 * E2 / den, G12
+        th = np.deg2rad(angle)
+        m, n = np.cos(th), np.sin(th)
+        m2, n2 = m * m, n * n
+        Qb = np.empty((3, 3))
+        Qb[0, 0] = Q11 * m2 * m2 + 2.0 * (Q12 + 2.0 * Q66) * m2 * n2 + Q22 * n2 * n2
+        Qb[1, 1] = Q11 * n2 * n2 + 2.0 * (Q12 + 2.0 * Q66) * m2 * n2 + Q22 * m2 * m2
+        Qb[0, 1] = Qb[1, 0] = (Q11 + Q22 - 4.0 * Q66) * m2 * n2 + Q12 * (m2 * m2 + n2 * n2)
+        Qb[0, 2] = Qb[2, 0] = (Q11 - Q12 - 2.0 * Q66) * n * m * m2 + (Q12 - Q22 + 2.0 * Q66) * n2 * n * m
+        Qb[1, 2] = Qb[2, 1] = (Q11 - Q12 - 2.0 * Q66) * m * n * n2 + (Q12 - Q22 + 2.0 * Q66) * m2 * m * n
+        Qb[2, 2] = (Q11 + Q22 - 2.0 * Q12 - 2.0 * Q66) * m2 * n2 + Q66 * (m2 * m2 + n2 * n2)
+        z1 = z + t
+        A += Qb * (z1 - z)
+        B += 0.5 * Qb * (z1 * z1 - z * z)
+        D += (1.0 / 3.0) * Qb * (z1 ** 3 - z ** 3)
+        z = z1
+    return A, B, D
+
+
 class PlateModel:
     """A synthetic plate (synth.Plate) on the GPU: shape functions of the faces and of
     every fold side, the assembler with the hinge union pattern and the material."""

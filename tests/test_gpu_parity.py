@@ -241,6 +241,28 @@ def test_deterministic_bitwise(ctx, arc_case):
         assert np.array_equal(K1, K3) and np.array_equal(F1, F3)
 
 
+def test_assembly_with_coupling(ctx, arc_case):
+    """B != 0 (an unsymmetric [0/45] layup): the general P = A Bm + B Bb, Q = B Bm + D Bb
+    path of every tangent kernel (FP64, FP32 merged, deterministic) against the oracle."""
+    c = arc_case
+    A, B, D = cg.abd_laminate([(1.0, 0.6, 0.25, 0.3, 0.0, 0.02), (1.4, 0.9, 0.3, 0.45, 45.0, 0.03)])
+    assert np.abs(B).max() > 0
+    ctx.set_nodes(c.p.node_xy)
+    asm = cg.NonLinearAssembler(ctx, c.faces_o, c.p.faces.weight, c.model.fold_specs)
+    asm.set_material(A, B, D)
+    r = c.ref
+    Ko, Fo = c.o.update_stiffness(c.p.n_nodes, c.p.faces.weight, r["ptr"], r["idx"], r["dpsi"], r["ddpsi"],
+                                  c.outer, c.mp, c.x, A, B, D)
+    Ko, Fo = c.o.hinge(c.p.n_nodes, c.x, c.folds, c.outer, c.col_ptr, c.col_nodes, Ko, Fo)
+    for fl, tolK in ((0, 1e-13), (cg.DETERMINISTIC, 1e-13), (cg.MIXED, 1e-5), (cg.MIXED | cg.DETERMINISTIC, 1e-5)):
+        K, F = asm.assemble(c.x, cg.TANGENT | cg.HINGE | fl)
+        assert rel(F, Fo) < 1e-12, fl
+        assert rel(K, Ko) < tolK, fl
+    K1, F1 = asm.assemble(c.x, cg.TANGENT | cg.HINGE | cg.MIXED | cg.DETERMINISTIC)
+    K2, F2 = asm.assemble(c.x, cg.TANGENT | cg.HINGE | cg.MIXED | cg.DETERMINISTIC)
+    assert np.array_equal(K1, K2) and np.array_equal(F1, F2)
+
+
 def test_assembler_stats(arc_case):
     c = arc_case
     n = np.diff(c.ref["ptr"])

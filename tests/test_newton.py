@@ -51,6 +51,28 @@ def test_constraint_rows(o):
     assert np.allclose(J[0].toarray()[0, 0::3], prob.edges[0][1].P[0].toarray()[0])
 
 
+def test_rigid_folds_hold_their_angle(o):
+    """flagRig: no hinge force, a fold-angle row per crease point (Constraints.h:280-304);
+    the converged state keeps every crease point at its rest angle."""
+    p = small_plate(9)
+    prob = oracle_problem(o, p, (0.0, 0.0, 3e-10), clamped_left_edge(p))
+    prob.flag_rig = True
+    c0, J0 = prob.constraints(np.zeros(prob.num_dofs()))
+    n_edge, n_crease = len(prob.edges[0][0].xy), len(p.folds[0].left.xy)
+    assert J0.shape[0] == 4 * n_edge + 4 * n_crease      # u, v, w, slope; 3 ties + 1 angle
+    states, iters = S.load_steps(S.ContinuationSolver(**TOL), prob, [0.5, 1.0])
+    x = states[-1]
+    c, J = prob.constraints(x)
+    assert np.abs(c).max() < 1e-12
+    # the rows are consistent: J is the derivative of c (central differences)
+    rng = np.random.default_rng(3)
+    v = rng.standard_normal(prob.num_dofs()) * 1e-3
+    cp, _ = prob.constraints(x + 1e-6 * v)
+    cm, _ = prob.constraints(x - 1e-6 * v)
+    assert np.abs((cp - cm) / 2e-6 - J @ v).max() < 1e-7 * max(1.0, np.abs(J @ v).max())
+    assert np.abs(x[2::3]).max() > 0
+
+
 def test_line_search_converges_and_is_linear_at_small_load(o):
     p = small_plate(9)
     edge = clamped_left_edge(p)

@@ -157,7 +157,7 @@ def test_singular_support_detected(o):
 
 # ---- assembly (plate/Assembly.h, Constraints.h, Meshless.h) ---------------------------
 
-def assemble_case(o, p, x, exact=False):
+def assemble_case(o, p, x, exact=False, abd=None):
     sh = shapes(o, p)
     folds = []
     for f in p.folds:
@@ -168,7 +168,7 @@ def assemble_case(o, p, x, exact=False):
         folds.append({"left": side["left"], "right": side["right"], "weight": f.left.weight,
                       "tangent": f.left.tangent, "Kt": f.Kt, "theta0": f.theta0})
     outer, inner, col_ptr, col_nodes, mp = o.pattern(p.n_nodes, sh["ptr"], sh["idx"], folds)
-    A, B, D = o.abd(p.E, p.nu, p.thickness)
+    A, B, D = o.abd(p.E, p.nu, p.thickness) if abd is None else abd
 
     def F_K(x, want_K=True, hinge=True):
         K, F = o.update_stiffness(p.n_nodes, p.faces.weight, sh["ptr"], sh["idx"], sh["dpsi"], sh["ddpsi"],
@@ -220,6 +220,44 @@ def test_tangent_check(o, case, exact):
         fd = (Fp - Fm) / (2 * h)
         worst = max(worst, np.linalg.norm(fd - Ks @ v) / np.linalg.norm(fd))
     assert worst < 1e-6  # the reference's CONSISTENT verdict
+
+
+UNSYMMETRIC = [(1.0, 0.6, 0.25, 0.3, 0.0, 0.02), (1.4, 0.9, 0.3, 0.45, 45.0, 0.03)]
+
+
+def test_laminate_abd():
+    import curvami_gb300 as cg
+
+    # one isotropic ply: the single-ply formula, B = 0
+    A, B, D = cg.abd_laminate([(1.0, 1.0, 0.3, 1.0 / 2.6, 30.0, 0.05)])
+    A0, B0, D0 = cg.abd_isotropic(1.0, 0.3, 0.05)
+    assert np.allclose(A, A0, rtol=1e-13, atol=1e-16) and np.allclose(D, D0, rtol=1e-13, atol=1e-18)
+    assert np.abs(B).max() < 1e-18
+    # [0 / 45] of different plies: membrane-bending coupling and shear-extension terms
+    A, B, D = cg.abd_laminate(UNSYMMETRIC)
+    assert np.abs(B).max() > 1e-4 * np.abs(A).max() * 0.05 and abs(A[0, 2]) > 0
+    assert np.allclose(A, A.T) and np.allclose(B, B.T) and np.allclose(D, D.T)
+    assert np.all(np.linalg.eigvalsh(np.block([[A, B], [B, D]])) > 0)
+
+
+def test_tangent_check_with_coupling(o, case):
+    """TangentCheck with B != 0 (an unsymmetric [0/45] layup)."""
+    import curvami_gb300 as cg
+
+    p, x = case
+    C = assemble_case(o, p, x, abd=cg.abd_laminate(UNSYMMETRIC))
+    n = 3 * p.n_nodes
+    K, F = C["F_K"](x, hinge=False)
+    Ks, _ = full_upper(K, C["inner"], C["outer"], n)
+    rng = np.random.default_rng(99)
+    h = 1e-6 * max(1.0, abs(x).max())
+    for _ in range(3):
+        v = rng.uniform(-1, 1, n)
+        v /= np.linalg.norm(v)
+        _, Fp = C["F_K"](x + h * v, want_K=False, hinge=False)
+        _, Fm = C["F_K"](x - h * v, want_K=False, hinge=False)
+        fd = (Fp - Fm) / (2 * h)
+        assert np.linalg.norm(fd - Ks @ v) / np.linalg.norm(fd) < 1e-6
 
 
 def test_residual_is_energy_gradient(o, case):
