@@ -84,12 +84,14 @@ __global__ void node_side_kernel(int n_nodes, const double* __restrict__ node_xy
 }
 
 // Gauss-point indicators, 6 doubles per point per crease.
-__global__ void gp_indicator_kernel(int n_gp, const double* __restrict__ gp_xy, DevCrease cr,
+// Crease c's indicator at every Gauss point, written in place into the [g][crease][6]
+// layout the RKPM kernel reads (n_creases values per point).
+__global__ void gp_indicator_kernel(int n_gp, const double* __restrict__ gp_xy, DevCrease cr, int c, int n_creases,
                                     double* __restrict__ out) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n_gp) return;
   const DevIndicator I = eval_indicator(gp_xy[2 * g], gp_xy[2 * g + 1], cr);
-  double* o = out + 6 * static_cast<int64_t>(g);
+  double* o = out + 6 * (static_cast<int64_t>(g) * n_creases + c);
   o[0] = I.f; o[1] = I.gx; o[2] = I.gy; o[3] = I.hxx; o[4] = I.hyy; o[5] = I.hxy;
 }
 
@@ -636,21 +638,10 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
     node_side_kernel<<<blocks_for(n_nodes), kThreads, 0, st>>>(n_nodes, ctx->node_xy.p, dcr[c],
                                                                  side.p + static_cast<int64_t>(c) * n_nodes);
   }
-  // Gauss-point indicators laid out [g][c][6]: computed per crease into a temporary,
-  // then interleaved.
-  if (nc > 0 && n_gp > 0) {
-    DevBuf<double> tmp(static_cast<size_t>(6) * n_gp);
-    std::vector<double> h_all(static_cast<size_t>(6) * nc * n_gp), h_one(static_cast<size_t>(6) * n_gp);
-    for (int c = 0; c < nc; ++c) {
-      gp_indicator_kernel<<<blocks_for(n_gp), kThreads, 0, st>>>(n_gp, out->gp_xy.p, dcr[c], tmp.p);
-      CGB_CUDA(cudaMemcpyAsync(h_one.data(), tmp.p, tmp.bytes(), cudaMemcpyDeviceToHost, st));
-      CGB_CUDA(cudaStreamSynchronize(st));
-      for (int g = 0; g < n_gp; ++g)
-        std::memcpy(&h_all[(static_cast<size_t>(g) * nc + c) * 6], &h_one[static_cast<size_t>(g) * 6],
-                    6 * sizeof(double));
-    }
-    CGB_CUDA(cudaMemcpyAsync(gind.p, h_all.data(), h_all.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-  }
+  // Gauss-point indicators laid out [g][c][6].
+  if (nc > 0 && n_gp > 0)
+    for (int c = 0; c < nc; ++c)
+      gp_indicator_kernel<<<blocks_for(n_gp), kThreads, 0, st>>>(n_gp, out->gp_xy.p, dcr[c], c, nc, gind.p);
   prof_end(ctx, CGB_PHASE_CREASE, nc * (1 + (n_gp > 0 ? 1 : 0)));
   CGB_CUDA(cudaGetLastError());
 

@@ -60,6 +60,8 @@ SHAPE_CASES = {
     "nocrease_order3": lambda: synth.square_plate(15, 0.5, 3, jitter=0.05, crease=None, order=3,
                                                   rho_factor=4.5, seed=3),
     "cubic_bspline": lambda: synth.square_plate(15, 0.5, 4, jitter=0.05, crease="row", kernel=1, seed=4),
+    "three_arcs": lambda: synth.batched_plate(31, np.random.default_rng(6)),
+    "three_cuts": lambda: synth.batched_plate(31, np.random.default_rng(7)),
 }
 
 

@@ -90,3 +90,22 @@ def test_reference_example_mesh():
     assert len(q["face"][0]) > 0 and len(q["active"]) > 0
     c = mesh.extract_curve(els, xy, [5])
     assert c is not None and len(c["vertices"]) >= 2 and c["dropped"] == 0
+
+
+def test_triangle_rules():
+    # two triangles splitting the unit square: weights sum to the area, 1- and 3-point rules
+    xy = np.array([[0.0, 0.0], [1.0, 0.0], [1.0, 1.0], [0.0, 1.0]])
+    els = [mesh.Element(2, 1, (0, 1, 2)), mesh.Element(2, 1, (0, 2, 3))]
+    for degree, per in ((1, 1), (3, 3)):
+        fxy, fw, _ = mesh.quadrature(xy, els, face_degree=degree)["face"]
+        assert len(fxy) == 2 * per and np.isclose(fw.sum(), 1.0)
+        # the rules integrate x exactly: int_0^1 int_0^1 x = 1/2
+        assert np.isclose((fw * fxy[:, 0]).sum(), 0.5)
+    fxy, fw, _ = mesh.quadrature(xy, els, face_degree=3)["face"]
+    assert np.isclose((fw * fxy[:, 0] * fxy[:, 1]).sum(), 0.25)   # degree 2 exact
+
+
+def test_clockwise_quad_has_positive_weights():
+    xy = np.array([[0.0, 0.0], [0.0, 1.0], [1.0, 1.0], [1.0, 0.0]])   # clockwise
+    fxy, fw, _ = mesh.quadrature(xy, [mesh.Element(3, 1, (0, 1, 2, 3))], face_degree=2)["face"]
+    assert np.all(fw > 0) and np.isclose(fw.sum(), 1.0)
