@@ -324,21 +324,24 @@ __global__ void __launch_bounds__(kThreads) rkpm_kernel(RkpmArgs a) {
     }
   }
 
-  // Leading 3x3 inverse with derivatives and the residual guard (GlobalRKPM.h:203-239).
-  double Iv[NM], Ix[NM], Iy[NM], Ixx[NM], Iyy[NM], Ixy[NM];
-#pragma unroll
-  for (int k = 0; k < NM; ++k) { Iv[k] = 0; Ix[k] = 0; Iy[k] = 0; Ixx[k] = 0; Iyy[k] = 0; Ixy[k] = 0; }
+  // The reference inverts M by blocks (GlobalRKPM.h:197-345): the leading 3x3 block with
+  // a residual guard, then one bordering step per further basis function with a Schur-pivot
+  // guard, carrying the five derivative jets of the whole inverse along. The shape
+  // functions only use row 0 of M^-1 and its jets, i.e. b = M^-1 e0 and
+  //   b_x = -M^-1 (M_x b),  b_xx = -M^-1 (M_xx b + 2 M_x b_x),
+  //   b_xy = -M^-1 (M_xy b + M_x b_y + M_y b_x)   (y alike),
+  // so M is factored once (LDL^T, no pivoting: M is symmetric positive semi-definite) and
+  // six solves give b and its jets - about a quarter of the FP64 work of the full inverse
+  // jets. The guards are evaluated as the reference does: the 3x3 residual test on the
+  // leading block, and the pivot test on the Schur complements, which are the LDL^T pivots
+  // d_k for k >= 3.
   int bad = 0;
   {
-    double m3[3][3], dx3[3][3], dy3[3][3], dxx3[3][3], dyy3[3][3], dxy3[3][3];
+    double m3[3][3];
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const int k = PI::k(r, c);
-        m3[r][c] = M[k]; dx3[r][c] = Mx[k]; dy3[r][c] = My[k];
-        dxx3[r][c] = Mxx[k]; dyy3[r][c] = Myy[k]; dxy3[r][c] = Mxy[k];
-      }
+      for (int c = 0; c < 3; ++c) m3[r][c] = M[PI::k(r, c)];
     double inv[3][3], chk[3][3];
     inv3(m3, inv);
     mm3(m3, inv, chk);
@@ -352,154 +355,61 @@ __global__ void __launch_bounds__(kThreads) rkpm_kernel(RkpmArgs a) {
         res = fmax(res, fabs(chk[r][c] - (r == c ? 1.0 : 0.0)));
       }
     if (!finite || res > 1e-8) bad = 1;
-    double ninv[3][3], t1[3][3], t2[3][3], invx[3][3], invy[3][3], invxx[3][3], invyy[3][3], invxy[3][3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) ninv[r][c] = -inv[r][c];
-    mm3(ninv, dx3, t1); mm3(t1, inv, invx);
-    mm3(ninv, dy3, t1); mm3(t1, inv, invy);
-    {
-      double a2[3][3], in[3][3];
-#pragma unroll
-      for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) a2[r][c] = 2.0 * dx3[r][c];
-      mm3(a2, inv, t1); mm3(t1, dx3, t2);
-#pragma unroll
-      for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) in[r][c] = t2[r][c] - dxx3[r][c];
-      mm3(inv, in, t1); mm3(t1, inv, invxx);
-#pragma unroll
-      for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) a2[r][c] = 2.0 * dy3[r][c];
-      mm3(a2, inv, t1); mm3(t1, dy3, t2);
-#pragma unroll
-      for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) in[r][c] = t2[r][c] - dyy3[r][c];
-      mm3(inv, in, t1); mm3(t1, inv, invyy);
-      double q1[3][3], q2[3][3];
-      mm3(dx3, inv, t1); mm3(t1, dy3, q1);
-      mm3(dy3, inv, t1); mm3(t1, dx3, q2);
-#pragma unroll
-      for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) in[r][c] = q1[r][c] + q2[r][c] - dxy3[r][c];
-      mm3(inv, in, t1); mm3(t1, inv, invxy);
-    }
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = r; c < 3; ++c) {
-        const int k = PI::k(r, c);
-        Iv[k] = inv[r][c]; Ix[k] = invx[r][c]; Iy[k] = invy[r][c];
-        Ixx[k] = invxx[r][c]; Iyy[k] = invyy[r][c]; Ixy[k] = invxy[r][c];
-      }
   }
-
-  // Bordered (Schur) inversion for np > 3 (GlobalRKPM.h:259-345).
+  // LDL^T of M: L unit lower (packed like M, strictly lower part used), D diagonal.
+  double Lf[NP][NP], Dg[NP], iD[NP];
 #pragma unroll
-  for (int it = 3; it < NP; ++it) {
-    double b[NP], bx[NP], by[NP], bxx[NP], byy[NP], bxy[NP];
-    double v[NP], vx[NP], vy[NP], vxx[NP], vyy[NP], vxy[NP];
+  for (int j = 0; j < NP; ++j) {
+    double d = M[PI::k(j, j)];
 #pragma unroll
-    for (int j = 0; j < it; ++j) {
-      const int k = PI::k(j, it);
-      b[j] = M[k]; bx[j] = Mx[k]; by[j] = My[k]; bxx[j] = Mxx[k]; byy[j] = Myy[k]; bxy[j] = Mxy[k];
+    for (int q = 0; q < j; ++q) d -= Lf[j][q] * Lf[j][q] * Dg[q];
+    Dg[j] = d;
+    iD[j] = 1.0 / d;
+    if (j >= 3 && !(fabs(d) > 1e-12 * fmax(fabs(M[PI::k(j, j)]), 1.0)) && bad == 0) bad = 2;
+#pragma unroll
+    for (int i = j + 1; i < NP; ++i) {
+      double v = M[PI::k(i, j)];
+#pragma unroll
+      for (int q = 0; q < j; ++q) v -= Lf[i][q] * Lf[j][q] * Dg[q];
+      Lf[i][j] = v * iD[j];
     }
-#pragma unroll
-    for (int r = 0; r < it; ++r) {
-      double aIb = 0, daxb = 0, aIdbx = 0, dayb = 0, aIdby = 0;
-      double d2xxb = 0, daxdbx = 0, aId2bxx = 0, d2yyb = 0, daydby = 0, aId2byy = 0;
-      double d2xyb = 0, daxdby = 0, daydbx = 0, aId2bxy = 0;
-#pragma unroll
-      for (int c = 0; c < it; ++c) {
-        const int k = PI::k(r, c);
-        aIb += Iv[k] * b[c];
-        daxb += Ix[k] * b[c]; aIdbx += Iv[k] * bx[c];
-        dayb += Iy[k] * b[c]; aIdby += Iv[k] * by[c];
-        d2xxb += Ixx[k] * b[c]; daxdbx += Ix[k] * bx[c]; aId2bxx += Iv[k] * bxx[c];
-        d2yyb += Iyy[k] * b[c]; daydby += Iy[k] * by[c]; aId2byy += Iv[k] * byy[c];
-        d2xyb += Ixy[k] * b[c]; daxdby += Ix[k] * by[c]; daydbx += Iy[k] * bx[c]; aId2bxy += Iv[k] * bxy[c];
-      }
-      v[r] = aIb;
-      vx[r] = daxb + aIdbx;
-      vy[r] = dayb + aIdby;
-      vxx[r] = d2xxb + 2.0 * daxdbx + aId2bxx;
-      vyy[r] = d2yyb + 2.0 * daydby + aId2byy;
-      vxy[r] = d2xyb + daxdby + daydbx + aId2bxy;
-    }
-    double d_bv = 0, d_bxv = 0, d_bvx = 0, d_byv = 0, d_bvy = 0;
-    double d_bxxv = 0, d_bxvx = 0, d_bvxx = 0, d_byyv = 0, d_byvy = 0, d_bvyy = 0;
-    double d_bxyv = 0, d_bxvy = 0, d_byvx = 0, d_bvxy = 0;
-#pragma unroll
-    for (int j = 0; j < it; ++j) {
-      d_bv += b[j] * v[j];
-      d_bxv += bx[j] * v[j]; d_bvx += b[j] * vx[j];
-      d_byv += by[j] * v[j]; d_bvy += b[j] * vy[j];
-      d_bxxv += bxx[j] * v[j]; d_bxvx += bx[j] * vx[j]; d_bvxx += b[j] * vxx[j];
-      d_byyv += byy[j] * v[j]; d_byvy += by[j] * vy[j]; d_bvyy += b[j] * vyy[j];
-      d_bxyv += bxy[j] * v[j]; d_bxvy += bx[j] * vy[j]; d_byvx += by[j] * vx[j]; d_bvxy += b[j] * vxy[j];
-    }
-    const int kii = PI::k(it, it);
-    const double q = M[kii] - d_bv;
-    const double qx = Mx[kii] - (d_bxv + d_bvx);
-    const double qy = My[kii] - (d_byv + d_bvy);
-    const double qxx = Mxx[kii] - (d_bxxv + 2.0 * d_bxvx + d_bvxx);
-    const double qyy = Myy[kii] - (d_byyv + 2.0 * d_byvy + d_bvyy);
-    const double qxy = Mxy[kii] - (d_bxyv + d_bxvy + d_byvx + d_bvxy);
-    // A point already flagged singular keeps that flag: the reference throws on the
-    // singular set before it reaches the bordering.
-    if (!(fabs(q) > 1e-12 * fmax(fabs(M[kii]), 1.0)) && bad == 0) bad = 2;
-    const double iQ = 1.0 / q, iQ2 = iQ * iQ, iQ3 = iQ2 * iQ;
-#pragma unroll
-    for (int r = 0; r < it; ++r) {
-#pragma unroll
-      for (int c = r; c < it; ++c) {
-        const int k = PI::k(r, c);
-        Iv[k] += v[r] * v[c] * iQ;
-        Ix[k] += (vx[r] * v[c] + v[r] * vx[c]) * iQ - v[r] * v[c] * qx * iQ2;
-        Iy[k] += (vy[r] * v[c] + v[r] * vy[c]) * iQ - v[r] * v[c] * qy * iQ2;
-        Ixx[k] += (vxx[r] * v[c] + 2.0 * vx[r] * vx[c] + v[r] * vxx[c]) * iQ -
-                  (vx[r] * v[c] + v[r] * vx[c]) * qx * iQ2 * 2.0 +
-                  v[r] * v[c] * (2.0 * qx * qx * iQ3 - qxx * iQ2);
-        Iyy[k] += (vyy[r] * v[c] + 2.0 * vy[r] * vy[c] + v[r] * vyy[c]) * iQ -
-                  (vy[r] * v[c] + v[r] * vy[c]) * qy * iQ2 * 2.0 +
-                  v[r] * v[c] * (2.0 * qy * qy * iQ3 - qyy * iQ2);
-        Ixy[k] += (vxy[r] * v[c] + vx[r] * vy[c] + vy[r] * vx[c] + v[r] * vxy[c]) * iQ -
-                  (vx[r] * v[c] + v[r] * vx[c]) * qy * iQ2 - (vy[r] * v[c] + v[r] * vy[c]) * qx * iQ2 +
-                  v[r] * v[c] * (2.0 * qx * qy * iQ3 - qxy * iQ2);
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < it; ++j) {
-      const int k = PI::k(j, it);
-      Iv[k] = -v[j] * iQ;
-      Ix[k] = -vx[j] * iQ + v[j] * qx * iQ2;
-      Iy[k] = -vy[j] * iQ + v[j] * qy * iQ2;
-      Ixx[k] = -vxx[j] * iQ + 2.0 * vx[j] * qx * iQ2 + v[j] * (qxx * iQ2 - 2.0 * qx * qx * iQ3);
-      Iyy[k] = -vyy[j] * iQ + 2.0 * vy[j] * qy * iQ2 + v[j] * (qyy * iQ2 - 2.0 * qy * qy * iQ3);
-      Ixy[k] = -vxy[j] * iQ + vx[j] * qy * iQ2 + vy[j] * qx * iQ2 + v[j] * (qxy * iQ2 - 2.0 * qx * qy * iQ3);
-    }
-    Iv[kii] = iQ;
-    Ix[kii] = -qx * iQ2;
-    Iy[kii] = -qy * iQ2;
-    Ixx[kii] = 2.0 * qx * qx * iQ3 - qxx * iQ2;
-    Iyy[kii] = 2.0 * qy * qy * iQ3 - qyy * iQ2;
-    Ixy[kii] = 2.0 * qx * qy * iQ3 - qxy * iQ2;
   }
   a.bad[g] = static_cast<int8_t>(bad);
-
-  // Row 0 of the inverse and its jets (the only part the shape functions use).
+  // x <- M^-1 x in place.
+  auto solve = [&](double* x) {
+#pragma unroll
+    for (int i = 1; i < NP; ++i)
+#pragma unroll
+      for (int q = 0; q < i; ++q) x[i] -= Lf[i][q] * x[q];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) x[i] *= iD[i];
+#pragma unroll
+    for (int i = NP - 2; i >= 0; --i)
+#pragma unroll
+      for (int q = i + 1; q < NP; ++q) x[i] -= Lf[q][i] * x[q];
+  };
+  // y += alpha * S x for a packed symmetric S.
+  auto symv = [&](const double* S, const double* x, double alpha, double* y) {
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      double t = 0.0;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) t += S[PI::k(i, q)] * x[q];
+      y[i] += alpha * t;
+    }
+  };
   double c0[NP], c0x[NP], c0y[NP], c0xx[NP], c0yy[NP], c0xy[NP];
 #pragma unroll
-  for (int jp = 0; jp < NP; ++jp) {
-    const int k = PI::k(0, jp);
-    c0[jp] = Iv[k]; c0x[jp] = Ix[k]; c0y[jp] = Iy[k]; c0xx[jp] = Ixx[k]; c0yy[jp] = Iyy[k]; c0xy[jp] = Ixy[k];
+  for (int i = 0; i < NP; ++i) {
+    c0[i] = i == 0 ? 1.0 : 0.0;
+    c0x[i] = 0.0; c0y[i] = 0.0; c0xx[i] = 0.0; c0yy[i] = 0.0; c0xy[i] = 0.0;
   }
+  solve(c0);
+  symv(Mx, c0, -1.0, c0x); solve(c0x);
+  symv(My, c0, -1.0, c0y); solve(c0y);
+  symv(Mxx, c0, -1.0, c0xx); symv(Mx, c0x, -2.0, c0xx); solve(c0xx);
+  symv(Myy, c0, -1.0, c0yy); symv(My, c0y, -2.0, c0yy); solve(c0yy);
+  symv(Mxy, c0, -1.0, c0xy); symv(Mx, c0y, -1.0, c0xy); symv(My, c0x, -1.0, c0xy); solve(c0xy);
   // Shape functions (GlobalRKPM.h:363-396).
   const double rho2 = a.rho * a.rho;
   for (int64_t e = p0; e < p1; ++e) {
