@@ -495,6 +495,25 @@ def shape_stage(cg, ctx, args, with_cpu):
     d = sh.download()
     nnz = int(d["ptr"][-1])
     n = np.diff(d["ptr"])
+    # Progressive creasing's per-step stage A: the same set rebuilt in place for a cut that
+    # moves every step (cgb_shape_rebuild: neighbour lists kept, no FRNN), alternating the
+    # cut stopped at the middle of its path with the full cut; the last rebuild (full cut)
+    # must reproduce the first build's bits.
+    full = plate.creases[0]
+    v = np.asarray(full["vertices"], np.float64)
+    half = {"vertices": np.vstack([v[0], 0.5 * (v[0] + v[-1])]), "extend_start": full.get("extend_start", False),
+            "extend_end": False, "is_closed": False}
+    cuts = ([half], list(plate.creases))
+    for c in cuts:
+        sh.rebuild(c)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for i in range(2 * steps):
+        sh.rebuild(cuts[i % 2])
+    ctx.synchronize()
+    wall_rb = (time.perf_counter() - t0) / (2 * steps)
+    d2 = sh.download()
+    rebuild_same = bool(all(np.array_equal(d[k], d2[k]) for k in ("psi", "dpsi", "ddpsi")))
     out = {
         "workload": ("1,000,000 uniform points in [0,200]^2 over 401x401 jittered nodes (+/-0.2h), quadratic "
                      "basis, cubic B-spline window, per-node support radius U[2.5h, 3.5h], one straight cut "
@@ -506,6 +525,10 @@ def shape_stage(cg, ctx, args, with_cpu):
         "rkpm_points_per_s": len(pts) / (ph["rkpm"] * 1e-3) if ph["rkpm"] > 0 else None,
         "reproducing_error": reproducing_error(d, plate.node_xy, pts, 1.5),
         "precision": "fp64",
+        "rebuild": {"ms_per_rebuild": wall_rb * 1e3, "points_per_s": len(pts) / wall_rb,
+                    "bitwise_equal_to_build": rebuild_same,
+                    "what": "cgb_shape_rebuild of the same set for a moved cut (progressive creasing's "
+                            "per-step stage A), alternating the half and the full cut"},
     }
     if with_cpu:
         # The oracle's restatement of GlobalFRNN::execute + GlobalRKPM::solve (OpenMP, all

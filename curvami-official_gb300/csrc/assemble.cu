@@ -1254,6 +1254,7 @@ constexpr int kStagePad = 16;
 void ensure_fp32_shapes(cgb_assembler* a) {
   if (a->dpsi32.p) return;
   const cgb_shape* S = a->faces;
+  a->faces_version = S->version;
   cudaStream_t st = a->ctx->stream;
   a->dpsi32.alloc(2 * S->nnz + kStagePad);
   a->ddpsi32.alloc(3 * S->nnz + kStagePad);
@@ -1290,6 +1291,7 @@ __global__ void fill_sell(int n_gp, const int64_t* __restrict__ ptr, const int32
 void ensure_sell(cgb_assembler* a) {
   if (a->sell_ptr.p) return;
   const cgb_shape* S = a->faces;
+  a->faces_version = S->version;
   cudaStream_t st = a->ctx->stream;
   std::vector<int64_t> ptr(S->n_gp + 1);
   CGB_CUDA(cudaMemcpyAsync(ptr.data(), S->nbr_ptr.p, ptr.size() * 8, cudaMemcpyDeviceToHost, st));
@@ -1312,6 +1314,25 @@ void ensure_sell(cgb_assembler* a) {
   CGB_CUDA(cudaGetLastError());
 }
 
+}  // namespace
+
+void refresh_face_copies(cgb_assembler* a) {
+  const cgb_shape* S = a->faces;
+  if (a->faces_version == S->version) return;
+  cudaStream_t st = a->ctx->stream;
+  if (a->dpsi32.p && S->nnz) {
+    to_float<<<nb(2 * S->nnz, 256), 256, 0, st>>>(2 * S->nnz, S->dpsi.p, a->dpsi32.p);
+    to_float<<<nb(3 * S->nnz, 256), 256, 0, st>>>(3 * S->nnz, S->ddpsi.p, a->ddpsi32.p);
+  }
+  if (a->sell_ptr.p && S->n_gp)
+    fill_sell<<<nb(S->n_gp, 128), 128, 0, st>>>(S->n_gp, S->nbr_ptr.p, S->nbr_idx.p, S->dpsi.p, S->ddpsi.p,
+                                                a->sell_ptr.p, a->sidx.p, a->sdpsi.p, a->sddpsi.p);
+  CGB_CUDA(cudaGetLastError());
+  a->faces_version = S->version;
+}
+
+namespace {
+
 constexpr int kChunks = 4;
 
 // The second stream and the events of the chunked face launch (created once per
@@ -1326,6 +1347,16 @@ void ensure_side_stream(cgb_assembler* a) {
 
 }  // namespace
 
+// Dynamic shared memory of the merged FP32 tangent for neighbour lists of up to nmax
+// entries: per-point state and frames of the 16 points, one record per (point, neighbour)
+// (RW float4, odd), and the staging windows of grad / Hessian Phi (20 bytes per entry + 64).
+constexpr size_t kMergedSmemMax = 220 * 1024;
+size_t merged_smem_bytes(int nmax, bool bzero) {
+  const size_t RW = bzero ? 7 : 9, FW = 3;
+  const size_t E = static_cast<size_t>(kMG) * nmax;
+  return (static_cast<size_t>(kState) * kMG + 4 * FW * kMG + 4 * RW * E) * sizeof(float) + (20 * E + 64);
+}
+
 void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags) {
   cgb_context* ctx = a->ctx;
   cudaStream_t st = ctx->stream;
@@ -1336,11 +1367,17 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   const bool hinge = (flags & CGB_HINGE) != 0;
   if (!a->have_material) throw Error(CGB_ERR_INVALID, "assemble: material not set (cgb_set_material)");
   if (want_K && !d_K) throw Error(CGB_ERR_INVALID, "assemble: K output missing with CGB_TANGENT");
+  refresh_face_copies(a);
   if (det) deterministic_prepare(a);
+  bool bzero = true;
+  for (double v : a->B) bzero = bzero && (v == 0.0);
   // The FP32 tangent merges each group's contributions per block; in deterministic mode the
-  // merged sums become the K units, unless a group is too large to merge.
+  // merged sums become the K units, unless a group is too large to merge. The merged kernel
+  // stages a group's records in shared memory: supports too wide for that (the reference
+  // app's cubic basis at rho = 6h has over 100 neighbours) take the per-point FP32 tangent.
+  const size_t msm = merged_smem_bytes(std::max(S->max_n, 1), bzero);
   bool merged = false;
-  if (mixed && want_K) {
+  if (mixed && want_K && msm <= kMergedSmemMax) {
     merge_prepare(a);
     merged = !det || a->mrg_n_direct == 0;
   }
@@ -1413,8 +1450,6 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   const int sms = sm_count(ctx->device);
   const unsigned grid = std::max(1u, std::min(nb(S->n_gp, 32 * kFaceWarps), static_cast<unsigned>(sms * 8)));
   (void)grid;
-  bool bzero = true;
-  for (double v : a->B) bzero = bzero && (v == 0.0);
   // Residual kernel (phase 1) then tangent kernel (phase 2), each at its own occupancy.
   const size_t state_bytes = static_cast<size_t>(kState) * std::max(S->n_gp, 1) * tk;
   if (want_K) {
@@ -1472,12 +1507,6 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     if (merged) {
       MergeArgs mg{a->mrg_ent_ptr.p, a->mrg_ent_slot.p, a->mrg_ent_cstart.p, a->mrg_direct.p, a->mrg_code.p,
                    ctx->dev_err.p, a->test_stage_extra_tx};
-      const int RW = bzero ? 7 : 9, FW = 3;  // record and frame strides of the kernel (float4)
-      const size_t E = static_cast<size_t>(kMG) * fa.nmax;
-      const size_t msm = (static_cast<size_t>(kState) * kMG + 4 * FW * kMG + 4 * static_cast<size_t>(RW) * E) *
-                             sizeof(float) +
-                         (20 * E + 64);  // + the staging windows
-      if (msm > 220 * 1024) throw Error(CGB_ERR_CAPACITY, "assemble: neighbour lists too long for the merged tangent");
       auto kern = det ? (bzero ? face_tangent_merged_kernel<true, true> : face_tangent_merged_kernel<false, true>)
                       : (bzero ? face_tangent_merged_kernel<true, false> : face_tangent_merged_kernel<false, false>);
       CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(msm)));
@@ -1488,7 +1517,8 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
       const unsigned mgrid = static_cast<unsigned>(std::max(1, std::min(groups, std::max(per_sm, 1) * sms)));
       kern<<<mgrid, kMrgThreads, msm, a->side>>>(fa, st32, mg);
     } else if (mixed) {
-      if (bzero) tl(face_tangent_kernel<float, true, true>, st32); else tl(face_tangent_kernel<float, true, false>, st32);
+      if (det) { if (bzero) tl(face_tangent_kernel<float, true, true>, st32); else tl(face_tangent_kernel<float, true, false>, st32); }
+      else { if (bzero) tl(face_tangent_kernel<float, false, true>, st32); else tl(face_tangent_kernel<float, false, false>, st32); }
     } else {
       if (det) { if (bzero) tl(face_tangent_kernel<double, true, true>, st64); else tl(face_tangent_kernel<double, true, false>, st64); }
       else { if (bzero) tl(face_tangent_kernel<double, false, true>, st64); else tl(face_tangent_kernel<double, false, false>, st64); }

@@ -204,6 +204,7 @@ int cgb_graph_launch(cgb_graph* g) {
   cgb_context* ctx = g->a->ctx;
   return guarded_ctx(ctx, [&] {
     CGB_CUDA(cudaSetDevice(ctx->device));
+    cgb::refresh_face_copies(g->a);   // the face set was rebuilt since the capture
     CGB_CUDA(cudaGraphLaunch(g->exec, ctx->stream));
   });
 }

@@ -209,12 +209,30 @@ int cgb_set_nodes(cgb_context* ctx, const double* node_xy, int n_nodes) {
   return guarded(ctx, [&] {
     need(n_nodes > 0 && node_xy, "cgb_set_nodes: need at least one node");
     bind_device(ctx);
+    const size_t m = 2 * static_cast<size_t>(n_nodes);
+    if (ctx->n_nodes != n_nodes || !std::equal(node_xy, node_xy + m, ctx->h_node_xy.begin())) ++ctx->node_gen;
     ctx->n_nodes = n_nodes;
-    ctx->h_node_xy.assign(node_xy, node_xy + 2 * static_cast<size_t>(n_nodes));
+    ctx->h_node_xy.assign(node_xy, node_xy + m);
     cgb::upload(ctx->node_xy, node_xy, 2 * static_cast<size_t>(n_nodes), ctx->stream);
     CGB_CUDA(cudaStreamSynchronize(ctx->stream));
   });
 }
+
+namespace {
+std::vector<cgb::Crease> crease_list(const cgb_crease* creases, int n_creases, const char* who) {
+  need(n_creases >= 0 && (n_creases == 0 || creases), (std::string(who) + ": bad crease list").c_str());
+  std::vector<cgb::Crease> cr(n_creases);
+  for (int c = 0; c < n_creases; ++c) {
+    need(creases[c].n_vertices >= 0 && (creases[c].n_vertices == 0 || creases[c].xy),
+         (std::string(who) + ": bad crease vertices").c_str());
+    cr[c].xy.assign(creases[c].xy, creases[c].xy + 2 * static_cast<size_t>(creases[c].n_vertices));
+    cr[c].extend_start = creases[c].extend_start;
+    cr[c].extend_end = creases[c].extend_end;
+    cr[c].is_closed = creases[c].is_closed;
+  }
+  return cr;
+}
+}  // namespace
 
 int cgb_shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shape_params* params,
                     const cgb_crease* creases, int n_creases, cgb_shape** out) {
@@ -224,17 +242,8 @@ int cgb_shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_s
   const int rc = guarded(ctx, [&] {
     need(params != nullptr, "cgb_shape_build: params is NULL");
     need(n_gp == 0 || gp_xy, "cgb_shape_build: gp_xy is NULL");
-    need(n_creases >= 0 && (n_creases == 0 || creases), "cgb_shape_build: bad crease list");
+    const std::vector<cgb::Crease> cr = crease_list(creases, n_creases, "cgb_shape_build");
     bind_device(ctx);
-    std::vector<cgb::Crease> cr(n_creases);
-    for (int c = 0; c < n_creases; ++c) {
-      need(creases[c].n_vertices >= 0 && (creases[c].n_vertices == 0 || creases[c].xy),
-           "cgb_shape_build: bad crease vertices");
-      cr[c].xy.assign(creases[c].xy, creases[c].xy + 2 * static_cast<size_t>(creases[c].n_vertices));
-      cr[c].extend_start = creases[c].extend_start;
-      cr[c].extend_end = creases[c].extend_end;
-      cr[c].is_closed = creases[c].is_closed;
-    }
     cgb::shape_build(ctx, gp_xy, n_gp, *params, cr, sh);
   });
   // A rank-deficient support still returns the (flagged) shape set, as the reference
@@ -247,6 +256,16 @@ int cgb_shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_s
     delete sh;
   }
   return rc;
+}
+
+int cgb_shape_rebuild(cgb_shape* sh, const cgb_crease* creases, int n_creases) {
+  if (!sh || !sh->ctx) return CGB_ERR_INVALID;
+  cgb_context* ctx = sh->ctx;
+  return guarded(ctx, [&] {
+    const std::vector<cgb::Crease> cr = crease_list(creases, n_creases, "cgb_shape_rebuild");
+    bind_device(ctx);
+    cgb::shape_rebuild(sh, cr);
+  });
 }
 
 int cgb_shape_from_host(cgb_context* ctx, int n_gp, const int64_t* nbr_ptr, const int32_t* nbr_idx,
@@ -339,6 +358,31 @@ int cgb_shape_destroy(cgb_shape* sh) {
   return CGB_OK;
 }
 
+namespace {
+// Fold::gp_theta0 / gp_active on the device. Both arrays always exist (filled with the
+// scalar rest angle and "active" when not given), so a graph captured before a later
+// cgb_assembler_set_fold_state reads the new state at replay.
+void set_fold_state(cgb_context* ctx, cgb_fold_dev& d, double theta0, const double* theta0_gp,
+                    const int8_t* active) {
+  cudaStream_t st = ctx->stream;
+  const size_t n = static_cast<size_t>(d.n_gp);
+  std::vector<double> t0(n, theta0);
+  std::vector<int8_t> ac(n, 1);
+  if (theta0_gp) std::copy(theta0_gp, theta0_gp + n, t0.begin());
+  if (active) std::copy(active, active + n, ac.begin());
+  d.theta0 = theta0;
+  d.theta0_gp.ensure(n);
+  d.active.ensure(n);
+  if (n) {
+    CGB_CUDA(cudaMemcpyAsync(d.theta0_gp.p, t0.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CGB_CUDA(cudaMemcpyAsync(d.active.p, ac.data(), n, cudaMemcpyHostToDevice, st));
+  }
+  CGB_CUDA(cudaStreamSynchronize(st));  // the host vectors go out of scope
+  d.has_theta0_gp = true;
+  d.has_active = true;
+}
+}  // namespace
+
 int cgb_assembler_create(cgb_context* ctx, const cgb_shape* faces, const double* face_weight, const cgb_fold* folds,
                          int n_folds, cgb_assembler** out) {
   if (!ctx || !out) return CGB_ERR_INVALID;
@@ -370,8 +414,7 @@ int cgb_assembler_create(cgb_context* ctx, const cgb_shape* faces, const double*
       d.right = f.right;
       cgb::upload(d.weight, f.weight, d.n_gp, st);
       cgb::upload(d.tangent, f.tangent, 2 * static_cast<size_t>(d.n_gp), st);
-      if (f.theta0_gp) { cgb::upload(d.theta0_gp, f.theta0_gp, d.n_gp, st); d.has_theta0_gp = true; }
-      if (f.active) { cgb::upload(d.active, f.active, d.n_gp, st); d.has_active = true; }
+      set_fold_state(ctx, d, f.theta0, f.theta0_gp, f.active);
     }
     cgb::pattern_build(a);
     a->F.alloc(3 * static_cast<size_t>(a->n_nodes));
@@ -384,6 +427,16 @@ int cgb_assembler_create(cgb_context* ctx, const cgb_shape* faces, const double*
     delete a;
   }
   return rc;
+}
+
+int cgb_assembler_set_fold_state(cgb_assembler* a, int fold, double theta0, const double* theta0_gp,
+                                 const int8_t* active) {
+  if (!a || !a->ctx) return CGB_ERR_INVALID;
+  return guarded(a->ctx, [&] {
+    need(fold >= 0 && fold < static_cast<int>(a->folds.size()), "cgb_assembler_set_fold_state: no such fold");
+    bind_device(a->ctx);
+    set_fold_state(a->ctx, a->folds[fold], theta0, theta0_gp, active);
+  });
 }
 
 int cgb_assembler_destroy(cgb_assembler* a) {

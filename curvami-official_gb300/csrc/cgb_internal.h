@@ -83,6 +83,7 @@ struct cgb_context {
   int n_nodes = 0;
   std::vector<double> h_node_xy;
   cgb::DevBuf<double> node_xy;
+  uint64_t node_gen = 0;  // bumped whenever cgb_set_nodes changes the coordinates
   // Device-side error word written by kernels (bounds checks, capacity).
   cgb::DevBuf<int> dev_err;
   int* h_err = nullptr;  // pinned mirror
@@ -107,6 +108,15 @@ struct cgb_shape {
   cgb::DevBuf<double> psi;        // nnz
   cgb::DevBuf<double> dpsi;       // 2 * nnz (x, y)
   cgb::DevBuf<double> ddpsi;      // 3 * nnz (xx, yy, xy)
+  // What a rebuild with other creases needs (sets made by cgb_shape_build only): the
+  // shape parameters and the node coordinates the neighbour lists were found on.
+  bool rebuildable = false;
+  double rho = 0.0;
+  int order = 0, kernel = 0;
+  bool has_rho_node = false;
+  cgb::DevBuf<double> rho_node;   // n_nodes (per-node radius) when has_rho_node
+  uint64_t node_gen = 0;
+  uint64_t version = 0;           // bumped by every rebuild (derived copies go stale)
 };
 
 // Per-fold data kept by the assembler (plate/PlateData.h: Fold; Constraints.h:341).
@@ -157,6 +167,7 @@ struct cgb_assembler {
   cgb::DevBuf<double> K;            // 9 n_blocks (device scratch for host-buffer calls)
   cgb::DevBuf<double> x;            // 3 n_nodes
   cgb::DevBuf<float> dpsi32, ddpsi32; // FP32 copies of the face shape derivatives (mixed mode)
+  uint64_t faces_version = 0;       // faces->version the copies (FP32, sliced-ELL) were made from
   // Merged contributions of the FP32 tangent: per group of 16 consecutive Gauss points the
   // distinct blocks ("entries", count-descending) and every pair's code in entry order.
   bool mrg_ready = false;
@@ -212,6 +223,9 @@ void prof_end(cgb_context* ctx, int phase, int launches, cudaStream_t stream = n
 // shape.cu
 void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shape_params& prm,
                  const std::vector<Crease>& creases, cgb_shape* out);
+// Phi and its derivatives of an existing set recomputed in place with other creases
+// (same points, radius and so neighbour lists).
+void shape_rebuild(cgb_shape* sh, const std::vector<Crease>& creases);
 // pattern.cu
 void pattern_build(cgb_assembler* a);
 void deterministic_prepare(cgb_assembler* a);
@@ -224,6 +238,9 @@ void deterministic_entry_lists(cgb_assembler* a);
 void merge_prepare(cgb_assembler* a);
 // assemble.cu
 void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags);
+// Re-derive the assembler's copies of the face shape derivatives after a rebuild of the
+// face set (no-op when they are current); enqueued on the context stream.
+void refresh_face_copies(cgb_assembler* a);
 void energies_device(cgb_assembler* a, const double* d_x, double* out3);
 void face_mixed_on_arrays(const cgb_face_problem& pr, const double* d_x, double* d_K, double* d_F,
                           float* kacc, cudaStream_t st);

@@ -442,6 +442,8 @@ inline unsigned blocks_for(int64_t n, int t = kThreads) { return static_cast<uns
 
 }  // namespace
 
+void shape_values(cgb_context* ctx, cgb_shape* out, const std::vector<Crease>& creases);
+
 void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shape_params& prm,
                  const std::vector<Crease>& creases, cgb_shape* out) {
   cudaStream_t st = ctx->stream;
@@ -454,6 +456,10 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
   if (creases.size() > 4) throw Error(CGB_ERR_CAPACITY, "cgb_shape_build: at most 4 creases per call");
   out->ctx = ctx;
   out->n_gp = n_gp;
+  out->rho = prm.rho;
+  out->order = prm.order;
+  out->kernel = prm.kernel;
+  out->node_gen = ctx->node_gen;
 
   // ---- node cell grid (FRNN.h:33-44), host side, O(n_nodes) ----
   const double* nxy = ctx->h_node_xy.data();
@@ -493,10 +499,11 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
     for (int i = 0; i < n_nodes; ++i) cnodes[cur[key[i]]++] = i;  // ascending node index per cell
   }
   DevBuf<int32_t> d_cstart, d_cnodes;
-  DevBuf<double> d_rn;
   upload(d_cstart, cstart.data(), cstart.size(), st);
   upload(d_cnodes, cnodes.data(), cnodes.size(), st);
-  if (prm.rho_node) upload(d_rn, rn.data(), rn.size(), st);
+  out->has_rho_node = prm.rho_node != nullptr;
+  if (prm.rho_node) upload(out->rho_node, rn.data(), rn.size(), st);
+  const double* d_rn = prm.rho_node ? out->rho_node.p : nullptr;
   GridDev G{minx, miny, cell, cols, ncells, d_cstart.p, d_cnodes.p};
 
   upload(out->gp_xy, gp_xy, 2 * static_cast<size_t>(n_gp), st);
@@ -505,7 +512,7 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
   prof_begin(ctx, CGB_PHASE_FRNN);
   if (n_gp > 0)
     frnn_kernel<<<blocks_for(n_gp), kThreads, 0, st>>>(n_gp, out->gp_xy.p, ctx->node_xy.p,
-                                                        prm.rho_node ? d_rn.p : nullptr, prm.rho, rho2, G,
+                                                        d_rn, prm.rho, rho2, G,
                                                         nullptr, d_cnt.p, nullptr, nullptr);
   CGB_CUDA(cudaGetLastError());
   prof_end(ctx, CGB_PHASE_FRNN, n_gp > 0 ? 1 : 0);
@@ -529,12 +536,25 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
   prof_begin(ctx, CGB_PHASE_FRNN);
   if (n_gp > 0)
     frnn_kernel<<<blocks_for(n_gp), kThreads, 0, st>>>(n_gp, out->gp_xy.p, ctx->node_xy.p,
-                                                        prm.rho_node ? d_rn.p : nullptr, prm.rho, rho2, G,
+                                                        d_rn, prm.rho, rho2, G,
                                                         out->nbr_ptr.p, nullptr, out->nbr_idx.p, out->s.p);
   prof_end(ctx, CGB_PHASE_FRNN, n_gp > 0 ? 1 : 0);
   CGB_CUDA(cudaGetLastError());
 
-  // ---- crease indicators: per node side, per Gauss point value and derivatives ----
+  out->rebuildable = true;
+  shape_values(ctx, out, creases);
+}
+
+// Crease indicators, RKPM and the reference's guards for the points and neighbour lists
+// already in `out` (SetupHelper::recomputeShapeFunctions after the FRNN). The value
+// arrays keep their allocation when they have one, so device pointers handed out
+// earlier (assemblers, captured graphs) stay valid across rebuilds.
+void shape_values(cgb_context* ctx, cgb_shape* out, const std::vector<Crease>& creases) {
+  cudaStream_t st = ctx->stream;
+  const int n_nodes = ctx->n_nodes;
+  const int n_gp = out->n_gp;
+  const int64_t nnz = out->nnz;
+  if (creases.size() > 4) throw Error(CGB_ERR_CAPACITY, "cgb_shape_build: at most 4 creases per call");
   const int nc = static_cast<int>(creases.size());
   std::vector<DevBuf<double>> cxy(nc);
   DevBuf<int8_t> side(static_cast<size_t>(std::max(nc, 1)) * n_nodes);
@@ -556,16 +576,16 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
   CGB_CUDA(cudaGetLastError());
 
   // ---- RKPM ----
-  out->psi.alloc(nnz);
-  out->dpsi.alloc(2 * nnz);
-  out->ddpsi.alloc(3 * nnz);
+  if (out->psi.n < static_cast<size_t>(std::max<int64_t>(nnz, 1))) out->psi.alloc(nnz);
+  if (out->dpsi.n < static_cast<size_t>(std::max<int64_t>(2 * nnz, 1))) out->dpsi.alloc(2 * nnz);
+  if (out->ddpsi.n < static_cast<size_t>(std::max<int64_t>(3 * nnz, 1))) out->ddpsi.alloc(3 * nnz);
   DevBuf<int8_t> bad(n_gp);
-  RkpmArgs ra{n_gp, n_nodes, prm.kernel, nc, prm.rho, out->gp_xy.p, ctx->node_xy.p,
-              prm.rho_node ? d_rn.p : nullptr, out->nbr_ptr.p, out->nbr_idx.p, out->s.p, gind.p,
+  RkpmArgs ra{n_gp, n_nodes, out->kernel, nc, out->rho, out->gp_xy.p, ctx->node_xy.p,
+              out->has_rho_node ? out->rho_node.p : nullptr, out->nbr_ptr.p, out->nbr_idx.p, out->s.p, gind.p,
               side.p, out->psi.p, out->dpsi.p, out->ddpsi.p, bad.p};
   prof_begin(ctx, CGB_PHASE_RKPM);
   if (n_gp > 0) {
-    switch (prm.order) {
+    switch (out->order) {
       case 1: rkpm_kernel<1><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
       case 2: rkpm_kernel<2><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
       default: rkpm_kernel<3><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
@@ -583,11 +603,16 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
     if (hbad[g] == 1) { if (!n1) f1 = g; ++n1; }
     if (hbad[g] == 2) { if (!n2) f2 = g; ++n2; }
   }
+  auto count_of = [&](size_t g) {
+    int64_t pr[2];
+    CGB_CUDA(cudaMemcpy(pr, out->nbr_ptr.p + g, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    return pr[1] - pr[0];
+  };
   if (n1) {
     throw Error(CGB_ERR_SINGULAR,
                 "RKPM: singular moment matrix at " + std::to_string(n1) + " of " + std::to_string(n_gp) +
                     " Gauss points (first is index " + std::to_string(f1) + " with " +
-                    std::to_string(cnt[f1]) +
+                    std::to_string(count_of(f1)) +
                     " neighbours). The support is rank-deficient for the requested "
                     "basis order - typically too few visible nodes, which happens "
                     "where a crease cuts most of a support away. Increase the support "
@@ -597,9 +622,20 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
     throw Error(CGB_ERR_PIVOT,
                 "RKPM: moment-matrix pivot collapsed during block inversion at " + std::to_string(n2) +
                     " of " + std::to_string(n_gp) + " Gauss points (first is index " + std::to_string(f2) +
-                    " with " + std::to_string(cnt[f2]) +
+                    " with " + std::to_string(count_of(f2)) +
                     " neighbours). Same cause and remedies as a singular moment matrix.");
   }
+}
+
+void shape_rebuild(cgb_shape* sh, const std::vector<Crease>& creases) {
+  cgb_context* ctx = sh->ctx;
+  if (!sh->rebuildable)
+    throw Error(CGB_ERR_INVALID, "cgb_shape_rebuild: the set was not made by cgb_shape_build (wrapped or concatenated)");
+  if (ctx->node_gen != sh->node_gen)
+    throw Error(CGB_ERR_INVALID, "cgb_shape_rebuild: the nodes changed since the set was built (cgb_set_nodes)");
+  // The new values stand even when a guard fires, as the reference's arrays do.
+  ++sh->version;
+  shape_values(ctx, sh, creases);
 }
 
 }  // namespace cgb

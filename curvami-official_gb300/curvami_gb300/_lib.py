@@ -36,6 +36,7 @@ SIGNATURES = {
     "cgb_synchronize": (i32, [vp]),
     "cgb_set_nodes": (i32, [vp, vp, i32]),
     "cgb_shape_build": (i32, [vp, vp, i32, vp, vp, i32, C.POINTER(vp)]),
+    "cgb_shape_rebuild": (i32, [vp, vp, i32]),
     "cgb_shape_from_host": (i32, [vp, i32, vp, vp, vp, vp, vp, C.POINTER(vp)]),
     "cgb_shape_size": (i32, [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i32)]),
     "cgb_shape_download": (i32, [vp, vp, vp, vp, vp, vp, vp]),
@@ -53,6 +54,7 @@ SIGNATURES = {
     "cgb_graph_launch": (i32, [vp]),
     "cgb_graph_destroy": (i32, [vp]),
     "cgb_test_stage_timeout": (i32, [vp, i32]),
+    "cgb_assembler_set_fold_state": (i32, [vp, i32, dbl, vp, vp]),
     "cgb_set_material": (i32, [vp, vp, vp, vp]),
     "cgb_assemble": (i32, [vp, vp, vp, vp, i32]),
     "cgb_assemble_device": (i32, [vp, vp, vp, vp, i32]),

@@ -101,6 +101,16 @@ class ShapeSet:
         ctx.check(ctx.lib.cgb_shape_size(self.h, C.byref(n), C.byref(nnz), C.byref(mx)))
         self.n_gp, self.nnz, self.max_n = n.value, nnz.value, mx.value
 
+    def rebuild(self, creases=()):
+        """cgb_shape_rebuild: Phi and its derivatives recomputed in place for other cuts
+        (SetupHelper::recomputeShapeFunctions, plate/SetupHelper.h:112-138); the points and
+        neighbour lists stay. Raises CGBError with the reference's message on a
+        rank-deficient support (the new, flagged values then stand)."""
+        arr, keep = _creases_struct(list(creases))
+        rc = self.ctx.lib.cgb_shape_rebuild(self.h, C.addressof(arr), len(creases))
+        del keep
+        self.ctx.check(rc)
+
     def download(self):
         ptr = np.zeros(self.n_gp + 1, np.int64)
         idx = np.zeros(max(self.nnz, 1), np.int32)
@@ -201,6 +211,14 @@ class NonLinearAssembler:
         nd = C.c_int(); nnz = C.c_int64()
         ctx.check(ctx.lib.cgb_assembler_pattern(self.h, C.byref(nd), C.byref(nnz)))
         self.n_dofs, self.nnz = nd.value, nnz.value
+
+    def set_fold_state(self, fold: int, theta0: float = 0.0, theta0_gp=None, active=None):
+        """cgb_assembler_set_fold_state: Fold::gp_theta0 / gp_active of one fold (None = the
+        scalar rest angle everywhere / every point active)."""
+        t0 = None if theta0_gp is None else _c(theta0_gp, np.float64)
+        ac = None if active is None else _c(np.asarray(active) != 0, np.int8)
+        self.ctx.check(self.ctx.lib.cgb_assembler_set_fold_state(self.h, int(fold), float(theta0), _p(t0),
+                                                                  _p(ac)))
 
     def set_material(self, A, B, D):
         self.A, self.B, self.D = (_c(A, np.float64).reshape(9), _c(B, np.float64).reshape(9),
@@ -357,9 +375,26 @@ class PlateModel:
             folds.append({"left": L_, "right": R_, "weight": f.left.weight, "tangent": f.left.tangent,
                           "Kt": f.Kt, "theta0": f.theta0})
         self.fold_specs = folds
+        # Point domains (GmshReader point elements), entity tag -> shape set, for
+        # point supports and loads.
+        self.point_sets = {tag: shape_functions(self.ctx, ps.xy, **kw) for tag, ps in plate.points.items()}
         self.asm = NonLinearAssembler(self.ctx, self.faces, plate.faces.weight, folds)
         A, B, D = abd_isotropic(plate.E, plate.nu, plate.thickness)
         self.asm.set_material(A, B, D)
+
+    def shape_sets(self):
+        """Every shape set of the model: faces, each fold's left and right, each point domain."""
+        out = [self.faces]
+        for L_, R_ in self.fold_sets:
+            out += [L_, R_]
+        return out + list(self.point_sets.values())
+
+    def rebuild(self, creases):
+        """SetupHelper::recomputeShapeFunctions (plate/SetupHelper.h:112-138) on the GPU:
+        every shape set of the model recomputed in place for the cuts `creases`, the
+        neighbour lists and the K pattern kept (they depend on the support radius only)."""
+        for sh in self.shape_sets():
+            sh.rebuild(creases)
 
     def assemble_system(self, x, flags=L.TANGENT | L.HINGE):
         return self.asm.assemble(x, flags)

@@ -272,6 +272,36 @@ def plate_from_mesh(path, crease_tags=(), Kt=1e-3, order=2, kernel=0, rho=None, 
     fxy, fw, _ = q["face"]
     faces, nsplit = synth.split_on_creases(synth.PointSet(fxy, fw), creases)
     r = support_radius(nodes, 3) if rho is None else float(rho)
+    pxy, pw, ptag = q["point"]
+    points = {int(t): synth.PointSet(pxy[ptag == t], pw[ptag == t]) for t in sorted(set(ptag.tolist()))}
     return synth.Plate(name=str(path), node_xy=nodes, faces=faces, creases=creases, folds=folds, rho=r,
                        order=order, kernel=kernel, E=E, nu=nu, thickness=thickness,
-                       meta={"mesh": str(path), "split": nsplit, "elements": len(elements)})
+                       meta={"mesh": str(path), "split": nsplit, "elements": len(elements)}, points=points)
+
+
+def centre_crease_sheet(n_cells=20, half=1.0, crease_half=0.5, crease_segments=10, crease_tag=5):
+    """Nodes and elements of a square sheet [-half, half]^2 of n_cells x n_cells quadrangles
+    (entity 1) with a crease line (-crease_half, 0) -> (crease_half, 0) of its own nodes,
+    one line element per segment (entity `crease_tag`), and point elements at the corners
+    (-half, -half), (half, -half), (-half, half) with entity tags 1, 2, 4: the layout of the
+    reference's centre-crease benchmark meshes (a transfinite, recombined square and a
+    crease that is not embedded in it). Returns (node_xy, [Element])."""
+    m = n_cells + 1
+    t = np.linspace(-half, half, m)
+    X, Y = np.meshgrid(t, t)                     # node (i, j) at index j * m + i
+    grid = np.stack([X.ravel(), Y.ravel()], axis=1)
+    c = np.stack([np.linspace(-crease_half, crease_half, crease_segments + 1),
+                  np.zeros(crease_segments + 1)], axis=1)
+    node_xy = np.vstack([grid, c])
+    els = []
+    for j in range(n_cells):
+        for i in range(n_cells):
+            a = j * m + i
+            els.append(Element(3, 1, (a, a + 1, a + m + 1, a + m)))
+    base = m * m
+    for k in range(crease_segments):
+        els.append(Element(1, crease_tag, (base + k, base + k + 1)))
+    els.append(Element(15, 1, (0,)))
+    els.append(Element(15, 2, (m - 1,)))
+    els.append(Element(15, 4, ((m - 1) * m,)))
+    return node_xy, els

@@ -164,20 +164,26 @@ def fold_angle_and_grad(F12: np.ndarray, tx: np.ndarray, ty: np.ndarray):
 
 @dataclass
 class FoldSides:
-    """One Fold for the constraint rows: both sides' shape tables and the crease data."""
+    """One Fold for the constraint rows: both sides' shape tables and the crease data.
+    active / theta0_gp: Fold::gp_active / gp_theta0 (None = every point active / the
+    scalar theta0), as progressive creasing sets them (plate/ProgressiveCreasing.h:621-639)."""
     left: ShapeTable
     right: ShapeTable
     tangent: np.ndarray
     theta0: float = 0.0
     rigid: bool = False
+    active: np.ndarray | None = None
+    theta0_gp: np.ndarray | None = None
 
 
 class GpuAssembly:
     """Backend over the GPU assembler (NonLinearAssembler of api.py)."""
 
-    def __init__(self, assembler, mixed: bool = False, deterministic: bool = False):
+    def __init__(self, assembler, mixed: bool = False, deterministic: bool = False, exact_hinge: bool = False):
+        """exact_hinge: the hinge tangent with the dihedral Hessian (Meshless::fold_exact_tangent)."""
         self.asm = assembler
-        self.extra = (L.MIXED if mixed else 0) | (L.DETERMINISTIC if deterministic else 0)
+        self.extra = ((L.MIXED if mixed else 0) | (L.DETERMINISTIC if deterministic else 0) |
+                      (L.HINGE_EXACT if exact_hinge else 0))
 
     def pattern(self):
         return self.asm.pattern()
@@ -198,13 +204,14 @@ class PlateProblem:
     for flagRig (plate/Meshless.h:113-127, Constraints.h:280-304)."""
 
     def __init__(self, n_nodes: int, backend, faces: ShapeTable, face_weight, face_load=None,
-                 edges=(), folds=(), flag_rig: bool = False):
+                 edges=(), folds=(), flag_rig: bool = False, points=()):
         self.n_nodes = n_nodes
         self.ns = 3 * n_nodes
         self.backend = backend
         self.faces = faces
         self.face_weight = np.asarray(face_weight, np.float64)
         self.face_load = None if face_load is None else np.asarray(face_load, np.float64)
+        self.points = list(points)        # (LineDomain of point Gauss points, ShapeTable)
         self.edges = list(edges)          # (LineDomain, ShapeTable)
         self.folds = list(folds)          # FoldSides
         self.flag_rig = flag_rig
@@ -240,7 +247,7 @@ class PlateProblem:
                 w = self.faces.P.T @ self.face_weight       # sum_g w_g Psi_I(x_g)
                 for d in range(3):
                     F[d::3] += w * self.face_load[d]
-            for dom, tab in self.edges:
+            for dom, tab in self.points + self.edges:
                 f = np.asarray(dom.bc.force, np.float64)
                 if np.any(f != 0.0):
                     w = tab.P.T @ dom.weight
@@ -260,7 +267,7 @@ class PlateProblem:
             cols.append(3 * col_nodes + comp)
             vals.append(v)
 
-        for dom, tab in self.edges:
+        for dom, tab in self.points + self.edges:      # points first (Meshless.h:166-172)
             bc = dom.bc
             U = tab.P @ X
             UX, UY = tab.Dx @ X, tab.Dy @ X
@@ -288,27 +295,34 @@ class PlateProblem:
             row += k * tab.n_gp
 
         for f in self.folds:
+            # Rows of the active crease points only, in point order (Constraints.h:263-266).
             Lt, Rt = f.left, f.right
-            jump = Lt.P @ X - Rt.P @ X
+            n_all = Lt.n_gp
+            act = np.ones(n_all, bool) if f.active is None or len(f.active) == 0 else np.asarray(f.active) != 0
+            slot = np.cumsum(act) - 1                     # row group of each active point
+            n = int(act.sum())
+            jump = (Lt.P @ X - Rt.P @ X)[act]
             k = 4 if self.flag_rig else 3
-            n = Lt.n_gp
             cv = np.zeros((n, k))
             cv[:, :3] = jump
             eL, eR = Lt.rows(), Rt.rows()
+            mL, mR = act[eL], act[eR]
             for d in range(3):
-                add_rows(eL * k + d, Lt.idx, d, Lt.psi)
-                add_rows(eR * k + d, Rt.idx, d, -Rt.psi)
-            if self.flag_rig:
-                F12 = np.empty((n, 12))
+                add_rows(slot[eL[mL]] * k + d, Lt.idx[mL], d, Lt.psi[mL])
+                add_rows(slot[eR[mR]] * k + d, Rt.idx[mR], d, -Rt.psi[mR])
+            if self.flag_rig and n:
+                F12 = np.empty((n_all, 12))
                 F12[:, 0:3] = Lt.Dx @ X; F12[:, 3:6] = Lt.Dy @ X
                 F12[:, 6:9] = Rt.Dx @ X; F12[:, 9:12] = Rt.Dy @ X
                 F12[:, 0] += 1.0; F12[:, 4] += 1.0; F12[:, 6] += 1.0; F12[:, 10] += 1.0
                 theta, g = fold_angle_and_grad(F12, f.tangent[:, 0], f.tangent[:, 1])
-                cv[:, 3] = theta - f.theta0
-                for side, tab, e in ((0, Lt, eL), (6, Rt, eR)):
+                th0 = f.theta0 if f.theta0_gp is None or len(f.theta0_gp) == 0 else np.asarray(f.theta0_gp)
+                cv[:, 3] = (theta - th0)[act] if np.ndim(th0) else theta[act] - th0
+                for side, tab, e, m in ((0, Lt, eL, mL), (6, Rt, eR, mR)):
+                    em = e[m]
                     for d in range(3):
-                        v = g[e, side + d] * tab.dpsi[:, 0] + g[e, side + 3 + d] * tab.dpsi[:, 1]
-                        add_rows(e * k + 3, tab.idx, d, v)
+                        v = g[em, side + d] * tab.dpsi[m, 0] + g[em, side + 3 + d] * tab.dpsi[m, 1]
+                        add_rows(slot[em] * k + 3, tab.idx[m], d, v)
             c_parts.append(cv.reshape(-1))
             row += k * n
 

@@ -71,6 +71,7 @@ class Plate:
     thickness: float = 0.05
     seed: int = 0
     meta: dict = field(default_factory=dict)
+    points: dict = field(default_factory=dict)   # entity tag -> PointSet (mesh point elements)
 
     @property
     def n_nodes(self) -> int:

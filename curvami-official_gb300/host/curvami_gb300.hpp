@@ -110,6 +110,15 @@ class ShapeSet {
     return s;
   }
   const cgb_shape* get() const { return h_; }
+  // SetupHelper::recomputeShapeFunctions for other cuts: Phi and its derivatives
+  // recomputed in place, points and neighbour lists kept (progressive creasing's rebuild).
+  void rebuild(const std::vector<Crease>& creases) {
+    std::vector<cgb_crease> cr(creases.size());
+    for (size_t k = 0; k < creases.size(); ++k)
+      cr[k] = cgb_crease{creases[k].xy.data(), static_cast<int>(creases[k].xy.size() / 2),
+                         creases[k].extend_start, creases[k].extend_end, creases[k].is_closed};
+    ctx_->check(cgb_shape_rebuild(h_, cr.data(), static_cast<int>(cr.size())));
+  }
 
  private:
   ShapeSet(Context& ctx, cgb_shape* h) : ctx_(&ctx), h_(h) {}
@@ -155,6 +164,12 @@ class NonLinearAssembler {
   }
   void set_material(const double A[9], const double B[9], const double D[9]) {
     ctx_->check(cgb_set_material(h_, A, B, D));
+  }
+  // Fold::gp_theta0 / gp_active of fold k (empty vectors: theta0 everywhere / all active).
+  void set_fold_state(int k, double theta0, const std::vector<double>& theta0_gp,
+                      const std::vector<int8_t>& active) {
+    ctx_->check(cgb_assembler_set_fold_state(h_, k, theta0, theta0_gp.empty() ? nullptr : theta0_gp.data(),
+                                             active.empty() ? nullptr : active.data()));
   }
   // Meshless::assembleSystem (flags CGB_TANGENT | CGB_HINGE) / assembleSystemInternalOnly
   // (CGB_HINGE): K values (nnz, block-upper CSC) and F_int (n_dofs) overwritten.

@@ -114,6 +114,16 @@ int cgb_set_nodes(cgb_context* ctx, const double* node_xy, int n_nodes);
 int cgb_shape_build(cgb_context* ctx, const double* gp_xy, int n_gp,
                     const cgb_shape_params* params, const cgb_crease* creases, int n_creases,
                     cgb_shape** out);
+/* SetupHelper::recomputeShapeFunctions for one domain after the creases change
+ * (plate/SetupHelper.h:112-138), as progressive creasing calls it at every tip move
+ * (plate/ProgressiveCreasing.h:587-613 via main.cpp:613-616): the points, the support
+ * radius and so the neighbour lists are kept (they do not depend on the creases), and
+ * Phi and its derivatives are recomputed in place with the given cuts; the FRNN is not
+ * repeated. Device pointers of the set stay valid. Assemblers built on the set use the
+ * new values from their next assembly or graph launch. Only sets made by cgb_shape_build,
+ * with the context's nodes unchanged since. Errors as cgb_shape_build (the new values
+ * stand, flagged, on CGB_ERR_SINGULAR / CGB_ERR_PIVOT). */
+int cgb_shape_rebuild(cgb_shape* sh, const cgb_crease* creases, int n_creases);
 /* Wrap shape functions computed elsewhere (GaussPointData::neighbor_node_ids, dPsi,
  * ddPsi; core/include/curvami/MeshfreeData.h:28-34) for the assembly. psi may be NULL. */
 int cgb_shape_from_host(cgb_context* ctx, int n_gp, const int64_t* nbr_ptr,
@@ -147,6 +157,13 @@ int cgb_assembler_download_map(const cgb_assembler* a, int32_t* map, int64_t n_e
  * entries of the FP32 tangent (distinct blocks per group of 16 consecutive Gauss points),
  * out[3] groups too large to merge. The first call builds the merge tables. */
 int cgb_assembler_stats(cgb_assembler* a, int64_t out[4]);
+/* Fold::gp_theta0 and Fold::gp_active of fold `fold` (plate/PlateData.h:54-76), which
+ * progressive creasing rewrites at every step (plate/ProgressiveCreasing.h:621-639):
+ * theta0_gp NULL = every point at the scalar theta0, active NULL = every point active.
+ * Inactive crease points get no hinge force, stiffness or energy (Constraints.h:350).
+ * Graphs captured earlier replay with the new state. */
+int cgb_assembler_set_fold_state(cgb_assembler* a, int fold, double theta0, const double* theta0_gp,
+                                 const int8_t* active);
 /* LaminateProperties A, B, D (plate/PlateData.h:20-35), row-major 3x3 each. */
 int cgb_set_material(cgb_assembler* a, const double* A, const double* B, const double* D);
 
