@@ -400,6 +400,7 @@ def run_gpu(args):
     v_mix = world * n_gp / (ms_mix * 1e-3)
     v_f64 = world * n_gp / (ms_f64 * 1e-3)
     shape = None if args.no_shape_stage else shape_stage(cg, ctx, args, rank == 0 and not args.no_cpu_baseline)
+    creasing = None if args.no_shape_stage else creasing_run(rank == 0 and not args.no_cpu_baseline)
 
     line = {
         "metric": METRIC, "value": v_mix, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -429,6 +430,7 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "clocks": clocks,
         "shape_stage": shape,
+        "progressive_creasing": creasing,
     }
     if rank == 0:
         print(json.dumps(line))
@@ -554,6 +556,92 @@ def shape_stage(cg, ctx, args, with_cpu):
             "neighbours_bit_exact": same,
             "psi": rel(d["psi"][:e], psi), "dpsi": rel(d["dpsi"][:e].reshape(-1), dpsi.reshape(-1)),
             "ddpsi": rel(d["ddpsi"][:e].reshape(-1), ddpsi.reshape(-1)), "sample_points": m}
+    return out
+
+
+# ---------------------------------------------------------------------------------
+# Progressive creasing: the reference's centre-crease smoke example end to end
+# ---------------------------------------------------------------------------------
+
+SMOKE_PUBLISHED = {"E_mem": 4.006e-08, "E_ben": 9.404e-06, "E_hin": 1.594e-05, "theta_mean_deg": 0.1962}
+
+
+def creasing_run(with_cpu):
+    """The reference's smoke example (examples/smoke_centre_crease: 20 x 20 sheet, order-3
+    RKPM at rho = 6h, crease grown from the centre in 5 steps, LineSearch at each) run by
+    curvami_gb300.creasing over the GPU library: every tip move rebuilds all shape functions
+    on the GPU, every Newton iteration assembles there (FP64, exact hinge tangent); the KKT
+    solve is a dense FP64 LU on the GPU. Reported: wall time of the whole run, the GPU time
+    per phase, the Newton iterations, and the last step against the published row."""
+    import tempfile
+
+    import curvami_gb300 as cg
+    from curvami_gb300 import creasing as PC
+    from curvami_gb300 import solver as S
+
+    fx = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "smoke_centre_crease_nodes.npy")
+    xy = np.load(fx) if os.path.exists(fx) else None
+    tmp = tempfile.mkdtemp()
+    case = PC.centre_crease_case(os.path.join(tmp, "smoke.msh"), 20, node_xy=xy)
+    out = {"workload": ("examples/smoke_centre_crease of the reference: [-1,1]^2 sheet, 20x20 quads (3x3 rule, "
+                        "3600 face points), cubic RKPM at rho = 6h (up to 113 neighbours), crease grown "
+                        "middle_out over 10 segments (6 steps), theta0* = 0.5 deg, Kt = D, three corner "
+                        "supports, LineSearch to 1e-10 / 1e-12"),
+           "mesh": "gmsh node coordinates of the reference's CB_n20.msh" if xy is not None else "ideal grid",
+           "published_last_step": SMOKE_PUBLISHED}
+    import torch
+
+    # One-time library initialisation (cuSOLVER's dense LU of the device KKT) outside the timing.
+    torch.linalg.lu_factor(torch.eye(8, dtype=torch.float64, device="cuda"))
+    torch.cuda.synchronize()
+    for name, mixed in (("fp64", False), ("mixed", True)):
+        ctx = cg.Context(0)
+        t0 = time.perf_counter()
+        model = cg.PlateModel(case.plate, ctx)
+        plate = PC.GpuCreasingPlate(model, case.point_bcs, [case.spec], exact_tangent=True, mixed=mixed)
+        setup = time.perf_counter() - t0
+        solver = S.ContinuationSolver(kkt="device", refine_steps=1 if mixed else 0, **case.solver_args)
+        ctx.profile(True)
+        ctx.profile_read(reset=True)
+        x = np.zeros(3 * len(case.plate.node_xy))
+        t0 = time.perf_counter()
+        res = PC.run(solver, plate, x, [case.line], cfg=case.config)
+        wall = time.perf_counter() - t0
+        ph, nl = ctx.profile_read(reset=True)
+        ctx.profile(False)
+        last = res.steps[-1] if res.steps else {}
+        out[name] = {
+            "setup_s": setup, "run_s": wall, "stopped": res.stopped, "steps": len(res.steps),
+            "newton_iters": [r["newton_iters"] for r in res.steps],
+            "assemblies": plate.problem.n_assemble, "residual_assemblies": plate.problem.n_residual,
+            "last_step": {k: last.get(k) for k in SMOKE_PUBLISHED},
+            "matches_published": bool(last) and all(
+                abs(last[k] - v) <= 0.5 * 10 ** (np.floor(np.log10(abs(v))) - 3) + 2e-4 * abs(v)
+                for k, v in SMOKE_PUBLISHED.items()),
+            "gpu_ms": {"rebuild (crease + rkpm)": ph["crease"] + ph["rkpm"],
+                       "assembly (face + tangent + hinge + reduce)": ph["face"] + ph["tangent"] + ph["hinge"] +
+                       ph["reduce"], "copies": ph["h2d"] + ph["d2h"] + ph["zero"]},
+            "gpu_launches": int(sum(nl.values())),
+            "precision": "FP64 assembly" if not mixed else "FP64 residual + FP32 tangent, one FP64 refinement "
+                                                            "of each Newton step",
+        }
+        del plate, model
+        ctx.close()
+    if with_cpu:
+        # The oracle's restatement of the same run (OpenMP over the host threads).
+        from oracle import Oracle
+        sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests"))
+        import creasing_helpers as H
+
+        o = Oracle(native=True)
+        plate = H.OracleCreasingPlate(o, case.plate, case.spec, case.point_bcs)
+        x = np.zeros(3 * len(case.plate.node_xy))
+        t0 = time.perf_counter()
+        res = PC.run(S.ContinuationSolver(**case.solver_args), plate, x, [case.line], cfg=case.config)
+        wall = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": wall, "unit": "s per run", "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": "the whole run (6 steps), oracle assembly and shape functions, sparse LU KKT",
+                               "last_step": {k: res.steps[-1][k] for k in SMOKE_PUBLISHED} if res.steps else None}
     return out
 
 

@@ -117,6 +117,11 @@ struct cgb_shape {
   cgb::DevBuf<double> rho_node;   // n_nodes (per-node radius) when has_rho_node
   uint64_t node_gen = 0;
   uint64_t version = 0;           // bumped by every rebuild (derived copies go stale)
+  // Scratch of the crease / RKPM stage, kept for the next rebuild (no allocation per step).
+  cgb::DevBuf<double> scr_cxy;    // crease vertices, all creases
+  cgb::DevBuf<int8_t> scr_side;   // n_creases * n_nodes
+  cgb::DevBuf<double> scr_gind;   // n_creases * 6 * n_gp
+  cgb::DevBuf<int8_t> scr_bad;    // n_gp
 };
 
 // Per-fold data kept by the assembler (plate/PlateData.h: Fold; Constraints.h:341).

@@ -556,22 +556,32 @@ void shape_values(cgb_context* ctx, cgb_shape* out, const std::vector<Crease>& c
   const int64_t nnz = out->nnz;
   if (creases.size() > 4) throw Error(CGB_ERR_CAPACITY, "cgb_shape_build: at most 4 creases per call");
   const int nc = static_cast<int>(creases.size());
-  std::vector<DevBuf<double>> cxy(nc);
-  DevBuf<int8_t> side(static_cast<size_t>(std::max(nc, 1)) * n_nodes);
-  DevBuf<double> gind(static_cast<size_t>(std::max(nc, 1)) * 6 * std::max(n_gp, 1));
+  std::vector<double> all_xy;
+  std::vector<size_t> off(nc + 1, 0);
+  for (int c = 0; c < nc; ++c) {
+    all_xy.insert(all_xy.end(), creases[c].xy.begin(), creases[c].xy.end());
+    off[c + 1] = all_xy.size();
+  }
+  out->scr_cxy.ensure(std::max<size_t>(all_xy.size(), 1));
+  out->scr_side.ensure(static_cast<size_t>(std::max(nc, 1)) * n_nodes);
+  out->scr_gind.ensure(static_cast<size_t>(std::max(nc, 1)) * 6 * std::max(n_gp, 1));
+  out->scr_bad.ensure(std::max(n_gp, 1));
+  if (!all_xy.empty())
+    CGB_CUDA(cudaMemcpyAsync(out->scr_cxy.p, all_xy.data(), all_xy.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  int8_t* side = out->scr_side.p;
+  double* gind = out->scr_gind.p;
   std::vector<DevCrease> dcr(nc);
   prof_begin(ctx, CGB_PHASE_CREASE);
   for (int c = 0; c < nc; ++c) {
-    upload(cxy[c], creases[c].xy.data(), creases[c].xy.size(), st);
-    dcr[c] = DevCrease{cxy[c].p, static_cast<int>(creases[c].xy.size() / 2), creases[c].extend_start,
+    dcr[c] = DevCrease{out->scr_cxy.p + off[c], static_cast<int>(creases[c].xy.size() / 2), creases[c].extend_start,
                        creases[c].extend_end, creases[c].is_closed};
     node_side_kernel<<<blocks_for(n_nodes), kThreads, 0, st>>>(n_nodes, ctx->node_xy.p, dcr[c],
-                                                                 side.p + static_cast<int64_t>(c) * n_nodes);
+                                                                 side + static_cast<int64_t>(c) * n_nodes);
   }
   // Gauss-point indicators laid out [g][c][6].
   if (nc > 0 && n_gp > 0)
     for (int c = 0; c < nc; ++c)
-      gp_indicator_kernel<<<blocks_for(n_gp), kThreads, 0, st>>>(n_gp, out->gp_xy.p, dcr[c], c, nc, gind.p);
+      gp_indicator_kernel<<<blocks_for(n_gp), kThreads, 0, st>>>(n_gp, out->gp_xy.p, dcr[c], c, nc, gind);
   prof_end(ctx, CGB_PHASE_CREASE, nc * (1 + (n_gp > 0 ? 1 : 0)));
   CGB_CUDA(cudaGetLastError());
 
@@ -579,10 +589,10 @@ void shape_values(cgb_context* ctx, cgb_shape* out, const std::vector<Crease>& c
   if (out->psi.n < static_cast<size_t>(std::max<int64_t>(nnz, 1))) out->psi.alloc(nnz);
   if (out->dpsi.n < static_cast<size_t>(std::max<int64_t>(2 * nnz, 1))) out->dpsi.alloc(2 * nnz);
   if (out->ddpsi.n < static_cast<size_t>(std::max<int64_t>(3 * nnz, 1))) out->ddpsi.alloc(3 * nnz);
-  DevBuf<int8_t> bad(n_gp);
+  int8_t* bad = out->scr_bad.p;
   RkpmArgs ra{n_gp, n_nodes, out->kernel, nc, out->rho, out->gp_xy.p, ctx->node_xy.p,
-              out->has_rho_node ? out->rho_node.p : nullptr, out->nbr_ptr.p, out->nbr_idx.p, out->s.p, gind.p,
-              side.p, out->psi.p, out->dpsi.p, out->ddpsi.p, bad.p};
+              out->has_rho_node ? out->rho_node.p : nullptr, out->nbr_ptr.p, out->nbr_idx.p, out->s.p, gind,
+              side, out->psi.p, out->dpsi.p, out->ddpsi.p, bad};
   prof_begin(ctx, CGB_PHASE_RKPM);
   if (n_gp > 0) {
     switch (out->order) {
@@ -594,7 +604,7 @@ void shape_values(cgb_context* ctx, cgb_shape* out, const std::vector<Crease>& c
   prof_end(ctx, CGB_PHASE_RKPM, n_gp > 0 ? 1 : 0);
   CGB_CUDA(cudaGetLastError());
   std::vector<int8_t> hbad(n_gp);
-  if (n_gp > 0) CGB_CUDA(cudaMemcpyAsync(hbad.data(), bad.p, n_gp, cudaMemcpyDeviceToHost, st));
+  if (n_gp > 0) CGB_CUDA(cudaMemcpyAsync(hbad.data(), bad, n_gp, cudaMemcpyDeviceToHost, st));
   CGB_CUDA(cudaStreamSynchronize(st));
   // The reference's guards (GlobalRKPM.h:241-257 after the 3x3 block, 347-359 after
   // the bordering): singular first, then pivot collapse.

@@ -717,3 +717,54 @@ def plate_for_mesh(path, crease_tag: int, E: float, nu: float, h: float, stiffne
                              thickness=h, theta0=0.0)
     spec = FoldSpec(fold_sign * angle_target_deg * math.pi / 180.0, crease_tag)
     return p, spec
+
+
+# ---- the reference's centre-crease example (examples/smoke_centre_crease, paperA_centre_crease) --
+
+CENTRE_CREASE = {"E": 96000000.0, "nu": 0.3, "h": 0.005, "crease_tag": 5, "stiffness": 1.098901098901099,
+                 "angle_target": 0.5, "mode": "middle_out", "tip_step": 1, "num_steps": 40,
+                 "fallback_substeps": 4, "L_ref": 1.0,
+                 "guard": {"max_theta_deg": 180.0, "energy_factor": 1e30, "max_motion": 1e30,
+                           "max_motion_topology": 1e30},
+                 "point_bcs": {1: (0.0, 0.0, 0.0), 2: (None, 0.0, 0.0), 4: (None, None, 0.0)},
+                 "ls_max_iters": 500, "tol_force": 1e-10, "tol_energy": 1e-12, "fold_exact_tangent": True}
+
+
+@dataclass
+class CentreCreaseCase:
+    plate: object
+    spec: FoldSpec
+    point_bcs: dict
+    line: Line
+    config: Config
+    solver_args: dict
+
+
+def centre_crease_case(path, n_cells=20, node_xy=None, log_file=None) -> CentreCreaseCase:
+    """The reference's centre-crease run (smoke.json / CB_n80_t0.5_xi1.json): a [-1, 1]^2 sheet
+    of n_cells^2 quadrangles, a crease (-0.5, 0) -> (0.5, 0) of n_cells / 2 segments grown from
+    the centre one segment per step at each end (middle_out), theta0* = 0.5 deg, Kt = D = 1.0989,
+    three corner supports that remove the rigid-body motions, Newton tolerances 1e-10 / 1e-12.
+    The mesh is written to `path`; node_xy replaces the ideal node coordinates (the gmsh
+    coordinates of the reference's own mesh, whose last bits decide on which side of the cut
+    the nodes of the crease line fall)."""
+    from . import mesh
+
+    c = CENTRE_CREASE
+    xy, els = mesh.centre_crease_sheet(n_cells=n_cells, half=1.0, crease_half=0.5, crease_segments=n_cells // 2,
+                                       crease_tag=c["crease_tag"])
+    if node_xy is not None:
+        xy = np.asarray(node_xy, np.float64)
+    mesh.write_msh41(path, xy, els)
+    p, spec = plate_for_mesh(path, c["crease_tag"], c["E"], c["nu"], c["h"], c["stiffness"], c["angle_target"])
+    bcs = {tag: S.BoundaryCondition(u is not None, v is not None, w is not None, u or 0.0, v or 0.0, w or 0.0)
+           for tag, (u, v, w) in c["point_bcs"].items()}
+    g = c["guard"]
+    cfg = Config(num_steps=c["num_steps"], fallback_substeps=c["fallback_substeps"], L_ref=c["L_ref"],
+                 guard_max_theta_deg=g["max_theta_deg"], guard_energy_factor=g["energy_factor"],
+                 guard_max_motion=g["max_motion"], guard_max_motion_topology=g["max_motion_topology"],
+                 log_file=log_file)
+    line = Line(folds=[0], full=p.creases[0], mode=c["mode"], tip_step=c["tip_step"])
+    return CentreCreaseCase(p, spec, bcs, line, cfg,
+                            {"tol_force": c["tol_force"], "tol_energy": c["tol_energy"],
+                             "ls_max_iters": c["ls_max_iters"]})

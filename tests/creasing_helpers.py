@@ -12,37 +12,23 @@ import os
 import numpy as np
 
 from curvami_gb300 import creasing as PC
-from curvami_gb300 import mesh
 from curvami_gb300 import solver as S
 
-# examples/smoke_centre_crease/smoke.json of the reference
-SMOKE = {"E": 96000000.0, "nu": 0.3, "h": 0.005, "crease_tag": 5, "stiffness": 1.098901098901099,
-         "angle_target": 0.5, "mode": "middle_out", "tip_step": 1, "num_steps": 40, "fallback_substeps": 4,
-         "L_ref": 1.0, "guard": {"max_theta_deg": 180.0, "energy_factor": 1e30, "max_motion": 1e30,
-                                 "max_motion_topology": 1e30},
-         "point_bcs": {1: (0.0, 0.0, 0.0), 2: (None, 0.0, 0.0), 4: (None, None, 0.0)},
-         "ls_max_iters": 500, "tol_force": 1e-10, "tol_energy": 1e-12}
+SMOKE = PC.CENTRE_CREASE
 GOLDEN_LAST_STEP = {"step": 5, "E_mem": 4.006e-08, "E_ben": 9.404e-06, "E_hin": 1.594e-05, "theta_mean_deg": 0.1962}
-
-
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def smoke_mesh(path, ideal=False):
-    """The smoke case's mesh: the sheet and crease of centre_crease_sheet() with the node
-    coordinates gmsh wrote for the reference's example (tests/golden/
-    smoke_centre_crease_nodes.npy), or the ideal grid."""
-    xy, els = mesh.centre_crease_sheet(n_cells=20, half=1.0, crease_half=0.5, crease_segments=10, crease_tag=5)
-    if not ideal:
-        xy = np.load(os.path.join(GOLDEN, "smoke_centre_crease_nodes.npy"))
-    mesh.write_msh41(path, xy, els)
-    return path
+def smoke_case(path, ideal=False, log_file=None):
+    """The smoke case (20 x 20 cells) with the node coordinates gmsh wrote for the
+    reference's example (tests/golden/smoke_centre_crease_nodes.npy), or the ideal grid."""
+    xy = None if ideal else np.load(os.path.join(GOLDEN, "smoke_centre_crease_nodes.npy"))
+    return PC.centre_crease_case(path, 20, node_xy=xy, log_file=log_file)
 
 
 def smoke_plate(path, ideal=False):
-    c = SMOKE
-    return PC.plate_for_mesh(smoke_mesh(path, ideal), c["crease_tag"], c["E"], c["nu"], c["h"], c["stiffness"],
-                             c["angle_target"])
+    c = smoke_case(path, ideal)
+    return c.plate, c.spec
 
 
 def smoke_fixture():
@@ -53,19 +39,11 @@ def smoke_fixture():
 
 
 def point_bcs():
-    out = {}
-    for tag, (u, v, w) in SMOKE["point_bcs"].items():
-        out[tag] = S.BoundaryCondition(u is not None, v is not None, w is not None,
-                                       u or 0.0, v or 0.0, w or 0.0)
-    return out
+    return smoke_case("/tmp/_smoke_bcs.msh", ideal=True).point_bcs
 
 
 def smoke_config(log_file=None):
-    g = SMOKE["guard"]
-    return PC.Config(num_steps=SMOKE["num_steps"], fallback_substeps=SMOKE["fallback_substeps"], L_ref=SMOKE["L_ref"],
-                     guard_max_theta_deg=g["max_theta_deg"], guard_energy_factor=g["energy_factor"],
-                     guard_max_motion=g["max_motion"], guard_max_motion_topology=g["max_motion_topology"],
-                     log_file=log_file)
+    return smoke_case("/tmp/_smoke_cfg.msh", ideal=True, log_file=log_file).config
 
 
 def smoke_solver(kkt="host"):
