@@ -313,6 +313,43 @@ def square_plate(n_side: int, h: float, rule: int, *, jitter: float = 0.0, seed:
                        "crease": crease, "split": nsplit})
 
 
+def four_crease_plate(n_side: int = 401, h: float = 0.5, rule: int = 4, seed: int = 1005, Kt: float = 1e-3,
+                      rho_factor: float = 3.5, kernel: int = 0, max_skew_deg: float = 15.0) -> Plate:
+    """n_side x n_side nodes of spacing h jittered by +/-0.2 h, and four straight creases from
+    the centre node to the boundary, the sector angles 90 deg +/- delta (delta ~ U[0, max_skew]
+    per crease, seeded): creases 0 and 2 rigid, 1 and 3 elastic with Kt. Each crease is a
+    polyline of segments about h/2 long, ending at the centre with an end cap and extended
+    at the boundary. rho = 3.5h: a point beside the junction sees only its own sector."""
+    rng = np.random.default_rng(seed)
+    nodes = grid_nodes(n_side, n_side, h, 0.2 * h, rng)
+    c = (n_side // 2) * n_side + n_side // 2
+    centre = nodes[c].copy()
+    faces = quad_gauss_points(nodes, n_side, n_side, rule)
+    hull = convex_hull(_hull_candidates(nodes))
+    lo, hi = nodes.min(0), nodes.max(0)
+    arng = np.random.default_rng([seed, 1])      # the crease directions, apart from the node jitter
+    base = arng.uniform(0.0, 2.0 * math.pi)
+    angles = [base]
+    for k in range(3):
+        angles.append(angles[-1] + math.radians(90.0 + arng.uniform(-max_skew_deg, max_skew_deg)))
+    creases, folds = [], []
+    for k, a in enumerate(angles):
+        d = np.array([math.cos(a), math.sin(a)])
+        # distance from the centre to the boundary box along d
+        tmax = min((hi[i] - centre[i]) / d[i] if d[i] > 0 else (lo[i] - centre[i]) / d[i] if d[i] < 0 else np.inf
+                   for i in range(2))
+        nseg = max(8, int(math.ceil(tmax / (0.5 * h))))
+        verts = centre[None, :] + np.linspace(0.0, tmax, nseg + 1)[:, None] * d[None, :]
+        creases.append(make_crease(verts, nodes, hull))
+        folds.append(make_fold(verts, Kt, 0.0, rigid=(k % 2 == 0)))
+    faces, nsplit = split_on_creases(faces, creases)
+    return Plate(name=f"four_creases{n_side}", node_xy=nodes, faces=faces, creases=creases, folds=folds,
+                 rho=rho_factor * h, order=2, kernel=kernel, seed=seed,
+                 meta={"n_side": n_side, "h": h, "rule": rule, "jitter": 0.2 * h, "crease": "four rays",
+                       "sector_deg": [math.degrees(b - a) for a, b in zip(angles, angles[1:] + [angles[0] + 2 * math.pi])],
+                       "split": nsplit})
+
+
 def config_smallplate(rule: int = 3, kernel: int = 0, seed: int = 1001,
                       rho_factor: float = 3.5) -> Plate:
     """Plain FP64 method, small: [0,20]^2, 41x41 nodes (h = 0.5), quadratic basis,

@@ -91,3 +91,20 @@ def test_autotune_search_and_cache(tmp_path):
     r3 = at.autotune(asm, 1, 2, 3, flags=3, device_name="fake", cache_path=cache, repeats=1,
                      candidates={"n_chunks": (1, 2), "residual_threads": (256,), "tangent_ctas_per_sm": (0,)})
     assert not r3["cached"] and tuple(r3["tuning"]) == (2, 256, 0)
+
+
+def test_four_crease_plate_layout():
+    """Four creases from the centre node to the boundary, sectors 90 +/- 15 deg summing to 360,
+    creases 0 and 2 rigid, an end cap at the centre and an extension at the boundary."""
+    import math
+    from curvami_gb300 import synth
+
+    p = synth.four_crease_plate(41, rule=2, seed=1005)
+    assert len(p.creases) == 4 and len(p.folds) == 4
+    sec = p.meta["sector_deg"]
+    assert abs(sum(sec) - 360.0) < 1e-9 and all(60.0 <= a <= 150.0 for a in sec[:3])
+    c = p.node_xy[(41 // 2) * 41 + 41 // 2]
+    for cr in p.creases:
+        assert np.allclose(cr["vertices"][0], c) and not cr["extend_start"] and cr["extend_end"]
+    assert [f.rigid for f in p.folds] == [True, False, True, False]
+    assert len(p.faces.xy) == 40 * 40 * 4
