@@ -401,6 +401,7 @@ def run_gpu(args):
     v_f64 = world * n_gp / (ms_f64 * 1e-3)
     shape = None if args.no_shape_stage else shape_stage(cg, ctx, args, rank == 0 and not args.no_cpu_baseline)
     creasing = None if args.no_shape_stage else creasing_run(rank == 0 and not args.no_cpu_baseline)
+    post = None if args.no_shape_stage else post_processing(cg, ctx, model, x_d, stream)
     four = None
     if not args.no_shape_stage:
         try:
@@ -438,6 +439,7 @@ def run_gpu(args):
         "shape_stage": shape,
         "progressive_creasing": creasing,
         "four_creases": four,
+        "post_processing": post,
     }
     if rank == 0:
         print(json.dumps(line))
@@ -564,6 +566,56 @@ def shape_stage(cg, ctx, args, with_cpu):
             "psi": rel(d["psi"][:e], psi), "dpsi": rel(d["dpsi"][:e].reshape(-1), dpsi.reshape(-1)),
             "ddpsi": rel(d["ddpsi"][:e].reshape(-1), ddpsi.reshape(-1)), "sample_points": m}
     return out
+
+
+# ---------------------------------------------------------------------------------
+# Post-processing: the kinematic state of every face Gauss point (exporter / sampler)
+# ---------------------------------------------------------------------------------
+
+def post_processing(cg, ctx, model, x_d, stream):
+    """cgb_point_state_device over the 640,000 face Gauss points of the workload: per point
+    the displacement sum and Kinematics::compute + Constitutive::evaluate in FP64 (18 FMA
+    per neighbour), 33 doubles out. Timed with CUDA events; roofline against the FP64 FMA
+    peak (measured live) and HBM."""
+    import torch
+    from curvami_gb300 import _lib as L
+
+    S = model.faces
+    n = S.n_gp
+    out = torch.empty((n, L.POINT_STATE_COLS), dtype=torch.float64, device="cuda")
+    A, B, D = (np.ascontiguousarray(M, np.float64).reshape(9) for M in (model.asm.A, model.asm.B, model.asm.D))
+
+    def call():
+        ctx.check(ctx.lib.cgb_point_state_device(ctx.h, S.h, ctx_ptr(x_d), A.ctypes.data, B.ctypes.data,
+                                                 D.ctypes.data, ctx_ptr(out)))
+
+    def ctx_ptr(t):
+        return __import__("ctypes").c_void_p(t.data_ptr())
+
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record(stream)
+    for _ in range(reps):
+        call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nnz = S.nnz
+    flops = 2.0 * 18 * nnz          # Psi u (3) + the 15 kinematic sums per neighbour
+    bytes_ = nnz * (4 + 8 + 16 + 24 + 24) + n * (8 + 33 * 8)
+    p64, _ = fma_peaks(torch.cuda.current_device())
+    peaks, kind = measured_peaks()
+    return {"what": "cgb_point_state_device, 640,000 face Gauss points (Exporter rows / StressSampler state)",
+            "ms": ms, "points_per_s": n / (ms * 1e-3),
+            "fp64_tflops": flops / (ms * 1e-3) / 1e12,
+            "fp64_frac": (flops / (ms * 1e-3) / 1e12) / p64 if p64 > 0 else None,
+            "algorithmic_GBps": bytes_ / (ms * 1e-3) / 1e9,
+            "hbm_frac": bytes_ / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"], "peak_source": kind,
+            "bytes_per_point": bytes_ / n, "flops_per_point": flops / n}
 
 
 # ---------------------------------------------------------------------------------

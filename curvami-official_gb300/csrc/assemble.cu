@@ -864,6 +864,49 @@ __global__ void __launch_bounds__(128) face_energy_kernel(int n_gp, const int64_
   if (lane == 0) { atomicAdd(out, em); atomicAdd(out + 1, eb); }
 }
 
+// ---- kinematic state of arbitrary points (post-processing) ---------------------------
+// One thread per point: the displacement sum_I Psi_I u_I and Kinematics::compute /
+// Constitutive::evaluate (plate/Kinematics.h:61-120, Constitutive.h:57-70) in FP64, one row
+// of kPointStateCols per point: u(3) r_X(3) r_Y(3) r_XX(3) r_YY(3) r_XY(3) b(3)
+// E0 (xx yy xy, tensor) E1 (xx yy xy, tensor) N (Voigt) M (Voigt).
+constexpr int kPointStateCols = 33;
+__global__ void __launch_bounds__(128) point_state_kernel(int n, const int64_t* __restrict__ ptr,
+                                                          const int32_t* __restrict__ idx,
+                                                          const double* __restrict__ psi,
+                                                          const double* __restrict__ dpsi,
+                                                          const double* __restrict__ ddpsi,
+                                                          const double* __restrict__ x, Material m,
+                                                          double* __restrict__ out) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  double s[15], u[3] = {0.0, 0.0, 0.0};
+  for (int k = 0; k < 15; ++k) s[k] = 0.0;
+  for (int64_t e = ptr[g]; e < ptr[g + 1]; ++e) {
+    const int64_t j = idx[e];
+    const double u0 = x[3 * j], u1 = x[3 * j + 1], u2 = x[3 * j + 2];
+    const double p = psi[e], dx = dpsi[2 * e], dy = dpsi[2 * e + 1];
+    const double dxx = ddpsi[3 * e], dyy = ddpsi[3 * e + 1], dxy = ddpsi[3 * e + 2];
+    u[0] += p * u0; u[1] += p * u1; u[2] += p * u2;
+    s[0] += u0 * dx; s[1] += u1 * dx; s[2] += u2 * dx;
+    s[3] += u0 * dy; s[4] += u1 * dy; s[5] += u2 * dy;
+    s[6] += u0 * dxx; s[7] += u1 * dxx; s[8] += u2 * dxx;
+    s[9] += u0 * dyy; s[10] += u1 * dyy; s[11] += u2 * dyy;
+    s[12] += u0 * dxy; s[13] += u1 * dxy; s[14] += u2 * dxy;
+  }
+  PointState P;
+  point_state(s, m, P);
+  double* o = out + static_cast<int64_t>(g) * kPointStateCols;
+  for (int c = 0; c < 3; ++c) {
+    o[c] = u[c];
+    o[3 + c] = P.a1[c]; o[6 + c] = P.a2[c];
+    o[9 + c] = P.rxx[c]; o[12 + c] = P.ryy[c]; o[15 + c] = P.rxy[c];
+    o[18 + c] = P.b[c];
+    o[27 + c] = P.N[c]; o[30 + c] = P.M[c];
+  }
+  o[21] = P.e0[0]; o[22] = P.e0[1]; o[23] = 0.5 * P.e0[2];
+  o[24] = P.e1[0]; o[25] = P.e1[1]; o[26] = 0.5 * P.e1[2];
+}
+
 __global__ void hinge_energy_kernel(HingeArgs a, double* out) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= a.n_gp) return;
@@ -1612,6 +1655,17 @@ void face_mixed_on_arrays(const cgb_face_problem& pr, const double* d_x, double*
   }
   const unsigned cg = std::max(1u, std::min(nb(pr.n_nodes, 4), static_cast<unsigned>(sms * 32)));
   blocks_to_csc_outer<float, 12><<<cg, 128, 0, st>>>(pr.n_nodes, pr.outer, kacc, d_K);
+  CGB_CUDA(cudaGetLastError());
+}
+
+void point_state_device(cgb_context* ctx, const cgb_shape* S, const double* d_x, const double* A, const double* B,
+                        const double* D, double* d_out) {
+  if (S->n_gp == 0) return;
+  if (!S->psi.p || S->psi.n < static_cast<size_t>(std::max<int64_t>(S->nnz, 1)))
+    throw Error(CGB_ERR_INVALID, "point state: the shape set has no Psi");
+  const Material m = make_material(A, B, D);
+  point_state_kernel<<<nb(S->n_gp, 128), 128, 0, ctx->stream>>>(S->n_gp, S->nbr_ptr.p, S->nbr_idx.p, S->psi.p,
+                                                                S->dpsi.p, S->ddpsi.p, d_x, m, d_out);
   CGB_CUDA(cudaGetLastError());
 }
 

@@ -583,6 +583,36 @@ int cgb_assemble(cgb_assembler* a, const double* x, double* K_values, double* F,
   });
 }
 
+int cgb_point_state_device(cgb_context* ctx, const cgb_shape* pts, const double* d_x, const double* A,
+                           const double* B, const double* D, double* d_out) {
+  if (!ctx) return CGB_ERR_INVALID;
+  return guarded(ctx, [&] {
+    need(pts && pts->ctx == ctx, "cgb_point_state: the shape set must come from this context");
+    need(A && B && D && (pts->n_gp == 0 || (d_x && d_out)), "cgb_point_state: NULL argument");
+    bind_device(ctx);
+    cgb::point_state_device(ctx, pts, d_x, A, B, D, d_out);
+  });
+}
+
+int cgb_point_state(cgb_context* ctx, const cgb_shape* pts, const double* x, const double* A, const double* B,
+                    const double* D, double* out) {
+  if (!ctx) return CGB_ERR_INVALID;
+  return guarded(ctx, [&] {
+    need(pts && pts->ctx == ctx, "cgb_point_state: the shape set must come from this context");
+    need(A && B && D && (pts->n_gp == 0 || (x && out)), "cgb_point_state: NULL argument");
+    need(ctx->n_nodes > 0, "cgb_point_state: nodes not set");
+    bind_device(ctx);
+    cudaStream_t st = ctx->stream;
+    const size_t nx = 3 * static_cast<size_t>(ctx->n_nodes);
+    const size_t no = static_cast<size_t>(pts->n_gp) * CGB_POINT_STATE_COLS;
+    cgb::DevBuf<double> dx(nx), dout(std::max<size_t>(no, 1));
+    CGB_CUDA(cudaMemcpyAsync(dx.p, x, nx * sizeof(double), cudaMemcpyHostToDevice, st));
+    cgb::point_state_device(ctx, pts, dx.p, A, B, D, dout.p);
+    if (no) CGB_CUDA(cudaMemcpyAsync(out, dout.p, no * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
 int cgb_energies(cgb_assembler* a, const double* x, double* E_mem, double* E_ben, double* E_hin) {
   if (!a) return CGB_ERR_INVALID;
   return guarded(a->ctx, [&] {

@@ -247,6 +247,9 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
 // face set (no-op when they are current); enqueued on the context stream.
 void refresh_face_copies(cgb_assembler* a);
 void energies_device(cgb_assembler* a, const double* d_x, double* out3);
+// Kinematic state rows (CGB_POINT_STATE_COLS per point) of a shape set at device x.
+void point_state_device(cgb_context* ctx, const cgb_shape* S, const double* d_x, const double* A, const double* B,
+                        const double* D, double* d_out);
 void face_mixed_on_arrays(const cgb_face_problem& pr, const double* d_x, double* d_K, double* d_F,
                           float* kacc, cudaStream_t st);
 }  // namespace cgb

@@ -60,6 +60,8 @@ SIGNATURES = {
     "cgb_assemble_device": (i32, [vp, vp, vp, vp, i32]),
     "cgb_energies": (i32, [vp, vp, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(dbl)]),
     "cgb_assemble_face_noalloc": (i32, [vp, vp, vp, vp, vp]),
+    "cgb_point_state": (i32, [vp, vp, vp, vp, vp, vp, vp]),
+    "cgb_point_state_device": (i32, [vp, vp, vp, vp, vp, vp, vp]),
     "cgb_profile_enable": (i32, [vp, i32]),
     "cgb_profile_read": (i32, [vp, vp, vp, i32]),
 }
@@ -86,6 +88,7 @@ class Fold(C.Structure):
 
 
 NOALLOC_MAX_BLOCKS = 699050
+POINT_STATE_COLS = 33
 
 
 class FaceProblem(C.Structure):

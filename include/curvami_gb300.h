@@ -179,6 +179,22 @@ int cgb_assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double
 int cgb_energies(cgb_assembler* a, const double* x, double* E_mem, double* E_ben,
                  double* E_hin);
 
+/* ---- post-processing: the kinematic state of any point set --------------------------- */
+/* Kinematics::compute + Constitutive::evaluate (plate/Kinematics.h:61-120,
+ * plate/Constitutive.h:57-70) and the displacement sum_I Psi_I u_I at every point of a shape
+ * set (face Gauss points, crease points, or sample points built with cgb_shape_build), for
+ * the step exporter (Exporter::writeBinaryStep, plate/Exporter.h:27-92) and the stress
+ * sampler (StressSampler::report, plate/StressSampler.h:79-170). Row-major, per point:
+ * u(3), r_X(3), r_Y(3), r_XX(3), r_YY(3), r_XY(3), b(3), E0_xx E0_yy E0_xy (tensor),
+ * E1_xx E1_yy E1_xy (tensor, the curvature), N(3, Voigt), M(3, Voigt); FP64. A, B, D row-major
+ * 3x3 (LaminateProperties). x: 3 n_nodes. The set must carry Psi. */
+#define CGB_POINT_STATE_COLS 33
+int cgb_point_state(cgb_context* ctx, const cgb_shape* pts, const double* x, const double* A, const double* B,
+                    const double* D, double* out);
+/* Same with device pointers, asynchronous on the context stream. */
+int cgb_point_state_device(cgb_context* ctx, const cgb_shape* pts, const double* d_x, const double* A,
+                           const double* B, const double* D, double* d_out);
+
 /* ---- allocation-free face assembly -------------------------------------------------- */
 /* No counterpart in the reference. It serves callers that cannot allocate GPU memory
  * while they assemble: cudaMalloc / cudaFree may synchronise the whole device (stalling
