@@ -541,6 +541,7 @@ def shape_stage(cg, ctx, args, with_cpu):
                     "what": "cgb_shape_rebuild of the same set for a moved cut (progressive creasing's "
                             "per-step stage A), alternating the half and the full cut"},
     }
+    out["mixed"] = shape_stage_mixed(cg, ctx, plate, pts, kw, steps, d, cuts)
     if with_cpu:
         # The oracle's restatement of GlobalFRNN::execute + GlobalRKPM::solve (OpenMP, all
         # host threads) on the first 20,000 points, and the GPU's difference from it there.
@@ -565,7 +566,66 @@ def shape_stage(cg, ctx, args, with_cpu):
             "neighbours_bit_exact": same,
             "psi": rel(d["psi"][:e], psi), "dpsi": rel(d["dpsi"][:e].reshape(-1), dpsi.reshape(-1)),
             "ddpsi": rel(d["ddpsi"][:e].reshape(-1), ddpsi.reshape(-1)), "sample_points": m}
+        dm = out["mixed"].pop("_values")
+        out["mixed"]["error_vs_oracle"] = {
+            "psi": rel(dm["psi"][:e], psi), "dpsi": rel(dm["dpsi"][:e].reshape(-1), dpsi.reshape(-1)),
+            "ddpsi": rel(dm["ddpsi"][:e].reshape(-1), ddpsi.reshape(-1)), "sample_points": m}
+    out["mixed"].pop("_values", None)
     return out
+
+
+def shape_stage_mixed(cg, ctx, plate, pts, kw, steps, d64, cuts):
+    """The same 1,000,000-point build with the mixed-precision RKPM (per-neighbour sums in
+    FP32 pairs on the FP32 pipe, per-point factorisation in FP64): time per build, per
+    phase, per rebuild, the reproducing-condition error, and the difference from the FP64
+    build of the same points (relative to each array's scale; over all points, and over
+    the points whose support the cut does not reach)."""
+    mkw = dict(kw, precision="mixed")
+    for _ in range(3):
+        cg.shape_functions(ctx, pts, **mkw)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sh = cg.shape_functions(ctx, pts, **mkw)
+    wall = (time.perf_counter() - t0) / steps
+    ctx.profile(True)
+    ctx.profile_read(reset=True)
+    sh = cg.shape_functions(ctx, pts, **mkw)
+    ph, _ = ctx.profile_read(reset=True)
+    ctx.profile(False)
+    dm = sh.download()
+    for c in cuts:
+        sh.rebuild(c)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for i in range(2 * steps):
+        sh.rebuild(cuts[i % 2])
+    ctx.synchronize()
+    wall_rb = (time.perf_counter() - t0) / (2 * steps)
+    # Points whose support the cut y = 100 does not reach (largest radius 3.5h = 1.75).
+    far_pt = np.abs(pts[:, 1] - 100.0) > 1.75 + 0.2
+    far = np.repeat(far_pt, np.diff(d64["ptr"]))
+
+    def rel(a, b, mask=None):
+        if mask is not None:
+            a, b = a[mask], b[mask]
+        return float(np.abs(a - b).max() / np.abs(b).max())
+
+    err = {}
+    for k, m in (("psi", 1), ("dpsi", 2), ("ddpsi", 3)):
+        a, b = dm[k].reshape(-1), d64[k].reshape(-1)
+        err[k] = {"all": rel(a, b), "away_from_cut": rel(a, b, np.repeat(far, m))}
+    return {
+        "precision": "mixed (per-neighbour sums in FP32 pairs, per-point LDL^T and solves in FP64)",
+        "value": len(pts) / wall, "unit": "points/s", "ms_per_build": wall * 1e3,
+        "phases_ms": {k: ph[k] for k in ("frnn", "crease", "rkpm")},
+        "rkpm_points_per_s": len(pts) / (ph["rkpm"] * 1e-3) if ph["rkpm"] > 0 else None,
+        "reproducing_error": reproducing_error(dm, plate.node_xy, pts, 1.5),
+        "error_vs_fp64_gpu": err,
+        "neighbours_same_as_fp64": bool(np.array_equal(dm["idx"], d64["idx"])),
+        "rebuild": {"ms_per_rebuild": wall_rb * 1e3, "points_per_s": len(pts) / wall_rb},
+        "_values": dm,
+    }
 
 
 # ---------------------------------------------------------------------------------

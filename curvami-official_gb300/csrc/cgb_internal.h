@@ -113,6 +113,7 @@ struct cgb_shape {
   bool rebuildable = false;
   double rho = 0.0;
   int order = 0, kernel = 0;
+  int precision = 0;              // CGB_SHAPE_FP64 / CGB_SHAPE_MIXED
   bool has_rho_node = false;
   cgb::DevBuf<double> rho_node;   // n_nodes (per-node radius) when has_rho_node
   uint64_t node_gen = 0;
@@ -122,6 +123,7 @@ struct cgb_shape {
   cgb::DevBuf<int8_t> scr_side;   // n_creases * n_nodes
   cgb::DevBuf<double> scr_gind;   // n_creases * 6 * n_gp
   cgb::DevBuf<int8_t> scr_bad;    // n_gp
+  cgb::DevBuf<float4> scr_node_pair;  // 2 * n_nodes, mixed precision only
 };
 
 // Per-fold data kept by the assembler (plate/PlateData.h: Fold; Constraints.h:341).

@@ -21,6 +21,7 @@
 
 #include "cgb_device.cuh"
 #include "cgb_internal.h"
+#include "cgb_pair.cuh"
 
 namespace cgb {
 namespace {
@@ -239,71 +240,31 @@ struct RawIdx {
   __host__ __device__ static constexpr int bx(int i) { return deg(i) - by(i); }
 };
 
-struct RkpmArgs {
-  int n_gp, n_nodes, kernel, n_creases;
-  double rho;
-  const double* gp_xy;
-  const double* node_xy;
-  const double* rho_node;
-  const int64_t* ptr;
-  const int32_t* idx;
-  const double* s;
-  const double* gind;        // 6 * n_creases per Gauss point
-  const int8_t* node_side;   // n_creases * n_nodes
-  double* psi;
-  double* dpsi;
-  double* ddpsi;
-  int8_t* bad;
+// Row 0 of M^-1 and its five jets at one point.
+template <int ORDER>
+struct RowJets {
+  static constexpr int NP = (ORDER + 1) * (ORDER + 2) / 2;
+  double c0[NP], c0x[NP], c0y[NP], c0xx[NP], c0yy[NP], c0xy[NP];
 };
 
-// One Gauss point per thread: GlobalRKPM.h:59-397 for that point.
+// The per-point part of GlobalRKPM::solve (GlobalRKPM.h:161-359) from the raw-moment sums
+// S^g_ab of the six weight jets (FP64): M and its jets, the reference's guards, and row 0
+// of M^-1 with its jets. Returns the guard code (0 fine, 1 singular, 2 pivot collapse).
+//
+// Moments (GlobalRKPM.h:161-189): M, dMx, dMy, d2Mxx, d2Myy, d2Mxy. Every entry of
+// M = sum_I w_I p_I p_I^T is a raw moment mu_ab = sum_I w_I xi^a eta^b with
+// a + b <= 2 ORDER, and the jets follow from the weight jets by the product rule,
+//   D_x mu_ab = S^x_ab + a S_{a-1,b},   D_xx mu_ab = S^xx_ab + 2a S^x_{a-1,b} + a(a-1) S_{a-2,b},
+//   D_xy mu_ab = S^xy_ab + b S^x_{a,b-1} + a S^y_{a-1,b} + ab S_{a-1,b-1}   (y alike),
+// with S^g_ab = sum_I (D^g w_I) xi^a eta^b.
 template <int ORDER>
-__global__ void __launch_bounds__(kThreads) rkpm_kernel(RkpmArgs a) {
+__device__ __forceinline__ int point_solve(const double* S0, const double* Sx, const double* Sy,
+                                           const double* Sxx, const double* Syy, const double* Sxy,
+                                           RowJets<ORDER>& R) {
   constexpr int NP = (ORDER + 1) * (ORDER + 2) / 2;
   constexpr int NM = NP * (NP + 1) / 2;
   using PI = PackedIdx<NP>;
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= a.n_gp) return;
-  const int64_t p0 = a.ptr[g], p1 = a.ptr[g + 1];
-  const double gx = a.gp_xy[2 * g], gy = a.gp_xy[2 * g + 1];
-  double gind[6 * 4];
-  const int nc = a.n_creases < 4 ? a.n_creases : 4;
-  for (int c = 0; c < 6 * nc; ++c) gind[c] = a.gind[static_cast<int64_t>(g) * 6 * a.n_creases + c];
-
-  // Moments (GlobalRKPM.h:161-189): M, dMx, dMy, d2Mxx, d2Myy, d2Mxy. Every entry of
-  // M = sum_I w_I p_I p_I^T is a raw moment mu_ab = sum_I w_I xi^a eta^b with
-  // a + b <= 2 ORDER, and the jets follow from the weight jets by the product rule,
-  //   D_x mu_ab = S^x_ab + a S_{a-1,b},   D_xx mu_ab = S^xx_ab + 2a S^x_{a-1,b} + a(a-1) S_{a-2,b},
-  //   D_xy mu_ab = S^xy_ab + b S^x_{a,b-1} + a S^y_{a-1,b} + ab S_{a-1,b-1}   (y alike),
-  // with S^g_ab = sum_I (D^g w_I) xi^a eta^b. Accumulating the 6 x NR sums S per neighbour
-  // (90 FMA for ORDER 2) replaces the 6 x NM jets of p_i p_j (about 6x the FP64 work);
-  // M and its jets are formed once per point.
   using RI = RawIdx<ORDER>;
-  constexpr int NR = RI::NR;
-  double S0[NR], Sx[NR], Sy[NR], Sxx[NR], Syy[NR], Sxy[NR];
-#pragma unroll
-  for (int k = 0; k < NR; ++k) { S0[k] = 0; Sx[k] = 0; Sy[k] = 0; Sxx[k] = 0; Syy[k] = 0; Sxy[k] = 0; }
-  for (int64_t e = p0; e < p1; ++e) {
-    const int j = a.idx[e];
-    const double xi = (gx - a.node_xy[2 * j]) / a.rho;
-    const double eta = (gy - a.node_xy[2 * j + 1]) / a.rho;
-    const double fac = a.rho_node ? a.rho / a.rho_node[j] : 1.0;
-    const Jets J = weight_jets(a.kernel, xi, eta, a.s[e], fac, nc, gind, a.node_side, a.n_nodes, j, a.rho);
-    double xp[RI::D + 1], yp[RI::D + 1];
-    xp[0] = 1.0; yp[0] = 1.0;
-#pragma unroll
-    for (int q = 1; q <= RI::D; ++q) { xp[q] = xp[q - 1] * xi; yp[q] = yp[q - 1] * eta; }
-#pragma unroll
-    for (int d = 0; d <= RI::D; ++d) {
-#pragma unroll
-      for (int b = 0; b <= d; ++b) {
-        const int k = RI::r(d - b, b);
-        const double m = xp[d - b] * yp[b];
-        S0[k] += J.w * m; Sx[k] += J.x * m; Sy[k] += J.y * m;
-        Sxx[k] += J.xx * m; Syy[k] += J.yy * m; Sxy[k] += J.xy * m;
-      }
-    }
-  }
   double M[NM], Mx[NM], My[NM], Mxx[NM], Myy[NM], Mxy[NM];
   {
     auto at = [](const double* S, int aa, int bb) { return (aa < 0 || bb < 0) ? 0.0 : S[RI::r(aa, bb)]; };
@@ -374,7 +335,6 @@ __global__ void __launch_bounds__(kThreads) rkpm_kernel(RkpmArgs a) {
       Lf[i][j] = v * iD[j];
     }
   }
-  a.bad[g] = static_cast<int8_t>(bad);
   // x <- M^-1 x in place.
   auto solve = [&](double* x) {
 #pragma unroll
@@ -398,7 +358,12 @@ __global__ void __launch_bounds__(kThreads) rkpm_kernel(RkpmArgs a) {
       y[i] += alpha * t;
     }
   };
-  double c0[NP], c0x[NP], c0y[NP], c0xx[NP], c0yy[NP], c0xy[NP];
+  double(&c0)[NP] = R.c0;
+  double(&c0x)[NP] = R.c0x;
+  double(&c0y)[NP] = R.c0y;
+  double(&c0xx)[NP] = R.c0xx;
+  double(&c0yy)[NP] = R.c0yy;
+  double(&c0xy)[NP] = R.c0xy;
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
     c0[i] = i == 0 ? 1.0 : 0.0;
@@ -410,6 +375,77 @@ __global__ void __launch_bounds__(kThreads) rkpm_kernel(RkpmArgs a) {
   symv(Mxx, c0, -1.0, c0xx); symv(Mx, c0x, -2.0, c0xx); solve(c0xx);
   symv(Myy, c0, -1.0, c0yy); symv(My, c0y, -2.0, c0yy); solve(c0yy);
   symv(Mxy, c0, -1.0, c0xy); symv(Mx, c0y, -1.0, c0xy); symv(My, c0x, -1.0, c0xy); solve(c0xy);
+  return bad;
+}
+
+struct RkpmArgs {
+  int n_gp, n_nodes, kernel, n_creases;
+  double rho;
+  const float4* node_pair;   // mixed kernel: 2 per node (node_pair_kernel)
+  fp2 irho, irho2;           // mixed kernel: 1 / rho and 1 / rho^2 as pairs
+  const double* gp_xy;
+  const double* node_xy;
+  const double* rho_node;
+  const int64_t* ptr;
+  const int32_t* idx;
+  const double* s;
+  const double* gind;        // 6 * n_creases per Gauss point
+  const int8_t* node_side;   // n_creases * n_nodes
+  double* psi;
+  double* dpsi;
+  double* ddpsi;
+  int8_t* bad;
+};
+
+// One Gauss point per thread: GlobalRKPM.h:59-397 for that point.
+template <int ORDER>
+__global__ void __launch_bounds__(kThreads) rkpm_kernel(RkpmArgs a) {
+  constexpr int NP = (ORDER + 1) * (ORDER + 2) / 2;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= a.n_gp) return;
+  const int64_t p0 = a.ptr[g], p1 = a.ptr[g + 1];
+  const double gx = a.gp_xy[2 * g], gy = a.gp_xy[2 * g + 1];
+  double gind[6 * 4];
+  const int nc = a.n_creases < 4 ? a.n_creases : 4;
+  for (int c = 0; c < 6 * nc; ++c) gind[c] = a.gind[static_cast<int64_t>(g) * 6 * a.n_creases + c];
+
+  // Raw-moment sums S^g_ab of the six weight jets (see point_solve). Accumulating the
+  // 6 x NR sums per neighbour (90 FMA for ORDER 2) replaces the 6 x NM jets of p_i p_j
+  // (about 6x the FP64 work); M and its jets are formed once per point.
+  using RI = RawIdx<ORDER>;
+  constexpr int NR = RI::NR;
+  double S0[NR], Sx[NR], Sy[NR], Sxx[NR], Syy[NR], Sxy[NR];
+#pragma unroll
+  for (int k = 0; k < NR; ++k) { S0[k] = 0; Sx[k] = 0; Sy[k] = 0; Sxx[k] = 0; Syy[k] = 0; Sxy[k] = 0; }
+  for (int64_t e = p0; e < p1; ++e) {
+    const int j = a.idx[e];
+    const double xi = (gx - a.node_xy[2 * j]) / a.rho;
+    const double eta = (gy - a.node_xy[2 * j + 1]) / a.rho;
+    const double fac = a.rho_node ? a.rho / a.rho_node[j] : 1.0;
+    const Jets J = weight_jets(a.kernel, xi, eta, a.s[e], fac, nc, gind, a.node_side, a.n_nodes, j, a.rho);
+    double xp[RI::D + 1], yp[RI::D + 1];
+    xp[0] = 1.0; yp[0] = 1.0;
+#pragma unroll
+    for (int q = 1; q <= RI::D; ++q) { xp[q] = xp[q - 1] * xi; yp[q] = yp[q - 1] * eta; }
+#pragma unroll
+    for (int d = 0; d <= RI::D; ++d) {
+#pragma unroll
+      for (int b = 0; b <= d; ++b) {
+        const int k = RI::r(d - b, b);
+        const double m = xp[d - b] * yp[b];
+        S0[k] += J.w * m; Sx[k] += J.x * m; Sy[k] += J.y * m;
+        Sxx[k] += J.xx * m; Syy[k] += J.yy * m; Sxy[k] += J.xy * m;
+      }
+    }
+  }
+  RowJets<ORDER> R;
+  a.bad[g] = static_cast<int8_t>(point_solve<ORDER>(S0, Sx, Sy, Sxx, Syy, Sxy, R));
+  const double(&c0)[NP] = R.c0;
+  const double(&c0x)[NP] = R.c0x;
+  const double(&c0y)[NP] = R.c0y;
+  const double(&c0xx)[NP] = R.c0xx;
+  const double(&c0yy)[NP] = R.c0yy;
+  const double(&c0xy)[NP] = R.c0xy;
   // Shape functions (GlobalRKPM.h:363-396).
   const double rho2 = a.rho * a.rho;
   for (int64_t e = p0; e < p1; ++e) {
@@ -438,6 +474,300 @@ __global__ void __launch_bounds__(kThreads) rkpm_kernel(RkpmArgs a) {
   }
 }
 
+
+// ---- mixed precision: the per-neighbour work in FP32 pairs ----------------------------
+//
+// The FP64 kernel spends about 650 FP64 operations per neighbour (differences and
+// divisions by rho, the window jets with their divisions by s, the crease product, the
+// 90 moment FMAs, then the jets again and the shape-function sums), and GB300 issues FP64
+// at 1/62 of the FP32 rate. rkpm_pair_kernel does all of that per-neighbour arithmetic in
+// FP32 pairs (cgb_pair.cuh, about 48 significant bits) on the FP32 pipe, and keeps FP64
+// for the per-point part: the raw-moment sums are rounded to FP64 and point_solve forms
+// M and its jets, applies the reference's guards, factors M (LDL^T) and solves for row 0
+// of M^-1 and its jets exactly as the FP64 kernel does. Only the per-point factorisation
+// is FP64, which is 1/n of the work; the shape functions are then summed in pairs from the
+// FP64 row jets and rounded to FP64 once.
+//
+// Coordinates: node and point coordinates are split into three floats each (72 bits, so
+// the split of a double is exact) and differenced in pairs, so xi = (x - x_I) / rho is
+// accurate to the pair precision relative to xi itself, not to the coordinates' size.
+
+__device__ __forceinline__ void split3(double v, float& a, float& b, float& c) {
+  a = __double2float_rn(v);
+  const double r = v - static_cast<double>(a);
+  b = __double2float_rn(r);
+  c = __double2float_rn(r - static_cast<double>(b));
+}
+
+// Per node: {x0, x1, x2, y0}, {y1, y2, fac.hi, fac.lo} with x = x0 + x1 + x2 and
+// fac = rho / rho_I (1 for the single radius).
+__global__ void node_pair_kernel(int n_nodes, const double* __restrict__ node_xy,
+                                 const double* __restrict__ rho_node, double rho, float4* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_nodes) return;
+  float x0, x1, x2, y0, y1, y2;
+  split3(node_xy[2 * j], x0, x1, x2);
+  split3(node_xy[2 * j + 1], y0, y1, y2);
+  const fp2 fac = rho_node ? fp2_from_double(rho / rho_node[j]) : fp2{1.0f, 0.0f};
+  out[2 * j] = make_float4(x0, x1, x2, y0);
+  out[2 * j + 1] = make_float4(y1, y2, fac.hi, fac.lo);
+}
+
+// (a0 + a1 + a2) - (b0 + b1 + b2) as a pair.
+__device__ __forceinline__ fp2 diff3(float a0, float a1, float a2, float b0, float b1, float b2) {
+  const fp2 h = fp2_two_sum(a0, -b0);
+  const fp2 m = fp2_two_sum(a1, -b1);
+  return fp2_add_exact(h, m) + __fsub_rn(a2, b2);
+}
+
+constexpr float kTwoThirdsHi = static_cast<float>(2.0 / 3.0);
+constexpr float kTwoThirdsLo = static_cast<float>(2.0 / 3.0 - static_cast<double>(kTwoThirdsHi));
+constexpr float kFourThirdsHi = static_cast<float>(4.0 / 3.0);
+constexpr float kFourThirdsLo = static_cast<float>(4.0 / 3.0 - static_cast<double>(kFourThirdsHi));
+
+// window() in pairs, same branches and cut-offs, polynomials in Horner form.
+__device__ __forceinline__ void window_pair(int kernel, fp2 s, fp2& w, fp2& dw, fp2& d2w) {
+  const fp2 z{0.0f, 0.0f};
+  if (fp2_ge(s, 1.0f)) { w = z; dw = z; d2w = z; return; }
+  const bool tiny = s.hi < 1e-14f;
+  if (kernel == 0) {  // 1 - 6 s^2 + 8 s^3 - 3 s^4
+    const fp2 s2 = fp2_sqr(s);
+    w = 1.0f + s2 * (-6.0f + s * (8.0f - 3.0f * s));
+    dw = tiny ? z : s * (-12.0f + s * (24.0f - 12.0f * s));
+    d2w = -12.0f + s * (48.0f - 36.0f * s);
+  } else if (fp2_le(s, 0.5f)) {  // 2/3 - 4 s^2 + 4 s^3
+    const fp2 s2 = fp2_sqr(s);
+    w = fp2{kTwoThirdsHi, kTwoThirdsLo} + s2 * (-4.0f + 4.0f * s);
+    dw = tiny ? z : s * (-8.0f + 12.0f * s);
+    d2w = -8.0f + 24.0f * s;
+  } else {  // 4/3 (1 - s)^3
+    const fp2 r = 1.0f - s;
+    const fp2 r2 = fp2_sqr(r);
+    w = fp2{kFourThirdsHi, kFourThirdsLo} * (r2 * r);
+    dw = -4.0f * r2;
+    d2w = 8.0f * r;
+  }
+}
+
+// weight_jets() in pairs: jets v = {w, x, y, xx, yy, xy}. gc holds per crease
+// 0.5 I_f, 0.5 I_gx rho, 0.5 I_gy rho, 0.5 I_hxx rho^2, 0.5 I_hyy rho^2, 0.5 I_hxy rho^2.
+struct JetsP {
+  fp2 v[6];
+};
+__device__ __forceinline__ JetsP weight_jets_pair(int kernel, fp2 xi, fp2 eta, fp2 fac, bool scaled, int nc,
+                                                  const fp2* gc, const int8_t* __restrict__ node_side,
+                                                  int n_nodes, int j) {
+  const fp2 zx = scaled ? xi * fac : xi, zy = scaled ? eta * fac : eta;
+  const fp2 si = fp2_sqrt(fp2_sqr(zx) + fp2_sqr(zy));
+  fp2 wi, d, dd;
+  window_pair(kernel, si, wi, d, dd);
+  JetsP J;
+  J.v[0] = wi;
+  if (fp2_is_zero(si)) {  // s == 0: dx = dy = 0, d2x = d2y = d2w, no cross term
+    const fp2 z{0.0f, 0.0f};
+    J.v[1] = z; J.v[2] = z;
+    J.v[3] = d * dd; J.v[4] = d * dd; J.v[5] = z;
+  } else {
+    const fp2 is = fp2_recip(si);
+    const fp2 dx = zx * is, dy = zy * is;
+    const fp2 is3 = fp2_sqr(is) * is;
+    J.v[1] = d * dx;
+    J.v[2] = d * dy;
+    J.v[3] = dd * fp2_sqr(dx) + d * (fp2_sqr(zx) * is3);  // the reference's d2x = xi^2 / s^3
+    J.v[4] = dd * fp2_sqr(dy) + d * (fp2_sqr(zy) * is3);  // and d2y = eta^2 / s^3
+    J.v[5] = dd * (dx * dy) - d * ((zx * zy) * is3);
+  }
+  if (scaled) {
+    const fp2 f2 = fp2_sqr(fac);
+    J.v[1] = J.v[1] * fac; J.v[2] = J.v[2] * fac;
+    J.v[3] = J.v[3] * f2; J.v[4] = J.v[4] * f2; J.v[5] = J.v[5] * f2;
+  }
+  for (int c = 0; c < nc; ++c) {
+    const fp2* G = gc + 6 * c;
+    const float sn = node_side[static_cast<int64_t>(c) * n_nodes + j] > 0 ? 1.0f : -1.0f;
+    const fp2 W = G[0] * sn + 0.5f;
+    const fp2 dWx = G[1] * sn, dWy = G[2] * sn;
+    const fp2 ddWxx = G[3] * sn, ddWyy = G[4] * sn, ddWxy = G[5] * sn;
+    const JetsP o = J;
+    J.v[0] = o.v[0] * W;
+    J.v[1] = o.v[1] * W + o.v[0] * dWx;
+    J.v[2] = o.v[2] * W + o.v[0] * dWy;
+    J.v[3] = o.v[3] * W + 2.0f * (o.v[1] * dWx) + o.v[0] * ddWxx;
+    J.v[4] = o.v[4] * W + 2.0f * (o.v[2] * dWy) + o.v[0] * ddWyy;
+    J.v[5] = o.v[5] * W + o.v[1] * dWy + o.v[2] * dWx + o.v[0] * ddWxy;
+  }
+  return J;
+}
+
+// Monomial basis jets in pairs (Basis<ORDER> above).
+template <int ORDER>
+struct BasisPair {
+  static constexpr int NP = (ORDER + 1) * (ORDER + 2) / 2;
+  fp2 p[NP], px[NP], py[NP], pxx[NP], pyy[NP], pxy[NP];
+  __device__ __forceinline__ static fp2 mono(const fp2* xp, const fp2* yp, int a, int b) {
+    return a == 0 ? yp[b] : (b == 0 ? xp[a] : xp[a] * yp[b]);
+  }
+  __device__ __forceinline__ explicit BasisPair(fp2 x, fp2 y) {
+    fp2 xp[ORDER + 1], yp[ORDER + 1];
+    xp[0] = fp2{1.0f, 0.0f}; yp[0] = fp2{1.0f, 0.0f};
+#pragma unroll
+    for (int q = 1; q <= ORDER; ++q) { xp[q] = q == 1 ? x : xp[q - 1] * x; yp[q] = q == 1 ? y : yp[q - 1] * y; }
+    const fp2 z{0.0f, 0.0f};
+    int idx = 0;
+#pragma unroll
+    for (int d = 0; d <= ORDER; ++d) {
+#pragma unroll
+      for (int qy = 0; qy <= d; ++qy) {
+        const int qx = d - qy;
+        p[idx] = mono(xp, yp, qx, qy);
+        px[idx] = qx > 0 ? static_cast<float>(qx) * mono(xp, yp, qx - 1, qy) : z;
+        py[idx] = qy > 0 ? static_cast<float>(qy) * mono(xp, yp, qx, qy - 1) : z;
+        pxx[idx] = qx > 1 ? static_cast<float>(qx * (qx - 1)) * mono(xp, yp, qx - 2, qy) : z;
+        pyy[idx] = qy > 1 ? static_cast<float>(qy * (qy - 1)) * mono(xp, yp, qx, qy - 2) : z;
+        pxy[idx] = (qx > 0 && qy > 0) ? static_cast<float>(qx * qy) * mono(xp, yp, qx - 1, qy - 1) : z;
+        ++idx;
+      }
+    }
+  }
+};
+
+// Per-point inputs of the pair passes.
+struct PairPoint {
+  float gx0, gx1, gx2, gy0, gy1, gy2;
+  int nc;
+  bool scaled;
+  fp2 gc[6 * 4];
+};
+
+__device__ __forceinline__ void pair_xi(const RkpmArgs& a, const PairPoint& P, int j, fp2& xi, fp2& eta, fp2& fac) {
+  const float4 n0 = __ldg(a.node_pair + 2 * j), n1 = __ldg(a.node_pair + 2 * j + 1);
+  xi = diff3(P.gx0, P.gx1, P.gx2, n0.x, n0.y, n0.z) * a.irho;
+  eta = diff3(P.gy0, P.gy1, P.gy2, n0.w, n1.x, n1.y) * a.irho;
+  fac = fp2{n1.z, n1.w};
+}
+
+// Raw-moment sums of weight jets J0 .. J0 + NJ - 1 over the point's neighbours, in pairs
+// (Dot2 accumulation), rounded to FP64 into Sd[J0 + jj][k].
+template <int ORDER, int J0, int NJ>
+__device__ __forceinline__ void pair_moment_sums(const RkpmArgs& a, const PairPoint& P, int64_t p0, int64_t p1,
+                                                 double (&Sd)[6][RawIdx<ORDER>::NR]) {
+  using RI = RawIdx<ORDER>;
+  constexpr int NR = RI::NR;
+  fp2 S[NJ][NR];
+#pragma unroll
+  for (int q = 0; q < NJ; ++q)
+#pragma unroll
+    for (int k = 0; k < NR; ++k) S[q][k] = fp2{0.0f, 0.0f};
+  for (int64_t e = p0; e < p1; ++e) {
+    const int j = a.idx[e];
+    fp2 xi, eta, fac;
+    pair_xi(a, P, j, xi, eta, fac);
+    const JetsP J = weight_jets_pair(a.kernel, xi, eta, fac, P.scaled, P.nc, P.gc, a.node_side, a.n_nodes, j);
+    fp2 xp[RI::D + 1], yp[RI::D + 1];
+    xp[0] = fp2{1.0f, 0.0f}; yp[0] = fp2{1.0f, 0.0f};
+#pragma unroll
+    for (int q = 1; q <= RI::D; ++q) { xp[q] = q == 1 ? xi : xp[q - 1] * xi; yp[q] = q == 1 ? eta : yp[q - 1] * eta; }
+#pragma unroll
+    for (int d = 0; d <= RI::D; ++d) {
+#pragma unroll
+      for (int b = 0; b <= d; ++b) {
+        const int k = RI::r(d - b, b);
+        const fp2 m = BasisPair<ORDER>::mono(xp, yp, d - b, b);
+#pragma unroll
+        for (int q = 0; q < NJ; ++q) fp2_fma_acc(S[q][k], J.v[J0 + q], m);
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NJ; ++q)
+#pragma unroll
+    for (int k = 0; k < NR; ++k) Sd[J0 + q][k] = fp2_to_double(S[q][k]);
+}
+
+// GlobalRKPM.h:59-397 for one Gauss point per thread, per-neighbour work in FP32 pairs.
+template <int ORDER>
+__global__ void __launch_bounds__(kThreads) rkpm_pair_kernel(RkpmArgs a) {
+  constexpr int NP = (ORDER + 1) * (ORDER + 2) / 2;
+  using RI = RawIdx<ORDER>;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= a.n_gp) return;
+  const int64_t p0 = a.ptr[g], p1 = a.ptr[g + 1];
+  PairPoint P;
+  split3(a.gp_xy[2 * g], P.gx0, P.gx1, P.gx2);
+  split3(a.gp_xy[2 * g + 1], P.gy0, P.gy1, P.gy2);
+  P.nc = a.n_creases < 4 ? a.n_creases : 4;
+  P.scaled = a.rho_node != nullptr;
+  const double r1 = 0.5 * a.rho, r2 = 0.5 * a.rho * a.rho;
+  for (int c = 0; c < P.nc; ++c) {
+    const double* I = a.gind + (static_cast<int64_t>(g) * a.n_creases + c) * 6;
+    P.gc[6 * c + 0] = fp2_from_double(0.5 * I[0]);
+    P.gc[6 * c + 1] = fp2_from_double(r1 * I[1]);
+    P.gc[6 * c + 2] = fp2_from_double(r1 * I[2]);
+    P.gc[6 * c + 3] = fp2_from_double(r2 * I[3]);
+    P.gc[6 * c + 4] = fp2_from_double(r2 * I[4]);
+    P.gc[6 * c + 5] = fp2_from_double(r2 * I[5]);
+  }
+  // Moment sums: all six jets in one pass up to ORDER 2; two passes of three jets for
+  // ORDER 3 (28 raw moments), which keeps the pair accumulators in registers.
+  double Sd[6][RI::NR];
+  if constexpr (ORDER <= 2) {
+    pair_moment_sums<ORDER, 0, 6>(a, P, p0, p1, Sd);
+  } else {
+    pair_moment_sums<ORDER, 0, 3>(a, P, p0, p1, Sd);
+    pair_moment_sums<ORDER, 3, 3>(a, P, p0, p1, Sd);
+  }
+  RowJets<ORDER> R;
+  a.bad[g] = static_cast<int8_t>(point_solve<ORDER>(Sd[0], Sd[1], Sd[2], Sd[3], Sd[4], Sd[5], R));
+  fp2 c0[NP], c0x[NP], c0y[NP], c0xx[NP], c0yy[NP], c0xy[NP], c0x2[NP], c0y2[NP];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    c0[i] = fp2_from_double(R.c0[i]);
+    c0x[i] = fp2_from_double(R.c0x[i]);
+    c0y[i] = fp2_from_double(R.c0y[i]);
+    c0xx[i] = fp2_from_double(R.c0xx[i]);
+    c0yy[i] = fp2_from_double(R.c0yy[i]);
+    c0xy[i] = fp2_from_double(R.c0xy[i]);
+    c0x2[i] = c0x[i] * 2.0f;
+    c0y2[i] = c0y[i] * 2.0f;
+  }
+  // Shape functions (GlobalRKPM.h:363-396).
+  for (int64_t e = p0; e < p1; ++e) {
+    const int j = a.idx[e];
+    fp2 xi, eta, fac;
+    pair_xi(a, P, j, xi, eta, fac);
+    const JetsP J = weight_jets_pair(a.kernel, xi, eta, fac, P.scaled, P.nc, P.gc, a.node_side, a.n_nodes, j);
+    const BasisPair<ORDER> B(xi, eta);
+    const fp2 z{0.0f, 0.0f};
+    fp2 C = z, Cx = z, Cy = z, Cxx = z, Cyy = z, Cxy = z;
+#pragma unroll
+    for (int jp = 0; jp < NP; ++jp) {
+      fp2_fma_acc(C, c0[jp], B.p[jp]);
+      fp2_fma_acc(Cx, c0x[jp], B.p[jp]); fp2_fma_acc(Cx, c0[jp], B.px[jp]);
+      fp2_fma_acc(Cy, c0y[jp], B.p[jp]); fp2_fma_acc(Cy, c0[jp], B.py[jp]);
+      fp2_fma_acc(Cxx, c0xx[jp], B.p[jp]); fp2_fma_acc(Cxx, c0x2[jp], B.px[jp]); fp2_fma_acc(Cxx, c0[jp], B.pxx[jp]);
+      fp2_fma_acc(Cyy, c0yy[jp], B.p[jp]); fp2_fma_acc(Cyy, c0y2[jp], B.py[jp]); fp2_fma_acc(Cyy, c0[jp], B.pyy[jp]);
+      fp2_fma_acc(Cxy, c0xy[jp], B.p[jp]); fp2_fma_acc(Cxy, c0x[jp], B.py[jp]);
+      fp2_fma_acc(Cxy, c0y[jp], B.px[jp]); fp2_fma_acc(Cxy, c0[jp], B.pxy[jp]);
+    }
+    C = fp2_norm(C); Cx = fp2_norm(Cx); Cy = fp2_norm(Cy);
+    Cxx = fp2_norm(Cxx); Cyy = fp2_norm(Cyy); Cxy = fp2_norm(Cxy);
+    const fp2* w = J.v;
+    fp2 gx = z, gy = z, hxx = z, hyy = z, hxy = z;
+    fp2_fma_acc(gx, Cx, w[0]); fp2_fma_acc(gx, C, w[1]);
+    fp2_fma_acc(gy, Cy, w[0]); fp2_fma_acc(gy, C, w[2]);
+    const fp2 Cx2 = Cx * 2.0f, Cy2 = Cy * 2.0f;
+    fp2_fma_acc(hxx, Cxx, w[0]); fp2_fma_acc(hxx, Cx2, w[1]); fp2_fma_acc(hxx, C, w[3]);
+    fp2_fma_acc(hyy, Cyy, w[0]); fp2_fma_acc(hyy, Cy2, w[2]); fp2_fma_acc(hyy, C, w[4]);
+    fp2_fma_acc(hxy, Cxy, w[0]); fp2_fma_acc(hxy, Cx, w[2]); fp2_fma_acc(hxy, Cy, w[1]); fp2_fma_acc(hxy, C, w[5]);
+    a.psi[e] = fp2_to_double(C * w[0]);
+    a.dpsi[2 * e] = fp2_to_double(fp2_norm(gx) * a.irho);
+    a.dpsi[2 * e + 1] = fp2_to_double(fp2_norm(gy) * a.irho);
+    a.ddpsi[3 * e] = fp2_to_double(fp2_norm(hxx) * a.irho2);
+    a.ddpsi[3 * e + 1] = fp2_to_double(fp2_norm(hyy) * a.irho2);
+    a.ddpsi[3 * e + 2] = fp2_to_double(fp2_norm(hxy) * a.irho2);
+  }
+}
+
 inline unsigned blocks_for(int64_t n, int t = kThreads) { return static_cast<unsigned>((n + t - 1) / t); }
 
 }  // namespace
@@ -459,6 +789,9 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
   out->rho = prm.rho;
   out->order = prm.order;
   out->kernel = prm.kernel;
+  if (prm.precision != CGB_SHAPE_FP64 && prm.precision != CGB_SHAPE_MIXED)
+    throw Error(CGB_ERR_INVALID, "cgb_shape_build: precision must be CGB_SHAPE_FP64 or CGB_SHAPE_MIXED");
+  out->precision = prm.precision;
   out->node_gen = ctx->node_gen;
 
   // ---- node cell grid (FRNN.h:33-44), host side, O(n_nodes) ----
@@ -590,18 +923,38 @@ void shape_values(cgb_context* ctx, cgb_shape* out, const std::vector<Crease>& c
   if (out->dpsi.n < static_cast<size_t>(std::max<int64_t>(2 * nnz, 1))) out->dpsi.alloc(2 * nnz);
   if (out->ddpsi.n < static_cast<size_t>(std::max<int64_t>(3 * nnz, 1))) out->ddpsi.alloc(3 * nnz);
   int8_t* bad = out->scr_bad.p;
-  RkpmArgs ra{n_gp, n_nodes, out->kernel, nc, out->rho, out->gp_xy.p, ctx->node_xy.p,
-              out->has_rho_node ? out->rho_node.p : nullptr, out->nbr_ptr.p, out->nbr_idx.p, out->s.p, gind,
-              side, out->psi.p, out->dpsi.p, out->ddpsi.p, bad};
+  const double* d_rn = out->has_rho_node ? out->rho_node.p : nullptr;
+  const bool mixed = out->precision == CGB_SHAPE_MIXED;
+  auto pair_of = [](double v) {
+    const float hi = static_cast<float>(v);
+    return fp2{hi, static_cast<float>(v - static_cast<double>(hi))};
+  };
+  RkpmArgs ra{n_gp, n_nodes, out->kernel, nc, out->rho, nullptr, pair_of(1.0 / out->rho),
+              pair_of(1.0 / (out->rho * out->rho)), out->gp_xy.p, ctx->node_xy.p, d_rn, out->nbr_ptr.p,
+              out->nbr_idx.p, out->s.p, gind, side, out->psi.p, out->dpsi.p, out->ddpsi.p, bad};
   prof_begin(ctx, CGB_PHASE_RKPM);
+  if (mixed && n_nodes > 0) {
+    out->scr_node_pair.ensure(2 * static_cast<size_t>(n_nodes));
+    node_pair_kernel<<<blocks_for(n_nodes), kThreads, 0, st>>>(n_nodes, ctx->node_xy.p, d_rn, out->rho,
+                                                                 out->scr_node_pair.p);
+    ra.node_pair = out->scr_node_pair.p;
+  }
   if (n_gp > 0) {
-    switch (out->order) {
-      case 1: rkpm_kernel<1><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
-      case 2: rkpm_kernel<2><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
-      default: rkpm_kernel<3><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
+    if (mixed) {
+      switch (out->order) {
+        case 1: rkpm_pair_kernel<1><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
+        case 2: rkpm_pair_kernel<2><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
+        default: rkpm_pair_kernel<3><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
+      }
+    } else {
+      switch (out->order) {
+        case 1: rkpm_kernel<1><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
+        case 2: rkpm_kernel<2><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
+        default: rkpm_kernel<3><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
+      }
     }
   }
-  prof_end(ctx, CGB_PHASE_RKPM, n_gp > 0 ? 1 : 0);
+  prof_end(ctx, CGB_PHASE_RKPM, (n_gp > 0 ? 1 : 0) + (mixed && n_nodes > 0 ? 1 : 0));
   CGB_CUDA(cudaGetLastError());
   std::vector<int8_t> hbad(n_gp);
   if (n_gp > 0) CGB_CUDA(cudaMemcpyAsync(hbad.data(), bad, n_gp, cudaMemcpyDeviceToHost, st));

@@ -75,7 +75,7 @@ class Crease(C.Structure):
 
 
 class ShapeParams(C.Structure):
-    _fields_ = [("rho", dbl), ("rho_node", vp), ("order", i32), ("kernel", i32)]
+    _fields_ = [("rho", dbl), ("rho_node", vp), ("order", i32), ("kernel", i32), ("precision", i32)]
 
 
 class Tuning(C.Structure):

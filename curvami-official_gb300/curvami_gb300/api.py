@@ -146,10 +146,15 @@ def concat_shapes(ctx: Context, sets, node_offsets) -> ShapeSet:
     return ShapeSet(ctx, h)
 
 
-def shape_functions(ctx: Context, gp_xy, rho, order=2, creases=(), rho_node=None, kernel=0) -> ShapeSet:
+SHAPE_PRECISIONS = {"fp64": 0, "mixed": 1}
+
+
+def shape_functions(ctx: Context, gp_xy, rho, order=2, creases=(), rho_node=None, kernel=0,
+                    precision="fp64") -> ShapeSet:
     """GlobalFRNN::execute + GlobalRKPM::solve for one set of Gauss points. Raises
     CGBError (CGB_ERR_SINGULAR / CGB_ERR_PIVOT) with the reference's message on a
-    rank-deficient support."""
+    rank-deficient support. precision "fp64" is the reference's arithmetic; "mixed" sums
+    the per-neighbour terms in FP32 pairs and factors the moment matrix in FP64."""
     gp_xy = _c(gp_xy, np.float64)
     prm = L.ShapeParams()
     prm.rho = float(rho)
@@ -157,6 +162,9 @@ def shape_functions(ctx: Context, gp_xy, rho, order=2, creases=(), rho_node=None
     prm.rho_node = _p(rn)
     prm.order = int(order)
     prm.kernel = int(kernel)
+    if precision not in SHAPE_PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(SHAPE_PRECISIONS)}")
+    prm.precision = SHAPE_PRECISIONS[precision]
     arr, keep = _creases_struct(list(creases))
     h = C.c_void_p()
     rc = ctx.lib.cgb_shape_build(ctx.h, _p(gp_xy), len(gp_xy), C.byref(prm), C.addressof(arr),
@@ -359,12 +367,12 @@ class PlateModel:
     """A synthetic plate (synth.Plate) on the GPU: shape functions of the faces and of
     every fold side, the assembler with the hinge union pattern and the material."""
 
-    def __init__(self, plate, ctx: Context | None = None):
+    def __init__(self, plate, ctx: Context | None = None, shape_precision: str = "fp64"):
         self.plate = plate
         self.ctx = ctx or Context(0)
         self.ctx.set_nodes(plate.node_xy)
         kw = dict(rho=plate.rho, order=plate.order, creases=plate.creases, rho_node=plate.rho_node,
-                  kernel=plate.kernel)
+                  kernel=plate.kernel, precision=shape_precision)
         self.faces = shape_functions(self.ctx, plate.faces.xy, **kw)
         self.fold_sets = []
         folds = []

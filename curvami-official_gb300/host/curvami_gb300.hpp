@@ -64,15 +64,15 @@ struct Shapes {  // GaussPointData::neighbor_node_ids / Psi / dPsi / ddPsi, flat
 class ShapeSet {
  public:
   // GlobalFRNN::execute + GlobalRKPM::solve; throws Error with the reference's message
-  // on a rank-deficient support.
+  // on a rank-deficient support. precision: CGB_SHAPE_FP64 or CGB_SHAPE_MIXED.
   static ShapeSet build(Context& ctx, const std::vector<double>& gp_xy, double rho, int order,
                         const std::vector<Crease>& creases = {}, const std::vector<double>* rho_node = nullptr,
-                        int kernel = 0) {
+                        int kernel = 0, int precision = CGB_SHAPE_FP64) {
     std::vector<cgb_crease> cr(creases.size());
     for (size_t k = 0; k < creases.size(); ++k)
       cr[k] = cgb_crease{creases[k].xy.data(), static_cast<int>(creases[k].xy.size() / 2),
                          creases[k].extend_start, creases[k].extend_end, creases[k].is_closed};
-    cgb_shape_params prm{rho, rho_node ? rho_node->data() : nullptr, order, kernel};
+    cgb_shape_params prm{rho, rho_node ? rho_node->data() : nullptr, order, kernel, precision};
     cgb_shape* h = nullptr;
     const int rc = cgb_shape_build(ctx.get(), gp_xy.data(), static_cast<int>(gp_xy.size() / 2), &prm,
                                    cr.data(), static_cast<int>(cr.size()), &h);

@@ -71,12 +71,19 @@ typedef struct {
 
 /* Shape-stage parameters. rho / order as GlobalRKPM::solve (GlobalRKPM.h:19-21).
  * rho_node: NULL for the reference's single radius, else a per-node radius (extension).
- * kernel: 0 quartic spline (GlobalRKPM.h:15-17), 1 cubic B-spline (extension). */
+ * kernel: 0 quartic spline (GlobalRKPM.h:15-17), 1 cubic B-spline (extension).
+ * precision: CGB_SHAPE_FP64 (0, the reference's arithmetic) or CGB_SHAPE_MIXED (1: the
+ * per-neighbour sums in FP32 pairs, about 48 significant bits, the moment matrix
+ * factored and solved per point in FP64; same neighbours, guards and error messages).
+ * Zero-initialised parameters select FP64. */
+#define CGB_SHAPE_FP64 0
+#define CGB_SHAPE_MIXED 1
 typedef struct {
   double rho;
   const double* rho_node;
   int order;
   int kernel;
+  int precision;
 } cgb_shape_params;
 
 /* One fold for the hinge. Replaces the arguments of Constraints::evaluateElasticFold

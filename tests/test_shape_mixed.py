@@ -1,0 +1,166 @@
+"""Mixed-precision shape stage (CGB_SHAPE_MIXED) on the GPU against the FP64 oracle.
+
+The mixed kernel sums every per-neighbour term in FP32 pairs (about 48 significant bits)
+and factors the moment matrix per point in FP64. Bars, relative to each array's scale:
+- the neighbour lists are the FP64 mode's (same FRNN): bit-exact;
+- points whose support no crease truncates: Phi, grad Phi, Hessian Phi within 1e-11 of
+  the oracle (the pair sums' rounding, ~1e-14, times the moment matrix's conditioning);
+- all points: within 1e-6 (crease-truncated supports are ill-conditioned; two FP64
+  evaluations already differ there by cond(M) * eps);
+- the RKPM reproducing conditions hold to within 300x of the FP64 mode's error;
+- the reference's guards fire on the same points with the same messages;
+- an FP64 assembly on mixed shape functions gives F within 1e-10 of the same assembly on
+  FP64 shape functions (the residual bar of the mixed assembly).
+"""
+import numpy as np
+import pytest
+
+import curvami_gb300 as cg
+from curvami_gb300 import synth
+from oracle import Oracle
+
+from test_gpu_parity import SHAPE_CASES, crease_distance, oracle_shapes, rel
+
+pytestmark = pytest.mark.gpu
+
+FAR_BAR = 1e-11
+ALL_BAR = 1e-6
+
+
+@pytest.fixture(scope="module")
+def o():
+    return Oracle()
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import __graft_entry__ as ge
+
+    ge.build()
+    yield cg.Context(0)
+
+
+def kw(p):
+    return dict(rho=p.rho, order=p.order, creases=p.creases, rho_node=p.rho_node, kernel=p.kernel)
+
+
+def reproducing(d, node_xy, pts, scale, order):
+    """Worst |scale^|a| sum_I D^a Phi_I t_I^b - a! delta_ab| over points and monomials b of
+    degree <= order (t_I = (X_I - x) / scale), per derivative order of a."""
+    ptr = d["ptr"]
+    n = len(ptr) - 1
+    row = np.repeat(np.arange(n), np.diff(ptr))
+    t = (node_xy[d["idx"]] - pts[row]) / scale
+    tx, ty = t[:, 0], t[:, 1]
+    mono = [(0, 0)] + [(d_ - b, b) for d_ in range(1, order + 1) for b in range(d_ + 1)]
+    dp = d["dpsi"].reshape(-1, 2)
+    ddp = d["ddpsi"].reshape(-1, 3)
+    jets = [(d["psi"], (0, 0)), (dp[:, 0] * scale, (1, 0)), (dp[:, 1] * scale, (0, 1)),
+            (ddp[:, 0] * scale ** 2, (2, 0)), (ddp[:, 1] * scale ** 2, (0, 2)), (ddp[:, 2] * scale ** 2, (1, 1))]
+    worst = [0.0, 0.0, 0.0]
+    for J, (ax, ay) in jets:
+        for (bx, by) in mono:
+            acc = np.bincount(row, weights=J * tx ** bx * ty ** by, minlength=n)
+            # sum_I Phi_I(x) q(X_I) = q(x) for q(X) = ((X - x0) / scale)^b; D^a at x = x0,
+            # times scale^|a|, is a! when a == b and 0 otherwise.
+            if (ax, ay) == (bx, by):
+                acc -= float(np.prod(range(1, ax + 1)) * np.prod(range(1, ay + 1)))
+            k = ax + ay
+            worst[k] = max(worst[k], float(np.abs(acc).max()))
+    return worst
+
+
+@pytest.mark.parametrize("name", sorted(SHAPE_CASES))
+def test_mixed_shape_functions_against_oracle(o, ctx, name):
+    p = SHAPE_CASES[name]()
+    ctx.set_nodes(p.node_xy)
+    mx = cg.shape_functions(ctx, p.faces.xy, precision="mixed", **kw(p)).download()
+    fp = cg.shape_functions(ctx, p.faces.xy, **kw(p)).download()
+    ref = oracle_shapes(o, p, p.faces.xy)
+    assert np.array_equal(mx["ptr"], ref["ptr"]) and np.array_equal(mx["idx"], ref["idx"])
+    far = np.repeat(crease_distance(p, p.faces.xy) > p.rho, np.diff(ref["ptr"]))
+    errs = {}
+    for k in ("psi", "dpsi", "ddpsi"):  # arrays are (nnz,), (nnz, 2), (nnz, 3)
+        errs[k] = (rel(mx[k][far], ref[k][far]) if far.any() else 0.0, rel(mx[k], ref[k]))
+    print(name, "mixed vs oracle (far, all):", errs)
+    for k, (e_far, e_all) in errs.items():
+        assert e_far < FAR_BAR, k
+        assert e_all < ALL_BAR, k
+    # Reproducing conditions: within 300x of the FP64 values' error (or 1e-12): the pair
+    # format carries 2^-48 against FP64's 2^-53, a factor of 32, and the measured ratio
+    # over these cases is 8 - 103.
+    h = p.rho
+    r_mx = reproducing(mx, p.node_xy, p.faces.xy, h, p.order)
+    r_fp = reproducing(fp, p.node_xy, p.faces.xy, h, p.order)
+    print(name, "reproducing error mixed / fp64:", r_mx, r_fp)
+    for a, b in zip(r_mx, r_fp):
+        assert a <= max(300.0 * b, 1e-12)
+
+
+def test_mixed_per_node_radius(o, ctx):
+    plate, pts = synth.config_shape_points(n_points=20000, n_side=61, per_node_rho=True, seed=11)
+    ctx.set_nodes(plate.node_xy)
+    mx = cg.shape_functions(ctx, pts, precision="mixed", **kw(plate)).download()
+    ref = oracle_shapes(o, plate, pts)
+    assert np.array_equal(mx["ptr"], ref["ptr"]) and np.array_equal(mx["idx"], ref["idx"])
+    far_pt = crease_distance(plate, pts) > 1.75
+    far = np.repeat(far_pt, np.diff(ref["ptr"]))
+    for k in ("psi", "dpsi", "ddpsi"):
+        e_far, e_all = rel(mx[k][far], ref[k][far]), rel(mx[k], ref[k])
+        print("per-node radius", k, e_far, e_all)
+        assert e_far < FAR_BAR, k
+        assert e_all < ALL_BAR, k
+
+
+def test_mixed_guards_match_fp64(ctx):
+    # The reference's errors on a rank-deficient support come out of the per-point FP64
+    # factorisation, so both modes report the same code and text.
+    nodes = np.array([[0.0, 0.0], [0.5, 0.0], [1.0, 0.0]])
+    ctx.set_nodes(nodes)
+    msgs = []
+    for prec in ("fp64", "mixed"):
+        with pytest.raises(cg.CGBError) as e:
+            cg.shape_functions(ctx, np.array([[0.5, 0.0]]), 1.5, 2, precision=prec)
+        msgs.append((e.value.code, str(e.value)))
+    assert msgs[0] == msgs[1]
+    p = synth.square_plate(9, 0.5, 2, crease=None)
+    ctx.set_nodes(p.node_xy)
+    with pytest.raises(cg.CGBError) as e:  # no neighbours at all
+        cg.shape_functions(ctx, np.array([[100.0, 100.0]]), p.rho, 2, precision="mixed")
+    assert e.value.code == 3 and "singular moment matrix" in str(e.value)
+    assert cg.shape_functions(ctx, np.zeros((0, 2)), p.rho, 2, precision="mixed").n_gp == 0
+    with pytest.raises(ValueError):
+        cg.shape_functions(ctx, p.faces.xy, p.rho, 2, precision="fp32")
+
+
+def test_mixed_rebuild_reproduces_build(ctx):
+    p = SHAPE_CASES["arc_r4_jitter"]()
+    ctx.set_nodes(p.node_xy)
+    sh = cg.shape_functions(ctx, p.faces.xy, precision="mixed", **kw(p))
+    first = sh.download()
+    sh.rebuild([])
+    plain = sh.download()
+    sh.rebuild(p.creases)
+    again = sh.download()
+    for k in ("psi", "dpsi", "ddpsi"):
+        assert np.array_equal(first[k], again[k]), k
+    # Without the cut the values change (the arc truncates supports).
+    assert not np.array_equal(first["psi"], plain["psi"])
+
+
+def test_fp64_assembly_on_mixed_shape_functions(ctx):
+    """F of the FP64 assembly on mixed shape functions against F on FP64 shape functions:
+    within the 1e-10 residual bar."""
+    p = synth.square_plate(31, 0.5, 4, jitter=0.1, crease="arc", rho_factor=3.5, seed=21)
+    x = synth.fourier_field(p.node_xy, np.random.default_rng(22), lam=(4.0, 20.0))
+    res = {}
+    for prec in ("fp64", "mixed"):
+        ctx.set_nodes(p.node_xy)
+        m = cg.PlateModel(p, ctx=ctx, shape_precision=prec)
+        K, F = m.assemble_system(x, cg.TANGENT | cg.HINGE)
+        res[prec] = (np.asarray(K), np.asarray(F))
+    eF = rel(res["mixed"][1], res["fp64"][1])
+    eK = rel(res["mixed"][0], res["fp64"][0])
+    print("FP64 assembly on mixed vs FP64 shape functions: F", eF, "K", eK)
+    assert eF < 1e-10
+    assert eK < 1e-9
