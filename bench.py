@@ -55,9 +55,11 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n-side", type=int, default=201, help="nodes per side (201 = the workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="assembly", choices=["assembly", "batched"],
+    ap.add_argument("--workload", default="assembly", choices=["assembly", "batched", "shape"],
                     help="assembly: the single-plate assembly at scale (the metric's workload); "
-                         "batched: 64 uneven plates in one graph launch per step")
+                         "batched: 64 uneven plates in one graph launch per step; "
+                         "shape: the shape-function stage alone (1,000,000 points)")
+    ap.add_argument("--n-points", type=int, default=1_000_000, help="points of the shape workload")
     ap.add_argument("--plates", type=int, default=64, help="plates of the batched workload")
     ap.add_argument("--no-shape-stage", action="store_true",
                     help="skip the shape-function stage object (shorter runs under a profiler)")
@@ -917,12 +919,78 @@ def run_batched(args):
     reps.close()
 
 
+def run_shape(args):
+    """The shape-function stage alone (GlobalFRNN::execute + GlobalRKPM::solve on
+    1,000,000 points): builds per second in the mixed mode, with the FP64 mode beside it.
+    A step is one build (FRNN, crease indicators, RKPM, guards, host set-up); the RKPM
+    phase is also timed on the device by the library's event profiler."""
+    import torch
+
+    import curvami_gb300 as cg
+    from curvami_gb300 import synth
+    from curvami_gb300.replicas import Replicas
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    reps = Replicas()
+    plate, pts = synth.config_shape_points(n_points=args.n_points, seed=SHAPE_SEED)
+    ctx = cg.Context(local)
+    ctx.set_nodes(plate.node_xy)
+    kw = dict(rho=plate.rho, order=plate.order, creases=plate.creases, rho_node=plate.rho_node,
+              kernel=plate.kernel)
+    W = max(args.warmup, 3)
+
+    def timed(prec, steps):
+        for _ in range(W):
+            cg.shape_functions(ctx, pts, precision=prec, **kw)
+        ctx.synchronize()
+        reps.barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            sh = cg.shape_functions(ctx, pts, precision=prec, **kw)
+        ctx.synchronize()
+        wall = reps.max((time.perf_counter() - t0) * 1e3 / steps)
+        ctx.profile(True)
+        ctx.profile_read(reset=True)
+        cg.shape_functions(ctx, pts, precision=prec, **kw)
+        ph, _ = ctx.profile_read(reset=True)
+        ctx.profile(False)
+        return wall, {k: ph[k] for k in ("frnn", "crease", "rkpm")}, sh
+
+    with ClockSampler(local) as clk:
+        ms_mx, ph_mx, sh = timed("mixed", args.steps)
+    nnz = sh.nnz
+    del sh
+    ms_64, ph_64, _ = timed("fp64", max(3, args.steps // 4))
+    line = {
+        "metric": "shape-function evaluations (Phi, grad Phi, Hessian Phi per point) per second, mixed vs FP64 GPU",
+        "value": world * len(pts) / (ms_mx * 1e-3), "unit": "points/s", "n_gpus": world, "steps": args.steps,
+        "warmup": W, "ms_per_step": ms_mx, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32 pairs per neighbour, fp64 per point", "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": (f"{len(pts):,} uniform points in [0,200]^2 over 401x401 jittered nodes (+/-0.2h), "
+                                "quadratic basis, cubic B-spline window, per-node support radius U[2.5h, 3.5h], one "
+                                "straight cut along the node row y = 100; one build (FRNN + crease indicators + RKPM) "
+                                "per step"), "seed": SHAPE_SEED, "pairs": nnz,
+                   "inputs": "larger than L2 (outputs 1.7 GB per build)"},
+        "phases_ms": ph_mx,
+        "rkpm_points_per_s": len(pts) / (ph_mx["rkpm"] * 1e-3) if ph_mx["rkpm"] > 0 else None,
+        "fp64": {"value": world * len(pts) / (ms_64 * 1e-3), "ms_per_step": ms_64, "phases_ms": ph_64,
+                 "rkpm_mixed_over_fp64": ph_64["rkpm"] / ph_mx["rkpm"] if ph_mx["rkpm"] > 0 else None},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    reps.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":
         run_batched(args)
+    elif args.workload == "shape":
+        run_shape(args)
     else:
         run_gpu(args)
 

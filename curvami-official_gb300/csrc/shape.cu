@@ -684,9 +684,18 @@ __device__ __forceinline__ void pair_moment_sums(const RkpmArgs& a, const PairPo
     for (int k = 0; k < NR; ++k) Sd[J0 + q][k] = fp2_to_double(S[q][k]);
 }
 
+// Launch shape of the pair kernel, measured on the 1,000,000-point stage (RKPM phase,
+// order 2): 3 blocks per SM (168 registers, some spills) 11.3 ms; 1 block (255 registers)
+// 12.0 ms; the moment sums split into two passes of three jets 13.3 - 14.1 ms at 128 -
+// 255 registers. The kernel is latency-bound at every shape (2 - 4 warps per scheduler),
+// so the shape matters little; order 3 (28 raw moments) needs the split to stay in
+// registers.
+constexpr int kPairMinBlocks = 3;
+constexpr int kPairSplitOrder = 3;
+
 // GlobalRKPM.h:59-397 for one Gauss point per thread, per-neighbour work in FP32 pairs.
 template <int ORDER>
-__global__ void __launch_bounds__(kThreads) rkpm_pair_kernel(RkpmArgs a) {
+__global__ void __launch_bounds__(kThreads, kPairMinBlocks) rkpm_pair_kernel(RkpmArgs a) {
   constexpr int NP = (ORDER + 1) * (ORDER + 2) / 2;
   using RI = RawIdx<ORDER>;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -710,7 +719,7 @@ __global__ void __launch_bounds__(kThreads) rkpm_pair_kernel(RkpmArgs a) {
   // Moment sums: all six jets in one pass up to ORDER 2; two passes of three jets for
   // ORDER 3 (28 raw moments), which keeps the pair accumulators in registers.
   double Sd[6][RI::NR];
-  if constexpr (ORDER <= 2) {
+  if constexpr (ORDER < kPairSplitOrder) {
     pair_moment_sums<ORDER, 0, 6>(a, P, p0, p1, Sd);
   } else {
     pair_moment_sums<ORDER, 0, 3>(a, P, p0, p1, Sd);
