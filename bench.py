@@ -405,11 +405,13 @@ def run_gpu(args):
     creasing = None if args.no_shape_stage else creasing_run(rank == 0 and not args.no_cpu_baseline)
     post = None if args.no_shape_stage else post_processing(cg, ctx, model, x_d, stream)
     four = None
+    arc = None
     if not args.no_shape_stage:
         try:
             four = four_creases_assembly(cg, ctx, stream)
         except cg.CGBError as e:   # a rank-deficient support at the junction is reported, not hidden
             four = {"error": str(e)}
+        arc = arc_length_path(cg, ctx)
 
     line = {
         "metric": METRIC, "value": v_mix, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -441,6 +443,7 @@ def run_gpu(args):
         "shape_stage": shape,
         "progressive_creasing": creasing,
         "four_creases": four,
+        "arc_length_path": arc,
         "post_processing": post,
     }
     if rank == 0:
@@ -746,6 +749,57 @@ def four_creases_assembly(cg, ctx, stream):
            "F_rel_diff_mixed_vs_fp64": float(np.abs(F_mix - F_f64).max() / np.abs(F_f64).max()),
            "unit": UNIT}
     del model, asm
+    return out
+
+
+def arc_length_path(cg, ctx, n_side=41, target_deg=150.0, kmax=80):
+    """The full arc-length path at reduced size: NonLinearSolver::KinematicArcLength restated
+    (curvami_gb300/arclength.py) over the GPU's mixed assembly (FP32 tangent, FP64 residual,
+    exact hinge tangent). Four creases from the centre, sectors 90 +/- 15 deg (seeded);
+    creases 0 and 2 are the drivers (stiff hinges, Kt = 0.1, whose rest angle goes from 0 to
+    150 deg with the deployment parameter mu), 1 and 3 passive elastic hinges (Kt = 1e-3);
+    three point supports in sector 0. The drivers' load direction is the exact fold-angle
+    gradient (an extension: the reference's formula drifts as the fold closes). The KKT
+    system is a dense FP64 LU on the GPU (torch.linalg, standing in for MUMPS), timed on its
+    own line with the host's constraint work."""
+    import math
+
+    from curvami_gb300 import arclength as A
+    from curvami_gb300 import solver as S
+    from curvami_gb300 import synth
+
+    p = synth.four_crease_plate(n_side=n_side, h=0.5, rule=4, seed=FOUR_SEED, Kt=1e-3, rho_factor=3.5)
+    for k, f in enumerate(p.folds):
+        f.rigid = False
+        f.Kt = 1e-1 if k % 2 == 0 else 1e-3
+    doms = A.sector_supports(p, 0, 1)
+    ctx.set_nodes(p.node_xy)
+    model = cg.PlateModel(p, ctx)
+    prob = S.gpu_problem(model, points=doms, exact_hinge=True, mixed=True)
+    drivers = [A.Driver(0, 0.0, math.radians(target_deg)), A.Driver(2, 0.0, math.radians(target_deg))]
+    # ds bounded as for the 13 x 13 plate of the tests (dsmax 2), scaled with the plate's
+    # displacement norm (nodes x width).
+    sol = A.ArcLengthSolver(kmax=kmax, max_iters=30, dsmax=2.0 * (n_side / 13.0) ** 2, kkt="device",
+                            exact_fold_gradient=True)
+    t0 = time.perf_counter()
+    sol.kinematic_arc_length(prob, np.zeros(prob.ns), drivers)
+    wall = time.perf_counter() - t0
+    last = sol.steps[-1] if sol.steps else None
+    out = {
+        "what": ("KinematicArcLength (plate/NonLinearSolver.h:607-812) restated, over the GPU mixed assembly, to a "
+                 f"{target_deg:.0f} deg rest angle of the drivers; config 5's 401x401 plate is not run: its "
+                 "482k-dof KKT needs a sparse direct solver (MUMPS and cuDSS are absent here)"),
+        "n_side": n_side, "n_dofs": prob.ns, "n_gauss_points": model.faces.n_gp, "n_constraint_rows":
+            int(len(sol.ind_rows)), "sector_deg": p.meta["sector_deg"], "seed": FOUR_SEED,
+        "accepted_steps": len(sol.steps), "failed_steps": sol.failed_steps,
+        "corrector_iterations": [st.iterations for st in sol.steps],
+        "final_mu": last.load if last else None,
+        "final_fold_angles_deg": last.angles if last else None,
+        "wall_s": wall, "timing_s": dict(sol.timing), "counts": dict(sol.counts),
+        "ms_per_assembly": 1e3 * sol.timing["assemble_s"] / max(sol.counts["assemblies"], 1),
+        "ms_per_kkt_factorisation": 1e3 * sol.timing["kkt_s"] / max(sol.counts["kkt_factorisations"], 1),
+    }
+    del model, prob
     return out
 
 

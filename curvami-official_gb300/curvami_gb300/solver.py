@@ -174,6 +174,8 @@ class FoldSides:
     rigid: bool = False
     active: np.ndarray | None = None
     theta0_gp: np.ndarray | None = None
+    Kt: float = 0.0                      # hinge stiffness (the arc-length drivers' pseudo-load)
+    weight: np.ndarray | None = None     # the left points' weights (fold angle and gradient)
 
 
 class GpuAssembly:
@@ -187,6 +189,10 @@ class GpuAssembly:
 
     def pattern(self):
         return self.asm.pattern()
+
+    def set_fold_theta0(self, fold: int, theta0: float):
+        """Fold::Ang0 of one fold: its hinge's rest angle at every crease point."""
+        self.asm.set_fold_state(fold, theta0)
 
     def assemble(self, x, want_K: bool, hinge: bool = True):
         flags = self.extra | (L.HINGE if hinge else 0)
@@ -226,6 +232,13 @@ class PlateProblem:
 
     def num_dofs(self) -> int:
         return self.ns
+
+    def set_fold_theta0(self, f: int, theta0: float):
+        """Fold::Ang0 of fold f (the rest angle of its hinge and the target of its rigid
+        row), as the arc-length drivers move it (NonLinearSolver.h:636-641)."""
+        self.folds[f].theta0 = float(theta0)
+        self.folds[f].theta0_gp = None
+        self.backend.set_fold_theta0(f, float(theta0))
 
     # Meshless::assembleSystem: K (stored upper, symmetric) and F_int.
     def assemble(self, x):
@@ -537,9 +550,10 @@ def load_steps(solver: ContinuationSolver, prob: PlateProblem, lambdas, x0=None)
 
 
 def gpu_problem(model, face_load=None, edges=(), mixed: bool = False, deterministic: bool = False,
-                flag_rig: bool = False) -> PlateProblem:
+                flag_rig: bool = False, points=(), exact_hinge: bool = False) -> PlateProblem:
     """PlateProblem of a PlateModel (api.py): the GPU's shape functions for the faces, the
-    folds and every edge domain, and its assembler as the backend."""
+    folds, every edge domain and every point domain (LineDomain of point supports), and its
+    assembler as the backend."""
     from .api import shape_functions
     p = model.plate
     n = len(p.node_xy)
@@ -549,7 +563,10 @@ def gpu_problem(model, face_load=None, edges=(), mixed: bool = False, determinis
     sides = []
     for (Ls, Rs), fd in zip(model.fold_sets, p.folds):
         sides.append(FoldSides(ShapeTable.from_shape_set(Ls, n), ShapeTable.from_shape_set(Rs, n),
-                               np.asarray(fd.left.tangent, np.float64), fd.theta0, fd.rigid))
+                               np.asarray(fd.left.tangent, np.float64), fd.theta0, fd.rigid,
+                               Kt=fd.Kt, weight=np.asarray(fd.left.weight, np.float64)))
     edge_tables = [(dom, ShapeTable.from_shape_set(shape_functions(model.ctx, dom.xy, **kw), n)) for dom in edges]
-    return PlateProblem(n, GpuAssembly(model.asm, mixed, deterministic), faces, p.faces.weight,
-                        face_load=face_load, edges=edge_tables, folds=sides, flag_rig=flag_rig)
+    point_tables = [(dom, ShapeTable.from_shape_set(shape_functions(model.ctx, dom.xy, **kw), n)) for dom in points]
+    return PlateProblem(n, GpuAssembly(model.asm, mixed, deterministic, exact_hinge), faces, p.faces.weight,
+                        face_load=face_load, edges=edge_tables, folds=sides, flag_rig=flag_rig,
+                        points=point_tables)
