@@ -752,10 +752,12 @@ def four_creases_assembly(cg, ctx, stream):
     return out
 
 
-def arc_length_path(cg, ctx, n_side=41, target_deg=150.0, kmax=80):
+def arc_length_path(cg, ctx, n_side=31, target_deg=150.0, kmax=80):
     """The full arc-length path at reduced size: NonLinearSolver::KinematicArcLength restated
-    (curvami_gb300/arclength.py) over the GPU's mixed assembly (FP32 tangent, FP64 residual,
-    exact hinge tangent). Four creases from the centre, sectors 90 +/- 15 deg (seeded);
+    (curvami_gb300/arclength.py) over the GPU's FP64 assembly with the exact hinge tangent
+    (the predictor of this thin plate, t / L = 3.3e-3, needs the FP64 tangent: with the FP32
+    one the 41 x 41 run reversed its first steps). Four creases from the centre, sectors
+    90 +/- 15 deg (seeded);
     creases 0 and 2 are the drivers (stiff hinges, Kt = 0.1, whose rest angle goes from 0 to
     150 deg with the deployment parameter mu), 1 and 3 passive elastic hinges (Kt = 1e-3);
     three point supports in sector 0. The drivers' load direction is the exact fold-angle
@@ -775,7 +777,7 @@ def arc_length_path(cg, ctx, n_side=41, target_deg=150.0, kmax=80):
     doms = A.sector_supports(p, 0, 1)
     ctx.set_nodes(p.node_xy)
     model = cg.PlateModel(p, ctx)
-    prob = S.gpu_problem(model, points=doms, exact_hinge=True, mixed=True)
+    prob = S.gpu_problem(model, points=doms, exact_hinge=True)
     drivers = [A.Driver(0, 0.0, math.radians(target_deg)), A.Driver(2, 0.0, math.radians(target_deg))]
     # ds bounded as for the 13 x 13 plate of the tests (dsmax 2), scaled with the plate's
     # displacement norm (nodes x width).
@@ -786,7 +788,7 @@ def arc_length_path(cg, ctx, n_side=41, target_deg=150.0, kmax=80):
     wall = time.perf_counter() - t0
     last = sol.steps[-1] if sol.steps else None
     out = {
-        "what": ("KinematicArcLength (plate/NonLinearSolver.h:607-812) restated, over the GPU mixed assembly, to a "
+        "what": ("KinematicArcLength (plate/NonLinearSolver.h:607-812) restated, over the GPU FP64 assembly, to a "
                  f"{target_deg:.0f} deg rest angle of the drivers; config 5's 401x401 plate is not run: its "
                  "482k-dof KKT needs a sparse direct solver (MUMPS and cuDSS are absent here)"),
         "n_side": n_side, "n_dofs": prob.ns, "n_gauss_points": model.faces.n_gp, "n_constraint_rows":

@@ -394,7 +394,14 @@ class _KKT:
         if self.device:
             import torch
 
-            self.lu, self.piv = torch.linalg.lu_factor(torch.from_numpy(A.toarray()).to("cuda"))
+            # Only the nonzeros cross to the GPU; the dense matrix is formed there.
+            C = A.tocoo()
+            n = A.shape[0]
+            dense = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+            rows = torch.from_numpy(C.row.astype(np.int64)).to("cuda")
+            cols = torch.from_numpy(C.col.astype(np.int64)).to("cuda")
+            dense.index_put_((rows, cols), torch.from_numpy(C.data).to("cuda"), accumulate=True)
+            self.lu, self.piv = torch.linalg.lu_factor(dense)
         else:
             self.lu = spla.splu(A)
 
