@@ -752,18 +752,19 @@ def four_creases_assembly(cg, ctx, stream):
     return out
 
 
-def arc_length_path(cg, ctx, n_side=31, target_deg=150.0, kmax=80):
+def arc_length_path(cg, ctx, n_side=41, target_deg=150.0, kmax=80):
     """The full arc-length path at reduced size: NonLinearSolver::KinematicArcLength restated
     (curvami_gb300/arclength.py) over the GPU's FP64 assembly with the exact hinge tangent
-    (the predictor of this thin plate, t / L = 3.3e-3, needs the FP64 tangent: with the FP32
-    one the 41 x 41 run reversed its first steps). Four creases from the centre, sectors
+    (the predictor of this thin plate, t / L = 2.5e-3, needs the FP64 tangent: with the FP32
+    one the run reversed its first steps). Four creases from the centre, sectors
     90 +/- 15 deg (seeded);
     creases 0 and 2 are the drivers (stiff hinges, Kt = 0.1, whose rest angle goes from 0 to
     150 deg with the deployment parameter mu), 1 and 3 passive elastic hinges (Kt = 1e-3);
     three point supports in sector 0. The drivers' load direction is the exact fold-angle
     gradient (an extension: the reference's formula drifts as the fold closes). The KKT
-    system is a dense FP64 LU on the GPU (torch.linalg, standing in for MUMPS), timed on its
-    own line with the host's constraint work."""
+    system is solved on the GPU by a dense FP32 LU refined against the FP64 residual (solver
+    "device_mixed", standing in for MUMPS), timed on its own line with the host's constraint
+    work."""
     import math
 
     from curvami_gb300 import arclength as A
@@ -781,7 +782,7 @@ def arc_length_path(cg, ctx, n_side=31, target_deg=150.0, kmax=80):
     drivers = [A.Driver(0, 0.0, math.radians(target_deg)), A.Driver(2, 0.0, math.radians(target_deg))]
     # ds bounded as for the 13 x 13 plate of the tests (dsmax 2), scaled with the plate's
     # displacement norm (nodes x width).
-    sol = A.ArcLengthSolver(kmax=kmax, max_iters=30, dsmax=2.0 * (n_side / 13.0) ** 2, kkt="device",
+    sol = A.ArcLengthSolver(kmax=kmax, max_iters=30, dsmax=2.0 * (n_side / 13.0) ** 2, kkt="device_mixed",
                             exact_fold_gradient=True)
     t0 = time.perf_counter()
     sol.kinematic_arc_length(prob, np.zeros(prob.ns), drivers)

@@ -226,7 +226,8 @@ class ArcLengthSolver(S.ContinuationSolver):
         self.failed_steps = 0
         self.log: list[str] = []
         self.timing = {"assemble_s": 0.0, "kkt_s": 0.0, "constraints_s": 0.0, "folds_s": 0.0}
-        self.counts = {"assemblies": 0, "kkt_factorisations": 0, "kkt_solves": 0}
+        self.counts = {"assemblies": 0, "kkt_factorisations": 0, "kkt_solves": 0, "kkt_refine_steps": 0,
+                       "kkt_fallbacks": 0}
 
     # -- StepController (StepController.h) --
     def note_reversal(self):
@@ -314,12 +315,15 @@ class ArcLengthSolver(S.ContinuationSolver):
 
     def _kkt(self, K, J, rhs_cols):
         t0 = time.perf_counter()
+        before = dict(S._KKT.stats)
         kkt = S._KKT(K, J, self.kkt)
         self.counts["kkt_factorisations"] += 1
         out = []
         for r in rhs_cols:
             out.append(kkt.solve(r))
             self.counts["kkt_solves"] += 1
+        self.counts["kkt_refine_steps"] += S._KKT.stats["refine_steps"] - before["refine_steps"]
+        self.counts["kkt_fallbacks"] += S._KKT.stats["fallbacks"] - before["fallbacks"]
         self.timing["kkt_s"] += time.perf_counter() - t0
         return out
 

@@ -381,16 +381,84 @@ class _Projector:
         return R - self.J.T @ self._solve(self.J @ R)
 
 
+def gmres_ir(A, lu, piv, b, tol=1e-12, restart=30, max_cycles=4):
+    """Solve A x = b (torch FP64, any device) with GMRES in FP64, right-preconditioned by an
+    LU factorisation made in lower precision (lu, piv: torch.linalg.lu_factor of A in FP32,
+    the factors then held in FP64 so that the preconditioner is applied in FP64 and stays
+    linear): GMRES-based iterative refinement (Carson and Higham, SIAM J. Sci. Comput. 40
+    (2018) A817-A847), which converges for condition numbers far beyond the reach of plain
+    refinement with the same LU. Arnoldi with classical Gram-Schmidt applied twice; the
+    small least-squares problem is solved every step to read the residual. Returns (x,
+    relative residual ||b - A x|| / ||b||, GMRES steps)."""
+    import torch
+
+    def M(v):
+        return torch.linalg.lu_solve(lu, piv, v.unsqueeze(1)).squeeze(1)
+
+    bn = float(torch.linalg.vector_norm(b))
+    if bn == 0.0:
+        return torch.zeros_like(b), 0.0, 0
+    x = M(b)
+    steps = 0
+    rel = float("inf")
+    n = b.numel()
+    for _ in range(max_cycles):
+        r = b - A @ x
+        rn = float(torch.linalg.vector_norm(r))
+        prev, rel = rel, rn / bn
+        if rel <= tol or rel > 0.5 * prev:     # converged, or at the attainable floor
+            break
+        m = min(restart, n)
+        V = torch.zeros((n, m + 1), dtype=b.dtype, device=b.device)
+        H = torch.zeros((m + 1, m), dtype=b.dtype, device=b.device)
+        V[:, 0] = r / rn
+        e1 = torch.zeros(m + 1, dtype=b.dtype, device=b.device)
+        e1[0] = rn
+        y = None
+        k = 0
+        for j in range(m):
+            w = A @ M(V[:, j])
+            for _ in range(2):
+                h = V[:, : j + 1].T @ w
+                w = w - V[:, : j + 1] @ h
+                H[: j + 1, j] += h
+            H[j + 1, j] = torch.linalg.vector_norm(w)
+            k = j + 1
+            steps += 1
+            y = torch.linalg.lstsq(H[: j + 2, : j + 1], e1[: j + 2].unsqueeze(1)).solution.squeeze(1)
+            res = float(torch.linalg.vector_norm(e1[: j + 2] - H[: j + 2, : j + 1] @ y))
+            if res <= tol * bn or float(H[j + 1, j]) <= 1e-300:
+                break
+            V[:, j + 1] = w / H[j + 1, j]
+        x = x + M(V[:, :k] @ y)
+    r = b - A @ x
+    return x, float(torch.linalg.vector_norm(r)) / bn, steps
+
+
 class _KKT:
     """One factorisation of [K J^T; J 0] (K given by its upper triangle), reusable for
-    several right-hand sides: sparse LU on the host or dense FP64 LU on the GPU."""
+    several right-hand sides:
+      "host":         sparse LU on the host (SciPy SuperLU);
+      "device":       dense FP64 LU on the GPU;
+      "device_mixed": dense LU in FP32 on the GPU (GB300 runs FP32 at 62x its FP64 rate) of
+                      the symmetrically equilibrated matrix, then GMRES in FP64 preconditioned
+                      by that LU (gmres_ir) to a residual <= 1e-12 of the right-hand side or
+                      its attainable floor; a solve that ends above 1e-9 falls back to an FP64
+                      LU (made on first need). Plain refinement with the FP32 LU stalls on the larger plates'
+                      KKT matrices (condition beyond 1e8), GMRES does not.
+    The two device modes stand in for the reference's symmetric MUMPS as direct solvers."""
+
+    stats = {"solves": 0, "refine_steps": 0, "fallbacks": 0}   # refine_steps: GMRES steps
 
     def __init__(self, K_upper, J, kkt="host"):
+        if kkt not in ("host", "device", "device_mixed"):
+            raise ValueError("kkt must be 'host', 'device' or 'device_mixed'")
         self.ns = K_upper.shape[0]
         self.nc = J.shape[0]
         K = K_upper + sp.triu(K_upper, k=1).T
         A = sp.bmat([[K, J.T], [J, None]], format="csc") if self.nc else K.tocsc()
-        self.device = kkt == "device"
+        self.mode = kkt
+        self.device = kkt != "host"
         if self.device:
             import torch
 
@@ -401,17 +469,44 @@ class _KKT:
             rows = torch.from_numpy(C.row.astype(np.int64)).to("cuda")
             cols = torch.from_numpy(C.col.astype(np.int64)).to("cuda")
             dense.index_put_((rows, cols), torch.from_numpy(C.data).to("cuda"), accumulate=True)
-            self.lu, self.piv = torch.linalg.lu_factor(dense)
+            if kkt == "device":
+                self.lu, self.piv = torch.linalg.lu_factor(dense)
+            else:
+                # D A D with D = |diag|^-1/2 (the constraint rows, zero on the diagonal,
+                # by their largest entry), then FP32 LU of the scaled matrix.
+                d = dense.diagonal().abs()
+                big = dense.abs().amax(dim=1)
+                self.scale = torch.where(d > 0, d, big).clamp_min(1e-300).rsqrt()
+                self.As = self.scale[:, None] * dense * self.scale[None, :]
+                lu32, self.piv = torch.linalg.lu_factor(self.As.float())
+                self.lu = lu32.double()      # the FP32 factors, applied in FP64
+                self.lu64 = None
         else:
             self.lu = spla.splu(A)
 
+    def _refined(self, b):
+        import torch
+
+        bs = b * self.scale
+        x, rel, steps = gmres_ir(self.As, self.lu, self.piv, bs)
+        _KKT.stats["refine_steps"] += steps
+        if not rel <= 1e-9:
+            _KKT.stats["fallbacks"] += 1
+            if self.lu64 is None:
+                self.lu64 = torch.linalg.lu_factor(self.As)
+            x = torch.linalg.lu_solve(self.lu64[0], self.lu64[1], bs.unsqueeze(1)).squeeze(1)
+        return x * self.scale
+
     def solve(self, rhs):
         b = np.ascontiguousarray(rhs[: self.ns + self.nc], dtype=np.float64)
+        _KKT.stats["solves"] += 1
         if self.device:
             import torch
 
-            bd = torch.from_numpy(b).to("cuda").unsqueeze(1)
-            return torch.linalg.lu_solve(self.lu, self.piv, bd).squeeze(1).cpu().numpy()
+            bd = torch.from_numpy(b).to("cuda")
+            if self.mode == "device_mixed":
+                return self._refined(bd).cpu().numpy()
+            return torch.linalg.lu_solve(self.lu, self.piv, bd.unsqueeze(1)).squeeze(1).cpu().numpy()
         return self.lu.solve(b)
 
 
@@ -422,15 +517,16 @@ class ContinuationSolver:
                  ls_fail_on_no_descent=False, verbose=False, kkt="host", refine_steps=0):
         """kkt: "host" solves the KKT system with a sparse LU on the host (SciPy SuperLU);
         "device" with a dense FP64 LU on the GPU (torch.linalg.lu_factor), for runs whose
-        host factorisations would dominate. Both are direct solves standing in for MUMPS.
+        host factorisations would dominate; "device_mixed" with a dense FP32 LU on the GPU
+        refined against the FP64 residual (see _KKT). All stand in for MUMPS.
 
         refine_steps: iterative refinement of each Newton step against the FP64 residual, for
         a tangent formed in lower precision (the mixed assembly's FP32 K): the action of the
         true tangent on the step is a central difference of the FP64 internal force
         (two residual-only assemblies), and the correction reuses the KKT factorisation. 0
         (the default) is the reference's algorithm exactly."""
-        if kkt not in ("host", "device"):
-            raise ValueError("kkt must be 'host' or 'device'")
+        if kkt not in ("host", "device", "device_mixed"):
+            raise ValueError("kkt must be 'host', 'device' or 'device_mixed'")
         self.kkt = kkt
         self.refine_steps = int(refine_steps)
         self.tol_force, self.tol_energy, self.tol_geom = tol_force, tol_energy, tol_geom

@@ -170,3 +170,27 @@ def test_target_directed_arc_length_oracle(o):
     assert st.load > 0.0
     for d in drivers:
         assert st.angles[d.fold] < 0.0
+
+
+def test_gmres_ir_on_an_ill_conditioned_indefinite_matrix():
+    """gmres_ir (solver.py) with an FP32 LU preconditioner, on the CPU: a symmetric
+    indefinite matrix of condition 1e8 (the KKT matrices of the arc-length runs reach
+    1e7 - 1e9); plain refinement with the same LU stalls there."""
+    import torch
+
+    rng = np.random.default_rng(11)
+    n = 300
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    sv = np.logspace(0, -8, n) * np.where(rng.random(n) < 0.3, -1.0, 1.0)
+    A = torch.from_numpy((Q * sv) @ Q.T)
+    b = torch.from_numpy(rng.standard_normal(n))
+    lu, piv = torch.linalg.lu_factor(A.float())
+    x, rel, steps = S.gmres_ir(A, lu.double(), piv, b)
+    ref = torch.linalg.solve(A, b)
+    assert rel <= 1e-8 and steps <= 60
+    # forward error within the conditioning of the problem (1e8 x 1e-16)
+    assert float((x - ref).norm() / ref.norm()) <= 1e-6
+    xp = torch.linalg.lu_solve(lu, piv, b.float().unsqueeze(1)).squeeze(1).double()
+    for _ in range(20):
+        xp = xp + torch.linalg.lu_solve(lu, piv, (b - A @ xp).float().unsqueeze(1)).squeeze(1).double()
+    assert float((b - A @ xp).norm() / b.norm()) > 1e-6

@@ -59,3 +59,33 @@ def test_kinematic_arc_length_gpu_matches_oracle(ctx):
     print("mixed: iterations", [s.iterations for s in mx.steps], "oracle", [s.iterations for s in ref.steps],
           "worst angle deviation from the oracle path (deg)", worst)
     assert worst <= 0.05
+
+
+def test_mixed_kkt_solve_on_device():
+    """The FP32-LU + FP64-refinement KKT solve against SciPy's sparse LU on arc-length KKT
+    matrices of the four-crease plate (flat and folded states): relative error <= 1e-8
+    (the matrices' condition numbers reach 3e8, so an FP64 direct solve is itself only
+    accurate to about 1e-8)."""
+    import scipy.sparse.linalg as spla
+
+    import scipy.sparse as sp
+
+    o = Oracle(native=True)
+    p, doms, drivers = four_crease_case(target_deg=150.0)
+    prob = oracle_arc_problem(o, p, doms)
+    sol = A.ArcLengthSolver(kmax=8, max_iters=30, dsmax=2.0, exact_fold_gradient=True)
+    states = [np.zeros(prob.ns)]
+    sol.kinematic_arc_length(prob, states[0], drivers, on_converged=lambda k, mu, x, ang: states.append(x.copy()))
+    rng = np.random.default_rng(7)
+    for x in (states[0], states[-1]):
+        K, _ = prob.assemble(x)
+        c_all, J_all = prob.constraints(x)
+        J = sol.filter_rows(J_all)
+        Kf = K + sp.triu(K, k=1).T
+        Afull = sp.bmat([[Kf, J.T], [J, None]], format="csc")
+        b = rng.standard_normal(Afull.shape[0])
+        ref = spla.spsolve(Afull, b)
+        got = S._KKT(K, J, "device_mixed").solve(b)
+        err = float(np.abs(got - ref).max() / np.abs(ref).max())
+        print("device_mixed KKT error", err, S._KKT.stats)
+        assert err <= 1e-8
