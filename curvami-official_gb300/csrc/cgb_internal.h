@@ -124,6 +124,7 @@ struct cgb_shape {
   cgb::DevBuf<double> scr_gind;   // n_creases * 6 * n_gp
   cgb::DevBuf<int8_t> scr_bad;    // n_gp
   cgb::DevBuf<float4> scr_node_pair;  // 2 * n_nodes, mixed precision only
+  cgb::DevBuf<float> scr_point_rec;   // point records of the mixed RKPM, n_gp x record floats
 };
 
 // Per-fold data kept by the assembler (plate/PlateData.h: Fold; Constraints.h:341).

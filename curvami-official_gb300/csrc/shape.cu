@@ -480,8 +480,8 @@ __global__ void __launch_bounds__(kThreads) rkpm_kernel(RkpmArgs a) {
 // The FP64 kernel spends about 650 FP64 operations per neighbour (differences and
 // divisions by rho, the window jets with their divisions by s, the crease product, the
 // 90 moment FMAs, then the jets again and the shape-function sums), and GB300 issues FP64
-// at 1/62 of the FP32 rate. rkpm_pair_kernel does all of that per-neighbour arithmetic in
-// FP32 pairs (cgb_pair.cuh, about 48 significant bits) on the FP32 pipe, and keeps FP64
+// at 1/62 of the FP32 rate. The mixed kernels do all of that per-neighbour arithmetic in
+// FP32 pairs (cgb_pair.cuh, about 48 significant bits) on the FP32 pipe, and keep FP64
 // for the per-point part: the raw-moment sums are rounded to FP64 and point_solve forms
 // M and its jets, applies the reference's guards, factors M (LDL^T) and solves for row 0
 // of M^-1 and its jets exactly as the FP64 kernel does. Only the per-point factorisation
@@ -684,18 +684,34 @@ __device__ __forceinline__ void pair_moment_sums(const RkpmArgs& a, const PairPo
     for (int k = 0; k < NR; ++k) Sd[J0 + q][k] = fp2_to_double(S[q][k]);
 }
 
-// Launch shape of the pair kernel, measured on the 1,000,000-point stage (RKPM phase,
-// order 2): 3 blocks per SM (168 registers, some spills) 11.3 ms; 1 block (255 registers)
-// 12.0 ms; the moment sums split into two passes of three jets 13.3 - 14.1 ms at 128 -
-// 255 registers. The kernel is latency-bound at every shape (2 - 4 warps per scheduler),
-// so the shape matters little; order 3 (28 raw moments) needs the split to stay in
+// The mixed RKPM runs as two kernels:
+//  - rkpm_pair_point_kernel, one Gauss point per thread: the raw-moment sums in pairs over
+//    the point's neighbours, the per-point FP64 solve, and a point record for the second
+//    kernel (the point's coordinates split in three floats, its crease indicators scaled
+//    for the visibility product, and row 0 of M^-1 with its five jets, all as pairs);
+//  - rkpm_pair_value_kernel, one (point, neighbour) pair per thread: the weight and basis
+//    jets of that neighbour and Phi, grad Phi, Hessian Phi from the point record.
+// Split this way the per-pair half runs at full occupancy instead of inside a thread
+// that holds 90 pair accumulators, and each kernel's code fits the instruction cache.
+//
+// Launch shape of the point kernel, measured on the 1,000,000-point stage (order 2; RKPM
+// phase of both kernels): 2 blocks per SM (255 registers) 8.24 ms, 3 blocks (168 registers,
+// more spills) 8.80 ms; before the split, one kernel doing both passes took 11.3 ms. Order 3
+// (28 raw moments) sums the jets in two passes of three to keep the accumulators in
 // registers.
-constexpr int kPairMinBlocks = 3;
+constexpr int kPairMinBlocks = 2;
 constexpr int kPairSplitOrder = 3;
+constexpr int kPairValueThreads = 256;
 
-// GlobalRKPM.h:59-397 for one Gauss point per thread, per-neighbour work in FP32 pairs.
+// Floats per point record: 6 coordinate parts, 12 per crease (6 pairs), 12 per basis
+// function (6 jets x 1 pair), rounded up to 4 so every record starts on 16 bytes.
+__host__ __device__ constexpr int pair_record_floats(int order, int n_creases) {
+  return (6 + 12 * n_creases + 6 * (order + 1) * (order + 2) + 3) & ~3;
+}
+
 template <int ORDER>
-__global__ void __launch_bounds__(kThreads, kPairMinBlocks) rkpm_pair_kernel(RkpmArgs a) {
+__global__ void __launch_bounds__(kThreads, kPairMinBlocks) rkpm_pair_point_kernel(RkpmArgs a, float* __restrict__ rec,
+                                                                                   int RS) {
   constexpr int NP = (ORDER + 1) * (ORDER + 2) / 2;
   using RI = RawIdx<ORDER>;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -716,8 +732,6 @@ __global__ void __launch_bounds__(kThreads, kPairMinBlocks) rkpm_pair_kernel(Rkp
     P.gc[6 * c + 4] = fp2_from_double(r2 * I[4]);
     P.gc[6 * c + 5] = fp2_from_double(r2 * I[5]);
   }
-  // Moment sums: all six jets in one pass up to ORDER 2; two passes of three jets for
-  // ORDER 3 (28 raw moments), which keeps the pair accumulators in registers.
   double Sd[6][RI::NR];
   if constexpr (ORDER < kPairSplitOrder) {
     pair_moment_sums<ORDER, 0, 6>(a, P, p0, p1, Sd);
@@ -727,54 +741,90 @@ __global__ void __launch_bounds__(kThreads, kPairMinBlocks) rkpm_pair_kernel(Rkp
   }
   RowJets<ORDER> R;
   a.bad[g] = static_cast<int8_t>(point_solve<ORDER>(Sd[0], Sd[1], Sd[2], Sd[3], Sd[4], Sd[5], R));
-  fp2 c0[NP], c0x[NP], c0y[NP], c0xx[NP], c0yy[NP], c0xy[NP], c0x2[NP], c0y2[NP];
+  float* out = rec + static_cast<int64_t>(g) * RS;
+  out[0] = P.gx0; out[1] = P.gx1; out[2] = P.gx2;
+  out[3] = P.gy0; out[4] = P.gy1; out[5] = P.gy2;
+  for (int c = 0; c < 6 * P.nc; ++c) {
+    out[6 + 2 * c] = P.gc[c].hi;
+    out[7 + 2 * c] = P.gc[c].lo;
+  }
+  float2* cj = reinterpret_cast<float2*>(out + 6 + 12 * P.nc);
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
-    c0[i] = fp2_from_double(R.c0[i]);
-    c0x[i] = fp2_from_double(R.c0x[i]);
-    c0y[i] = fp2_from_double(R.c0y[i]);
-    c0xx[i] = fp2_from_double(R.c0xx[i]);
-    c0yy[i] = fp2_from_double(R.c0yy[i]);
-    c0xy[i] = fp2_from_double(R.c0xy[i]);
-    c0x2[i] = c0x[i] * 2.0f;
-    c0y2[i] = c0y[i] * 2.0f;
+    fp2 v = fp2_from_double(R.c0[i]);   cj[i] = make_float2(v.hi, v.lo);
+    v = fp2_from_double(R.c0x[i]);      cj[NP + i] = make_float2(v.hi, v.lo);
+    v = fp2_from_double(R.c0y[i]);      cj[2 * NP + i] = make_float2(v.hi, v.lo);
+    v = fp2_from_double(R.c0xx[i]);     cj[3 * NP + i] = make_float2(v.hi, v.lo);
+    v = fp2_from_double(R.c0yy[i]);     cj[4 * NP + i] = make_float2(v.hi, v.lo);
+    v = fp2_from_double(R.c0xy[i]);     cj[5 * NP + i] = make_float2(v.hi, v.lo);
   }
-  // Shape functions (GlobalRKPM.h:363-396).
-  for (int64_t e = p0; e < p1; ++e) {
-    const int j = a.idx[e];
-    fp2 xi, eta, fac;
-    pair_xi(a, P, j, xi, eta, fac);
-    const JetsP J = weight_jets_pair(a.kernel, xi, eta, fac, P.scaled, P.nc, P.gc, a.node_side, a.n_nodes, j);
-    const BasisPair<ORDER> B(xi, eta);
-    const fp2 z{0.0f, 0.0f};
-    fp2 C = z, Cx = z, Cy = z, Cxx = z, Cyy = z, Cxy = z;
-#pragma unroll
-    for (int jp = 0; jp < NP; ++jp) {
-      fp2_fma_acc(C, c0[jp], B.p[jp]);
-      fp2_fma_acc(Cx, c0x[jp], B.p[jp]); fp2_fma_acc(Cx, c0[jp], B.px[jp]);
-      fp2_fma_acc(Cy, c0y[jp], B.p[jp]); fp2_fma_acc(Cy, c0[jp], B.py[jp]);
-      fp2_fma_acc(Cxx, c0xx[jp], B.p[jp]); fp2_fma_acc(Cxx, c0x2[jp], B.px[jp]); fp2_fma_acc(Cxx, c0[jp], B.pxx[jp]);
-      fp2_fma_acc(Cyy, c0yy[jp], B.p[jp]); fp2_fma_acc(Cyy, c0y2[jp], B.py[jp]); fp2_fma_acc(Cyy, c0[jp], B.pyy[jp]);
-      fp2_fma_acc(Cxy, c0xy[jp], B.p[jp]); fp2_fma_acc(Cxy, c0x[jp], B.py[jp]);
-      fp2_fma_acc(Cxy, c0y[jp], B.px[jp]); fp2_fma_acc(Cxy, c0[jp], B.pxy[jp]);
+}
+
+// Shape functions (GlobalRKPM.h:363-396) of one (point, neighbour) pair per thread. The
+// point of pair e is the last g with ptr[g] <= e: lane 0 of each warp finds it for the
+// warp's first pair by bisection, the other lanes step forward from there.
+template <int ORDER>
+__global__ void __launch_bounds__(kPairValueThreads) rkpm_pair_value_kernel(RkpmArgs a, const float* __restrict__ rec,
+                                                                            int RS, int64_t nnz) {
+  constexpr int NP = (ORDER + 1) * (ORDER + 2) / 2;
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  int g0 = 0;
+  if (lane == 0) {
+    const int64_t ef = e < nnz ? e : nnz - 1;
+    int lo = 0, hi = a.n_gp;             // ptr[lo] <= ef < ptr[hi]
+    while (hi - lo > 1) {
+      const int mid = lo + (hi - lo) / 2;
+      if (__ldg(a.ptr + mid) <= ef) lo = mid; else hi = mid;
     }
-    C = fp2_norm(C); Cx = fp2_norm(Cx); Cy = fp2_norm(Cy);
-    Cxx = fp2_norm(Cxx); Cyy = fp2_norm(Cyy); Cxy = fp2_norm(Cxy);
-    const fp2* w = J.v;
-    fp2 gx = z, gy = z, hxx = z, hyy = z, hxy = z;
-    fp2_fma_acc(gx, Cx, w[0]); fp2_fma_acc(gx, C, w[1]);
-    fp2_fma_acc(gy, Cy, w[0]); fp2_fma_acc(gy, C, w[2]);
-    const fp2 Cx2 = Cx * 2.0f, Cy2 = Cy * 2.0f;
-    fp2_fma_acc(hxx, Cxx, w[0]); fp2_fma_acc(hxx, Cx2, w[1]); fp2_fma_acc(hxx, C, w[3]);
-    fp2_fma_acc(hyy, Cyy, w[0]); fp2_fma_acc(hyy, Cy2, w[2]); fp2_fma_acc(hyy, C, w[4]);
-    fp2_fma_acc(hxy, Cxy, w[0]); fp2_fma_acc(hxy, Cx, w[2]); fp2_fma_acc(hxy, Cy, w[1]); fp2_fma_acc(hxy, C, w[5]);
-    a.psi[e] = fp2_to_double(C * w[0]);
-    a.dpsi[2 * e] = fp2_to_double(fp2_norm(gx) * a.irho);
-    a.dpsi[2 * e + 1] = fp2_to_double(fp2_norm(gy) * a.irho);
-    a.ddpsi[3 * e] = fp2_to_double(fp2_norm(hxx) * a.irho2);
-    a.ddpsi[3 * e + 1] = fp2_to_double(fp2_norm(hyy) * a.irho2);
-    a.ddpsi[3 * e + 2] = fp2_to_double(fp2_norm(hxy) * a.irho2);
+    g0 = lo;
   }
+  g0 = __shfl_sync(0xffffffffu, g0, 0);
+  if (e >= nnz) return;
+  int g = g0;
+  while (__ldg(a.ptr + g + 1) <= e) ++g;
+  const float* R = rec + static_cast<int64_t>(g) * RS;
+  const int nc = a.n_creases < 4 ? a.n_creases : 4;
+  const fp2* gc = reinterpret_cast<const fp2*>(R + 6);
+  const fp2* cj = reinterpret_cast<const fp2*>(R + 6 + 12 * nc);
+  const int j = a.idx[e];
+  const float4 n0 = __ldg(a.node_pair + 2 * j), n1 = __ldg(a.node_pair + 2 * j + 1);
+  const fp2 xi = diff3(__ldg(R), __ldg(R + 1), __ldg(R + 2), n0.x, n0.y, n0.z) * a.irho;
+  const fp2 eta = diff3(__ldg(R + 3), __ldg(R + 4), __ldg(R + 5), n0.w, n1.x, n1.y) * a.irho;
+  const fp2 fac{n1.z, n1.w};
+  const JetsP J = weight_jets_pair(a.kernel, xi, eta, fac, a.rho_node != nullptr, nc, gc, a.node_side, a.n_nodes, j);
+  const BasisPair<ORDER> B(xi, eta);
+  const fp2 z{0.0f, 0.0f};
+  fp2 C = z, Cx = z, Cy = z, Cxx = z, Cyy = z, Cxy = z;
+#pragma unroll
+  for (int jp = 0; jp < NP; ++jp) {
+    const fp2 c0 = cj[jp], c0x = cj[NP + jp], c0y = cj[2 * NP + jp];
+    const fp2 c0xx = cj[3 * NP + jp], c0yy = cj[4 * NP + jp], c0xy = cj[5 * NP + jp];
+    const fp2 c0x2 = c0x * 2.0f, c0y2 = c0y * 2.0f;
+    fp2_fma_acc(C, c0, B.p[jp]);
+    fp2_fma_acc(Cx, c0x, B.p[jp]); fp2_fma_acc(Cx, c0, B.px[jp]);
+    fp2_fma_acc(Cy, c0y, B.p[jp]); fp2_fma_acc(Cy, c0, B.py[jp]);
+    fp2_fma_acc(Cxx, c0xx, B.p[jp]); fp2_fma_acc(Cxx, c0x2, B.px[jp]); fp2_fma_acc(Cxx, c0, B.pxx[jp]);
+    fp2_fma_acc(Cyy, c0yy, B.p[jp]); fp2_fma_acc(Cyy, c0y2, B.py[jp]); fp2_fma_acc(Cyy, c0, B.pyy[jp]);
+    fp2_fma_acc(Cxy, c0xy, B.p[jp]); fp2_fma_acc(Cxy, c0x, B.py[jp]);
+    fp2_fma_acc(Cxy, c0y, B.px[jp]); fp2_fma_acc(Cxy, c0, B.pxy[jp]);
+  }
+  C = fp2_norm(C); Cx = fp2_norm(Cx); Cy = fp2_norm(Cy);
+  Cxx = fp2_norm(Cxx); Cyy = fp2_norm(Cyy); Cxy = fp2_norm(Cxy);
+  const fp2* w = J.v;
+  fp2 gx = z, gy = z, hxx = z, hyy = z, hxy = z;
+  fp2_fma_acc(gx, Cx, w[0]); fp2_fma_acc(gx, C, w[1]);
+  fp2_fma_acc(gy, Cy, w[0]); fp2_fma_acc(gy, C, w[2]);
+  const fp2 Cx2 = Cx * 2.0f, Cy2 = Cy * 2.0f;
+  fp2_fma_acc(hxx, Cxx, w[0]); fp2_fma_acc(hxx, Cx2, w[1]); fp2_fma_acc(hxx, C, w[3]);
+  fp2_fma_acc(hyy, Cyy, w[0]); fp2_fma_acc(hyy, Cy2, w[2]); fp2_fma_acc(hyy, C, w[4]);
+  fp2_fma_acc(hxy, Cxy, w[0]); fp2_fma_acc(hxy, Cx, w[2]); fp2_fma_acc(hxy, Cy, w[1]); fp2_fma_acc(hxy, C, w[5]);
+  a.psi[e] = fp2_to_double(C * w[0]);
+  a.dpsi[2 * e] = fp2_to_double(fp2_norm(gx) * a.irho);
+  a.dpsi[2 * e + 1] = fp2_to_double(fp2_norm(gy) * a.irho);
+  a.ddpsi[3 * e] = fp2_to_double(fp2_norm(hxx) * a.irho2);
+  a.ddpsi[3 * e + 1] = fp2_to_double(fp2_norm(hyy) * a.irho2);
+  a.ddpsi[3 * e + 2] = fp2_to_double(fp2_norm(hxy) * a.irho2);
 }
 
 inline unsigned blocks_for(int64_t n, int t = kThreads) { return static_cast<unsigned>((n + t - 1) / t); }
@@ -950,10 +1000,23 @@ void shape_values(cgb_context* ctx, cgb_shape* out, const std::vector<Crease>& c
   }
   if (n_gp > 0) {
     if (mixed) {
+      const int RS = pair_record_floats(out->order, nc);
+      out->scr_point_rec.ensure(static_cast<size_t>(n_gp) * RS);
+      float* rec = out->scr_point_rec.p;
+      const unsigned vb = blocks_for(std::max<int64_t>(nnz, 1), kPairValueThreads);
       switch (out->order) {
-        case 1: rkpm_pair_kernel<1><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
-        case 2: rkpm_pair_kernel<2><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
-        default: rkpm_pair_kernel<3><<<blocks_for(n_gp), kThreads, 0, st>>>(ra); break;
+        case 1:
+          rkpm_pair_point_kernel<1><<<blocks_for(n_gp), kThreads, 0, st>>>(ra, rec, RS);
+          if (nnz > 0) rkpm_pair_value_kernel<1><<<vb, kPairValueThreads, 0, st>>>(ra, rec, RS, nnz);
+          break;
+        case 2:
+          rkpm_pair_point_kernel<2><<<blocks_for(n_gp), kThreads, 0, st>>>(ra, rec, RS);
+          if (nnz > 0) rkpm_pair_value_kernel<2><<<vb, kPairValueThreads, 0, st>>>(ra, rec, RS, nnz);
+          break;
+        default:
+          rkpm_pair_point_kernel<3><<<blocks_for(n_gp), kThreads, 0, st>>>(ra, rec, RS);
+          if (nnz > 0) rkpm_pair_value_kernel<3><<<vb, kPairValueThreads, 0, st>>>(ra, rec, RS, nnz);
+          break;
       }
     } else {
       switch (out->order) {
@@ -963,7 +1026,7 @@ void shape_values(cgb_context* ctx, cgb_shape* out, const std::vector<Crease>& c
       }
     }
   }
-  prof_end(ctx, CGB_PHASE_RKPM, (n_gp > 0 ? 1 : 0) + (mixed && n_nodes > 0 ? 1 : 0));
+  prof_end(ctx, CGB_PHASE_RKPM, (n_gp > 0 ? 1 : 0) + (mixed && n_nodes > 0 ? 1 : 0) + (mixed && nnz > 0 ? 1 : 0));
   CGB_CUDA(cudaGetLastError());
   std::vector<int8_t> hbad(n_gp);
   if (n_gp > 0) CGB_CUDA(cudaMemcpyAsync(hbad.data(), bad, n_gp, cudaMemcpyDeviceToHost, st));
