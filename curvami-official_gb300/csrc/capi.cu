@@ -327,6 +327,8 @@ int cgb_shape_download(const cgb_shape* sh, int64_t* nbr_ptr, int32_t* nbr_idx, 
     };
     get(nbr_ptr, sh->nbr_ptr.p, (sh->n_gp + 1) * sizeof(int64_t));
     get(nbr_idx, sh->nbr_idx.p, sh->nnz * sizeof(int32_t));
+    // s is a cache of derived data: a mixed-precision set fills it on the first request.
+    if (s) cgb::shape_distances(const_cast<cgb_shape*>(sh));
     if (s && sh->s.n >= static_cast<size_t>(sh->nnz)) get(s, sh->s.p, sh->nnz * sizeof(double));
     get(psi, sh->psi.p, sh->nnz * sizeof(double));
     get(dpsi, sh->dpsi.p, 2 * sh->nnz * sizeof(double));

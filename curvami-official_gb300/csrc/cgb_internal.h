@@ -234,6 +234,9 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
 // Phi and its derivatives of an existing set recomputed in place with other creases
 // (same points, radius and so neighbour lists).
 void shape_rebuild(cgb_shape* sh, const std::vector<Crease>& creases);
+// The normalised distances s of a set built in mixed precision (which skips them), computed
+// on demand with the FRNN's rounded operations; a no-op when the set has them.
+void shape_distances(cgb_shape* sh);
 // pattern.cu
 void pattern_build(cgb_assembler* a);
 void deterministic_prepare(cgb_assembler* a);

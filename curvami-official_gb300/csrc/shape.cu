@@ -64,7 +64,7 @@ __global__ void frnn_kernel(int n_gp, const double* __restrict__ gp_xy,
         if (dist2 <= r2) {
           if (out_idx) {
             out_idx[pos] = j;
-            out_s[pos] = __ddiv_rn(__dsqrt_rn(dist2), r);
+            if (out_s) out_s[pos] = __ddiv_rn(__dsqrt_rn(dist2), r);
             ++pos;
           }
           ++cnt;
@@ -73,6 +73,76 @@ __global__ void frnn_kernel(int n_gp, const double* __restrict__ gp_xy,
     }
   }
   if (!out_idx) count[g] = cnt;
+}
+
+// Normalised distances s of an existing neighbour list, with the FRNN's own rounded
+// operations (so bitwise equal to what frnn_kernel writes); sets built in mixed
+// precision skip s in the FRNN and compute it here when a caller downloads it.
+__global__ void distance_kernel(int n_gp, const double* __restrict__ gp_xy, const double* __restrict__ node_xy,
+                                const double* __restrict__ rho_node, double rho, const int64_t* __restrict__ ptr,
+                                const int32_t* __restrict__ idx, double* __restrict__ out_s) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_gp) return;
+  const double gx = gp_xy[2 * g], gy = gp_xy[2 * g + 1];
+  for (int64_t e = ptr[g]; e < ptr[g + 1]; ++e) {
+    const int j = idx[e];
+    const double ddx = __dsub_rn(node_xy[2 * j], gx);
+    const double ddy = __dsub_rn(node_xy[2 * j + 1], gy);
+    const double dist2 = __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy));
+    const double r = rho_node ? rho_node[j] : rho;
+    out_s[e] = __ddiv_rn(__dsqrt_rn(dist2), r);
+  }
+}
+
+// Neighbour counts -> CSR offsets on the device: ptr[g + 1] = sum of cnt[0..g], plus the
+// total and the largest count for the host (two numbers instead of the whole array).
+constexpr int kScanThreads = 1024;
+
+__global__ void scan_local_kernel(int n, const int32_t* __restrict__ cnt, int64_t* __restrict__ ptr,
+                                  int64_t* __restrict__ block_sum, int32_t* __restrict__ block_max) {
+  __shared__ int64_t sv[kScanThreads];
+  __shared__ int32_t mv[kScanThreads];
+  const int t = threadIdx.x;
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * kScanThreads + t;
+  const int32_t c = i < n ? cnt[i] : 0;
+  sv[t] = c;
+  mv[t] = c;
+  __syncthreads();
+  for (int off = 1; off < kScanThreads; off <<= 1) {   // Hillis-Steele inclusive scan
+    const int64_t a = t >= off ? sv[t - off] : 0;
+    const int32_t m = t >= off ? mv[t - off] : 0;
+    __syncthreads();
+    sv[t] += a;
+    mv[t] = max(mv[t], m);
+    __syncthreads();
+  }
+  if (i < n) ptr[i + 1] = sv[t];
+  if (t == kScanThreads - 1) {
+    block_sum[blockIdx.x] = sv[t];
+    block_max[blockIdx.x] = mv[t];
+  }
+}
+
+// One thread: block totals -> exclusive block offsets (in place); totals[0] = nnz, [1] = max.
+__global__ void scan_blocks_kernel(int nb, int64_t* __restrict__ block_sum, const int32_t* __restrict__ block_max,
+                                   int64_t* __restrict__ totals) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  int64_t run = 0;
+  int32_t mx = 0;
+  for (int b = 0; b < nb; ++b) {
+    const int64_t v = block_sum[b];
+    block_sum[b] = run;
+    run += v;
+    mx = max(mx, block_max[b]);
+  }
+  totals[0] = run;
+  totals[1] = mx;
+}
+
+__global__ void scan_add_kernel(int n, int64_t* __restrict__ ptr, const int64_t* __restrict__ block_off) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * kScanThreads + threadIdx.x;
+  if (i < n) ptr[i + 1] += block_off[blockIdx.x];
+  if (i == 0) ptr[0] = 0;
 }
 
 // Per-node crease side sn = (f >= 0 ? +1 : -1) (GlobalRKPM.h:92-93).
@@ -908,28 +978,38 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
                                                         nullptr, d_cnt.p, nullptr, nullptr);
   CGB_CUDA(cudaGetLastError());
   prof_end(ctx, CGB_PHASE_FRNN, n_gp > 0 ? 1 : 0);
-  std::vector<int32_t> cnt(n_gp);
-  if (n_gp > 0)
-    CGB_CUDA(cudaMemcpyAsync(cnt.data(), d_cnt.p, sizeof(int32_t) * n_gp, cudaMemcpyDeviceToHost, st));
-  CGB_CUDA(cudaStreamSynchronize(st));
-  std::vector<int64_t> ptr(n_gp + 1, 0);
-  int max_n = 0;
-  for (int g = 0; g < n_gp; ++g) {
-    ptr[g + 1] = ptr[g] + cnt[g];
-    max_n = std::max(max_n, cnt[g]);
+  // CSR offsets on the device; only the total and the largest count come back.
+  out->nbr_ptr.alloc(static_cast<size_t>(n_gp) + 1);
+  int64_t totals[2] = {0, 0};
+  if (n_gp > 0) {
+    const int nb = static_cast<int>((static_cast<int64_t>(n_gp) + kScanThreads - 1) / kScanThreads);
+    DevBuf<int64_t> bsum(nb), tot(2);
+    DevBuf<int32_t> bmax(nb);
+    scan_local_kernel<<<nb, kScanThreads, 0, st>>>(n_gp, d_cnt.p, out->nbr_ptr.p, bsum.p, bmax.p);
+    scan_blocks_kernel<<<1, 1, 0, st>>>(nb, bsum.p, bmax.p, tot.p);
+    scan_add_kernel<<<nb, kScanThreads, 0, st>>>(n_gp, out->nbr_ptr.p, bsum.p);
+    CGB_CUDA(cudaGetLastError());
+    CGB_CUDA(cudaMemcpyAsync(totals, tot.p, sizeof(totals), cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+  } else {
+    CGB_CUDA(cudaMemsetAsync(out->nbr_ptr.p, 0, sizeof(int64_t), st));
   }
-  const int64_t nnz = ptr[n_gp];
+  const int64_t nnz = totals[0];
   if (nnz >= (1LL << 31)) throw Error(CGB_ERR_CAPACITY, "cgb_shape_build: more than 2^31 neighbour entries");
   out->nnz = nnz;
-  out->max_n = max_n;
-  upload(out->nbr_ptr, ptr.data(), ptr.size(), st);
+  out->max_n = static_cast<int>(totals[1]);
   out->nbr_idx.alloc(nnz);
-  out->s.alloc(nnz);
+  // The mixed RKPM recomputes distances in FP32 pairs and does not read s, so a mixed set
+  // skips the FRNN's rounded square roots and divisions; cgb_shape_download computes s on
+  // demand (shape_distances), bitwise equal.
+  const bool want_s = prm.precision != CGB_SHAPE_MIXED;
+  if (want_s) out->s.alloc(nnz); else out->s.reset();
   prof_begin(ctx, CGB_PHASE_FRNN);
   if (n_gp > 0)
     frnn_kernel<<<blocks_for(n_gp), kThreads, 0, st>>>(n_gp, out->gp_xy.p, ctx->node_xy.p,
                                                         d_rn, prm.rho, rho2, G,
-                                                        out->nbr_ptr.p, nullptr, out->nbr_idx.p, out->s.p);
+                                                        out->nbr_ptr.p, nullptr, out->nbr_idx.p,
+                                                        want_s ? out->s.p : nullptr);
   prof_end(ctx, CGB_PHASE_FRNN, n_gp > 0 ? 1 : 0);
   CGB_CUDA(cudaGetLastError());
 
@@ -1060,6 +1140,21 @@ void shape_values(cgb_context* ctx, cgb_shape* out, const std::vector<Crease>& c
                     " with " + std::to_string(count_of(f2)) +
                     " neighbours). Same cause and remedies as a singular moment matrix.");
   }
+}
+
+void shape_distances(cgb_shape* sh) {
+  cgb_context* ctx = sh->ctx;
+  // Only sets built here in mixed precision lack s; wrapped or concatenated sets without
+  // distances keep returning none, as before.
+  if (sh->nnz == 0 || sh->s.n >= static_cast<size_t>(sh->nnz) || !sh->rebuildable) return;
+  if (ctx->node_gen != sh->node_gen)
+    throw Error(CGB_ERR_INVALID, "cgb_shape_download: s is computed on demand for mixed-precision sets and the "
+                                 "nodes changed since the set was built (cgb_set_nodes)");
+  sh->s.alloc(sh->nnz);
+  distance_kernel<<<blocks_for(sh->n_gp), kThreads, 0, ctx->stream>>>(
+      sh->n_gp, sh->gp_xy.p, ctx->node_xy.p, sh->has_rho_node ? sh->rho_node.p : nullptr, sh->rho, sh->nbr_ptr.p,
+      sh->nbr_idx.p, sh->s.p);
+  CGB_CUDA(cudaGetLastError());
 }
 
 void shape_rebuild(cgb_shape* sh, const std::vector<Crease>& creases) {

@@ -137,7 +137,10 @@ int cgb_shape_from_host(cgb_context* ctx, int n_gp, const int64_t* nbr_ptr,
                         const int32_t* nbr_idx, const double* psi, const double* dpsi,
                         const double* ddpsi, cgb_shape** out);
 int cgb_shape_size(const cgb_shape* sh, int* n_gp, int64_t* nnz, int* max_neighbours);
-/* Copy results to host arrays; any pointer may be NULL. */
+/* Copy results to host arrays; any pointer may be NULL. A set built with
+ * CGB_SHAPE_MIXED does not keep the distances s (its RKPM does not read them); the first
+ * download that asks for s computes them, bitwise equal to an FP64 build's, and needs the
+ * context's nodes unchanged since the build. */
 int cgb_shape_download(const cgb_shape* sh, int64_t* nbr_ptr, int32_t* nbr_idx, double* s,
                        double* psi, double* dpsi, double* ddpsi);
 /* Device pointers of the shape arrays (for callers that keep data on the GPU). */

@@ -2,7 +2,8 @@
 
 The mixed kernel sums every per-neighbour term in FP32 pairs (about 48 significant bits)
 and factors the moment matrix per point in FP64. Bars, relative to each array's scale:
-- the neighbour lists are the FP64 mode's (same FRNN): bit-exact;
+- the neighbour lists are the FP64 mode's (same FRNN): bit-exact, and so are the distances
+  s, which a mixed set computes only when downloaded;
 - points whose support no crease truncates: Phi, grad Phi, Hessian Phi within 1e-11 of
   the oracle (the pair sums' rounding, ~1e-14, times the moment matrix's conditioning);
 - all points: within 1e-6 (crease-truncated supports are ill-conditioned; two FP64
@@ -78,6 +79,8 @@ def test_mixed_shape_functions_against_oracle(o, ctx, name):
     fp = cg.shape_functions(ctx, p.faces.xy, **kw(p)).download()
     ref = oracle_shapes(o, p, p.faces.xy)
     assert np.array_equal(mx["ptr"], ref["ptr"]) and np.array_equal(mx["idx"], ref["idx"])
+    # s is computed on demand for a mixed set, with the FRNN's own rounded operations
+    assert np.array_equal(mx["s"], ref["s"])
     far = np.repeat(crease_distance(p, p.faces.xy) > p.rho, np.diff(ref["ptr"]))
     errs = {}
     for k in ("psi", "dpsi", "ddpsi"):  # arrays are (nnz,), (nnz, 2), (nnz, 3)
@@ -103,6 +106,7 @@ def test_mixed_per_node_radius(o, ctx):
     mx = cg.shape_functions(ctx, pts, precision="mixed", **kw(plate)).download()
     ref = oracle_shapes(o, plate, pts)
     assert np.array_equal(mx["ptr"], ref["ptr"]) and np.array_equal(mx["idx"], ref["idx"])
+    assert np.array_equal(mx["s"], ref["s"])
     far_pt = crease_distance(plate, pts) > 1.75
     far = np.repeat(far_pt, np.diff(ref["ptr"]))
     for k in ("psi", "dpsi", "ddpsi"):
