@@ -450,25 +450,42 @@ class _KKT:
 
     stats = {"solves": 0, "refine_steps": 0, "fallbacks": 0}   # refine_steps: GMRES steps
 
-    def __init__(self, K_upper, J, kkt="host"):
+    def __init__(self, K_upper, J, kkt="host", device="cuda"):
+        """device: where the two dense modes run (a torch device; "cuda" for the GPU)."""
         if kkt not in ("host", "device", "device_mixed"):
             raise ValueError("kkt must be 'host', 'device' or 'device_mixed'")
         self.ns = K_upper.shape[0]
         self.nc = J.shape[0]
-        K = K_upper + sp.triu(K_upper, k=1).T
-        A = sp.bmat([[K, J.T], [J, None]], format="csc") if self.nc else K.tocsc()
         self.mode = kkt
         self.device = kkt != "host"
         if self.device:
             import torch
 
-            # Only the nonzeros cross to the GPU; the dense matrix is formed there.
-            C = A.tocoo()
-            n = A.shape[0]
-            dense = torch.zeros((n, n), dtype=torch.float64, device="cuda")
-            rows = torch.from_numpy(C.row.astype(np.int64)).to("cuda")
-            cols = torch.from_numpy(C.col.astype(np.int64)).to("cuda")
-            dense.index_put_((rows, cols), torch.from_numpy(C.data).to("cuda"), accumulate=True)
+            # Only the nonzeros cross to the GPU and the dense symmetric matrix is formed
+            # there: K's stored upper triangle into both triangles, J into its two blocks
+            # (no sparse symmetrisation or block assembly on the host).
+            Kc = K_upper.tocsc()
+            kr = Kc.indices.astype(np.int64)
+            kc = np.repeat(np.arange(self.ns, dtype=np.int64), np.diff(Kc.indptr))
+            keep = kr <= kc
+            kr, kc, kv = kr[keep], kc[keep], Kc.data[keep]
+            Jo = J.tocoo()
+            n = self.ns + self.nc
+            dev = device
+            self.dev = dev
+            dense = torch.zeros((n, n), dtype=torch.float64, device=dev)
+            r = torch.from_numpy(kr).to(dev)
+            c = torch.from_numpy(kc).to(dev)
+            v = torch.from_numpy(kv).to(dev)
+            dense.index_put_((r, c), v, accumulate=True)
+            off = r != c
+            dense.index_put_((c[off], r[off]), v[off], accumulate=True)
+            if self.nc:
+                jr = torch.from_numpy(Jo.row.astype(np.int64) + self.ns).to(dev)
+                jc = torch.from_numpy(Jo.col.astype(np.int64)).to(dev)
+                jv = torch.from_numpy(Jo.data).to(dev)
+                dense.index_put_((jr, jc), jv, accumulate=True)
+                dense.index_put_((jc, jr), jv, accumulate=True)
             if kkt == "device":
                 self.lu, self.piv = torch.linalg.lu_factor(dense)
             else:
@@ -482,6 +499,8 @@ class _KKT:
                 self.lu = lu32.double()      # the FP32 factors, applied in FP64
                 self.lu64 = None
         else:
+            K = K_upper + sp.triu(K_upper, k=1).T
+            A = sp.bmat([[K, J.T], [J, None]], format="csc") if self.nc else K.tocsc()
             self.lu = spla.splu(A)
 
     def _refined(self, b):
@@ -503,7 +522,7 @@ class _KKT:
         if self.device:
             import torch
 
-            bd = torch.from_numpy(b).to("cuda")
+            bd = torch.from_numpy(b).to(self.dev)
             if self.mode == "device_mixed":
                 return self._refined(bd).cpu().numpy()
             return torch.linalg.lu_solve(self.lu, self.piv, bd.unsqueeze(1)).squeeze(1).cpu().numpy()

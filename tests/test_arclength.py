@@ -194,3 +194,23 @@ def test_gmres_ir_on_an_ill_conditioned_indefinite_matrix():
     for _ in range(20):
         xp = xp + torch.linalg.lu_solve(lu, piv, (b - A @ xp).float().unsqueeze(1)).squeeze(1).double()
     assert float((b - A @ xp).norm() / b.norm()) > 1e-6
+
+
+@pytest.mark.parametrize("mode", ["device", "device_mixed"])
+def test_dense_kkt_formation_and_solve(mode):
+    """The dense KKT modes (formed from K's stored upper triangle and J, on a torch device;
+    the CPU here) against SciPy's sparse LU of the same [K J^T; J 0]."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+
+    n, m = 80, 9
+    A = sp.random(n, n, density=0.15, random_state=1)
+    A = (A + A.T + 4.0 * sp.eye(n)).tocsc()
+    cols = np.repeat(np.arange(n), np.diff(A.indptr))
+    K_upper = sp.csc_matrix((np.where(A.indices <= cols, A.data, 0.0), A.indices, A.indptr), shape=(n, n))
+    J = sp.random(m, n, density=0.3, random_state=2).tocsr()
+    full = sp.bmat([[A, J.T], [J, None]], format="csc")
+    b = np.random.default_rng(0).standard_normal(n + m)
+    ref = spla.spsolve(full, b)
+    got = S._KKT(K_upper, J, mode, device="cpu").solve(b)
+    assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
