@@ -377,3 +377,28 @@ def test_full_size_properties(ctx):
     assert rel(Fr, Fmx) < 1e-14
     # K's checksum is independent of the scatter order up to round-off
     assert abs(Kd.sum() - K64.sum()) <= 1e-10 * np.abs(K64).sum()
+
+
+def test_assemble_into_page_locked_host_memory(ctx):
+    """cgb_assemble into page-locked host buffers (as the end-to-end benchmark uses) gives
+    what it gives into ordinary host memory: bitwise with the deterministic scatter, to the
+    atomic scatter's run-to-run rounding otherwise."""
+    import torch
+
+    p = synth.square_plate(21, 0.5, 3, jitter=0.1, crease="arc", seed=8)
+    model = cg.PlateModel(p, ctx)
+    x = synth.fourier_field(p.node_xy, np.random.default_rng(9), lam=(4.0, 20.0))
+    asm = model.asm
+    for flags in (cg.TANGENT | cg.HINGE | cg.MIXED, cg.TANGENT | cg.HINGE, cg.TANGENT | cg.MIXED | cg.DETERMINISTIC):
+        K_pl, F_pl = asm.assemble(x, flags)
+        K_h = torch.empty(asm.nnz, dtype=torch.float64, pin_memory=True).numpy()
+        F_h = torch.empty(asm.n_dofs, dtype=torch.float64, pin_memory=True).numpy()
+        x_h = torch.empty(asm.n_dofs, dtype=torch.float64, pin_memory=True).numpy()
+        x_h[:] = x
+        asm.assemble(x_h, flags, K_out=K_h, F_out=F_h)
+        if flags & cg.DETERMINISTIC:
+            assert np.array_equal(K_h, K_pl) and np.array_equal(F_h, F_pl)
+        else:   # atomic scatter: the order of the additions may differ between calls
+            k_tol = 1e-6 if flags & cg.MIXED else 1e-12      # FP32 / FP64 accumulation
+            assert np.abs(K_h - K_pl).max() <= k_tol * np.abs(K_pl).max()
+            assert np.abs(F_h - F_pl).max() <= 1e-12 * np.abs(F_pl).max()
