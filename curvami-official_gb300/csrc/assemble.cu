@@ -1507,6 +1507,16 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   const int n_chunks = a->tuning.n_chunks > 0 ? a->tuning.n_chunks : (S->n_gp >= 65536 ? kChunks : 1);
   const int rthreads = a->tuning.residual_threads > 0 ? a->tuning.residual_threads : 256;
   const int chunk = ((S->n_gp + n_chunks - 1) / n_chunks + 31) / 32 * 32;
+  // Chunk c covers [cb(c), cb(c + 1)). The first chunk is a quarter of the others: the
+  // tangent stream waits for its residual, and from then on the tangent stream is the
+  // longer of the two, so a short first chunk shortens the step; the rest share the
+  // remaining points evenly. All bounds are multiples of 32 points.
+  const int first = n_chunks > 1 ? std::max(32, (chunk / 4 + 31) / 32 * 32) : chunk;
+  const int rest = n_chunks > 1 ? ((std::max(S->n_gp - first, 0) + n_chunks - 2) / (n_chunks - 1) + 31) / 32 * 32 : 0;
+  auto cb = [&](int c) {
+    const int64_t b = c == 0 ? 0 : static_cast<int64_t>(first) + static_cast<int64_t>(c - 1) * rest;
+    return static_cast<int>(std::min<int64_t>(b, S->n_gp));
+  };
   int nface = 0;
   const size_t tsm = static_cast<size_t>(kTanWarps) * ((kState * 32 + kRec * fa.nmax) * tk + fa.nmax * sizeof(int));
   // Work counters of the chunks' residual launches.
@@ -1518,8 +1528,8 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   }
   for (int c = 0; c < n_chunks && S->n_gp > 0; ++c) {
     int* work = a->work_ctr.p + c;
-    fa.g_begin = c * chunk;
-    fa.g_end = std::min(S->n_gp, (c + 1) * chunk);
+    fa.g_begin = cb(c);
+    fa.g_end = cb(c + 1);
     if (fa.g_begin >= fa.g_end) break;
     const int ncg = fa.g_end - fa.g_begin;
     const unsigned rgrid = std::max(1u, std::min(nb(ncg, rthreads), static_cast<unsigned>(sms * 16 * (256 / rthreads))));
@@ -1570,13 +1580,11 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     prof_end(ctx, CGB_PHASE_TANGENT, 1, a->side);
     CGB_CUDA(cudaGetLastError());
   }
-  if (want_K) {
-    CGB_CUDA(cudaEventRecord(a->ev_done, a->side));
-    CGB_CUDA(cudaStreamWaitEvent(st, a->ev_done, 0));
-  }
   (void)nface;
 
-  // Hinge.
+  // Hinge, on the context stream beside the last tangent chunks: it reads x, its shape sets
+  // and the fold state and adds into F and the block accumulator with atomics (or into its
+  // own contribution slots in deterministic mode), none of which the tangent reads.
   if (hinge) {
     prof_begin(ctx, CGB_PHASE_HINGE);
     int nl = 0;
@@ -1600,6 +1608,10 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
       fb += f.n_u;
     }
     prof_end(ctx, CGB_PHASE_HINGE, nl);
+  }
+  if (want_K) {
+    CGB_CUDA(cudaEventRecord(a->ev_done, a->side));
+    CGB_CUDA(cudaStreamWaitEvent(st, a->ev_done, 0));
   }
 
   // Reductions / output.
