@@ -79,3 +79,32 @@ def test_split_on_crease():
     cr = [{"vertices": np.array([[0.0, 0.25], [1.0, 0.25]])}]
     out, n = synth.split_on_creases(faces, cr)
     assert n == 2 and len(out.xy) == 4 and abs(out.weight.sum() - 2.0) < 1e-15
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every struct the Python mirror passes by pointer has the header's size and field
+    offsets (a C program built with the host compiler prints them)."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"cgb_crease": _lib.Crease, "cgb_shape_params": _lib.ShapeParams, "cgb_fold": _lib.Fold,
+               "cgb_face_problem": _lib.FaceProblem, "cgb_tuning": _lib.Tuning}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "curvami_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.check_call([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    out = subprocess.check_output([str(exe)]).decode().split("\n")
+    got = {tuple(line.split()[:-1]): int(line.split()[-1]) for line in out if line.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
