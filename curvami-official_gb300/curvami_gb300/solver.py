@@ -656,6 +656,24 @@ class ContinuationSolver:
         return False
 
 
+def tracking_displacement(prob: PlateProblem, x) -> float:
+    """trackingDisplacement (plate/PlateProblem.h:14-44), the scalar the reference's
+    continuation exports per step: the mean displacement along the load direction over the
+    Gauss points of every loaded point and edge domain (|force| > 1e-12); with no loaded
+    domain, the mean deflection w over the nodes. (Fold domains carry no loads here.)"""
+    X = np.asarray(x, np.float64).reshape(-1, 3)
+    total, count = 0.0, 0
+    for dom, tab in list(prob.points) + list(prob.edges):
+        f = np.asarray(dom.bc.force, np.float64)
+        if np.linalg.norm(f) > 1e-12:
+            u = tab.P @ X
+            total += float((u @ (f / np.linalg.norm(f))).sum())
+            count += tab.n_gp
+    if count > 0:
+        return total / count
+    return float(X[:, 2].mean())
+
+
 def load_steps(solver: ContinuationSolver, prob: PlateProblem, lambdas, x0=None):
     """Static load stepping: one LineSearch per load factor, each starting from the
     previous solution. Returns the converged states and the Newton iterations per step

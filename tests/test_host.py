@@ -4,6 +4,7 @@ import math
 import time
 
 import numpy as np
+import pytest
 
 from curvami_gb300 import autotune as at
 from curvami_gb300 import synth
@@ -108,3 +109,31 @@ def test_four_crease_plate_layout():
         assert np.allclose(cr["vertices"][0], c) and not cr["extend_start"] and cr["extend_end"]
     assert [f.rigid for f in p.folds] == [True, False, True, False]
     assert len(p.faces.xy) == 40 * 40 * 4
+
+
+def test_tracking_displacement():
+    """trackingDisplacement: mean displacement along the load over loaded domains, else the
+    mean deflection of the nodes (plate/PlateProblem.h:14-44)."""
+    import scipy.sparse as sp
+
+    from curvami_gb300 import solver as S
+
+    n = 4
+    x = np.arange(3 * n, dtype=np.float64)
+
+    class Tab:
+        def __init__(self, P):
+            self.P = sp.csr_matrix(P)
+            self.n_gp = P.shape[0]
+
+    class Prob:
+        points, edges = [], []
+
+    prob = Prob()
+    assert S.tracking_displacement(prob, x) == pytest.approx(np.mean(x[2::3]))
+    dom = S.LineDomain(np.zeros((2, 2)), np.ones(2), np.zeros((2, 2)), np.zeros((2, 2)),
+                       S.BoundaryCondition(force=(0.0, 0.0, -2.0)))
+    P = np.array([[0.5, 0.5, 0.0, 0.0], [0.0, 0.0, 1.0, 0.0]])
+    prob.edges = [(dom, Tab(P))]
+    w = P @ x.reshape(-1, 3)[:, 2]
+    assert S.tracking_displacement(prob, x) == pytest.approx(-w.mean())
