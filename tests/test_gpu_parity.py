@@ -402,3 +402,32 @@ def test_assemble_into_page_locked_host_memory(ctx):
             k_tol = 1e-6 if flags & cg.MIXED else 1e-12      # FP32 / FP64 accumulation
             assert np.abs(K_h - K_pl).max() <= k_tol * np.abs(K_pl).max()
             assert np.abs(F_h - F_pl).max() <= 1e-12 * np.abs(F_pl).max()
+
+
+def test_large_K_host_and_device_entry_points_agree():
+    """A K of more than 64 MB: the deterministic K through cgb_assemble (page-locked and
+    ordinary host buffers) equals, bitwise, K assembled by cgb_assemble_device on a caller's
+    stream and copied by torch."""
+    import torch
+
+    p = synth.square_plate(141, 0.5, 2, jitter=0.1, crease="arc", seed=12)
+    ctx = cg.Context(0)              # its own context: the test moves it onto a torch stream
+    model = cg.PlateModel(p, ctx)
+    asm = model.asm
+    assert asm.nnz * 8 >= 64 << 20
+    x = synth.fourier_field(p.node_xy, np.random.default_rng(13), lam=(4.0, 40.0))
+    flags = cg.TANGENT | cg.HINGE | cg.MIXED | cg.DETERMINISTIC
+    K_h = torch.empty(asm.nnz, dtype=torch.float64, pin_memory=True).numpy()
+    F_h = torch.empty(asm.n_dofs, dtype=torch.float64, pin_memory=True).numpy()
+    asm.assemble(x, flags, K_out=K_h, F_out=F_h)
+    K_pg, F_pg = asm.assemble(x, flags)                      # ordinary host memory
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    x_d = torch.from_numpy(x).cuda()
+    K_d = torch.empty(asm.nnz, dtype=torch.float64, device="cuda")
+    F_d = torch.empty(asm.n_dofs, dtype=torch.float64, device="cuda")
+    asm.assemble_device(x_d.data_ptr(), K_d.data_ptr(), F_d.data_ptr(), flags)
+    ctx.synchronize()
+    K_dev = K_d.cpu().numpy()
+    assert np.array_equal(K_h, K_dev) and np.array_equal(K_pg, K_dev)
+    assert np.array_equal(F_h, F_d.cpu().numpy())
