@@ -352,14 +352,19 @@ class PlateProblem:
 
 class _Projector:
     """ConstraintProjector: (J J^T) factorised once, used for the corrector and the
-    projection; a least-squares fallback when the Gram matrix is not positive definite."""
+    projection; a least-squares fallback when the Gram matrix is not positive definite.
+    J stays sparse (a few nonzeros per row), so the Gram matrix costs the sparse product,
+    not a dense one over every dof."""
 
     def __init__(self, J):
-        self.J = J.toarray() if sp.issparse(J) else np.asarray(J)
+        self.J = sp.csr_matrix(J) if sp.issparse(J) else np.asarray(J)
         self.chol = None
+        self.gram = None
         if self.J.shape[0]:
+            G = self.J @ self.J.T
+            self.gram = G.toarray() if sp.issparse(G) else np.asarray(G)
             try:
-                self.chol = sla.cho_factor(self.J @ self.J.T)
+                self.chol = sla.cho_factor(self.gram)
             except np.linalg.LinAlgError:
                 self.chol = None
 
@@ -368,7 +373,7 @@ class _Projector:
             out = sla.cho_solve(self.chol, rhs)
             if np.all(np.isfinite(out)):
                 return out
-        return np.linalg.lstsq(self.J @ self.J.T, rhs, rcond=None)[0]
+        return np.linalg.lstsq(self.gram, rhs, rcond=None)[0]
 
     def corrector(self, c, ns):
         if len(c) == 0:
