@@ -766,9 +766,10 @@ __device__ __forceinline__ void pair_moment_sums(const RkpmArgs& a, const PairPo
 //
 // Launch shape of the point kernel, measured on the 1,000,000-point stage (order 2; RKPM
 // phase of both kernels): 2 blocks per SM (255 registers) 8.24 ms, 3 blocks (168 registers,
-// more spills) 8.80 ms; before the split, one kernel doing both passes took 11.3 ms. Order 3
-// (28 raw moments) sums the jets in two passes of three to keep the accumulators in
-// registers.
+// more spills) 8.80 ms; the jets summed in two passes of three (half the accumulators, the
+// weight jets computed twice) 9.4 ms at 3 and 9.2 ms at 4 blocks per SM; before the split,
+// one kernel doing both passes took 11.3 ms. Order 3 (28 raw moments) needs the two passes
+// to keep the accumulators in registers.
 constexpr int kPairMinBlocks = 2;
 constexpr int kPairSplitOrder = 3;
 constexpr int kPairValueThreads = 256;
