@@ -790,7 +790,7 @@ def arc_length_path(cg, ctx, n_side=41, target_deg=150.0, kmax=80):
     last = sol.steps[-1] if sol.steps else None
     out = {
         "what": ("KinematicArcLength (plate/NonLinearSolver.h:607-812) restated, over the GPU FP64 assembly, to a "
-                 f"{target_deg:.0f} deg rest angle of the drivers; config 5's 401x401 plate is not run: its "
+                 f"{target_deg:.0f} deg rest angle of the drivers; the same path on the 401x401 plate is not run: its "
                  "482k-dof KKT needs a sparse direct solver (MUMPS and cuDSS are absent here)"),
         "n_side": n_side, "n_dofs": prob.ns, "n_gauss_points": model.faces.n_gp, "n_constraint_rows":
             int(len(sol.ind_rows)), "sector_deg": p.meta["sector_deg"], "seed": FOUR_SEED,
