@@ -13,7 +13,9 @@ The reference drives its fold mechanisms with two arc-length continuations in
     the driver creases (r_i their remaining travel, scaled to max |r_i| = 1) until every
     driver is within target_tol_deg of its target.
 
-Both share the step control of StepController (core/include/curvami/solver/
+Both, and the generic ``arc_length`` (ContinuationSolver::ArcLength, core/include/curvami/
+solver/ContinuationSolver.h:329-540, checked against the reference's own consumer tests),
+share the step control of StepController (core/include/curvami/solver/
 StepController.h:16-229), restated here with the same names and defaults: ASLA (Crisfield's
 square-root rule with target relaxation), the curvature controller, reversal bookkeeping
 and the no-progress stall test at dsmin. ``fold_gradient`` restates ComputeFoldGradient
@@ -344,6 +346,108 @@ class ArcLengthSolver(S.ContinuationSolver):
     @staticmethod
     def _sym_upper_times(K, v):
         return K @ v + sp.triu(K, k=1).T @ v          # selfadjointView<Upper> * v
+
+    # -- ContinuationSolver::ArcLength (core/include/curvami/solver/ContinuationSolver.h:329-540) --
+    def arc_length(self, prob, lambda_0, x0, lambda_tot, on_converged=None):
+        """The generic arc-length continuation of F_int(x) - lambda F_ext(x) = 0 with c(x) = 0
+        for any problem with num_dofs / assemble / internal_force / external_force /
+        constraints (and optionally load_stiffness): predictor K d_T = F_ext, Crisfield's
+        corrector with the sphere ||dU||^2 + psi^2 dl^2 ||F_ext||^2 = ds^2, the step control
+        above. on_converged(k, lambda, x, W_ext) after every accepted step (W_ext by the
+        trapezoidal rule on the initial load). Returns the final state."""
+        jmax = self.max_iters
+        x = np.array(x0, np.float64, copy=True)
+        ns = x.size
+        if ns != prob.num_dofs():
+            raise ValueError(f"ArcLength: state vector has {ns} entries, problem has {prob.num_dofs()} DOFs")
+        lam, k = float(lambda_0), 1
+        dU_old, dl_old = np.zeros(ns), 0.0
+        c_all, J_all = prob.constraints(x)
+        self.initialize_topology(J_all)
+        self.reset_inertia_tracking()
+        nc = len(self.ind_rows)
+        W_ext = 0.0
+        F_ref = np.asarray(prob.external_force(x), np.float64)
+        x_prev = x.copy()
+        while k <= self.kmax and lam <= lambda_tot:
+            Fext = np.asarray(prob.external_force(x), np.float64)
+            K, _ = self._assemble(prob, x)
+            K = self.with_load_stiffness(prob, K, x, lam)
+            c_ind, J_ind = self._constraints(prob, x)
+            xb_p = S._Projector(J_ind).corrector(c_ind, ns)
+            rhs = np.zeros(ns + nc)
+            rhs[:ns] = Fext
+            (sol,) = self._kkt(K, J_ind, [rhs])
+            if not np.all(np.isfinite(sol)):
+                break
+            d_T = sol[:ns]
+            ff = float(Fext @ Fext)
+            sgn = 1.0
+            if k == 1:
+                sgn = 1.0 if float(d_T @ Fext) >= 0.0 else -1.0
+            elif float(dU_old @ d_T) < 0.0 and self.confirm_reversal(f"snap-back at step {k}"):
+                sgn = -1.0
+                self.note_reversal()
+            dl = sgn * self.ds / math.sqrt(float(d_T @ d_T) + self.psi * self.psi * ff)
+            dU = dl * d_T + xb_p
+            icorr_ok, k_corr = 0, jmax
+            for j in range(1, jmax + 1):
+                curr_lam = lam + dl
+                x_curr = x + dU
+                c_ind_c, J_ind_c = self._constraints(prob, x_curr)
+                Fext_c = np.asarray(prob.external_force(x_curr), np.float64)
+                K_c, Fint_c = self._assemble(prob, x_curr)
+                K_c = self.with_load_stiffness(prob, K_c, x_curr, curr_lam)
+                R = Fint_c - curr_lam * Fext_c
+                v_res = float(dU @ dU) + self.psi * self.psi * dl * dl * ff - self.ds * self.ds
+                xb_c = S._Projector(J_ind_c).corrector(c_ind_c, ns)
+                r0 = np.zeros(ns + nc)
+                r1 = np.zeros(ns + nc)
+                r0[:ns] = Fext_c
+                r1[:ns] = -(R + self._sym_upper_times(K_c, xb_c))
+                s0, s1 = self._kkt(K_c, J_ind_c, [r0, r1])
+                if not (np.all(np.isfinite(s0)) and np.all(np.isfinite(s1))):
+                    icorr_ok, k_corr = 0, j
+                    break
+                daP = s0[:ns]
+                daPsi = s1[:ns] + xb_c
+                mult = s1[ns:]
+                denom = float(dU @ daP) + self.psi * self.psi * dl * ff
+                dl_c = -(0.5 * v_res + float(dU @ daPsi)) / denom
+                dl += dl_c
+                dU = dU + daPsi + dl_c * daP
+                Rm = R + (J_ind_c.T @ mult if nc else 0.0)
+                max_force = float(np.abs(Rm).max())
+                energy = abs(float(daPsi @ R))
+                geom = float(np.abs(c_ind_c).max()) if nc else 0.0
+                if j > 1 and max_force <= self.tol_force and energy <= self.tol_energy and \
+                        geom <= self.tol_geom and abs(v_res) <= self.tol_geom:
+                    icorr_ok, k_corr = 1, j
+                    break
+                if max_force >= self.div or math.isnan(max_force):
+                    icorr_ok, k_corr = 0, j
+                    break
+            cos_t = self._cos_theta(dU_old, dl_old, dU, dl) if (k > 1 and icorr_ok == 1) else 1.0
+            self.asla(icorr_ok, k_corr, cos_t)
+            if icorr_ok == 1:
+                self.curvature_controller(k, cos_t)
+                self.note_accepted_step()
+                dU_old, dl_old = dU, dl
+                x = x + dU
+                lam += dl
+                W_ext += 0.5 * ((lam - dl) + lam) * float(F_ref @ (x - x_prev))
+                x_prev = x.copy()
+                self.steps.append(Step(k, lam, k_corr, self.ds, []))
+                if on_converged is not None:
+                    on_converged(k, lam, x, W_ext)
+                k += 1
+                if self.stalled_at_dsmin(x, dU):
+                    break
+            else:
+                self.failed_steps += 1
+                if self.ds <= self.dsmin:
+                    break
+        return x
 
     # -- NonLinearSolver::KinematicArcLength --
     def kinematic_arc_length(self, prob, x0, drivers, on_converged=None):

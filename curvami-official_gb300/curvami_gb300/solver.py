@@ -580,6 +580,21 @@ class ContinuationSolver:
         return J[self.ind_rows] if J.shape[0] else J
 
     @staticmethod
+    def with_load_stiffness(prob, K, x, lam):
+        """applyLoadStiffness (ContinuationSolver.h:84-95): K - lambda K_load when the problem
+        supplies a load stiffness (``load_stiffness(x)`` returning its upper triangle), else K
+        unchanged."""
+        f = getattr(prob, "load_stiffness", None)
+        if f is None:
+            return K
+        KL = f(x)
+        if KL is None:
+            return K
+        if KL.shape != K.shape:
+            raise ValueError(f"loadStiffness: K_load is {KL.shape[0]}x{KL.shape[1]}, K is {K.shape[0]}x{K.shape[1]}")
+        return (sp.csc_matrix(K) - lam * sp.csc_matrix(KL)).tocsc()
+
+    @staticmethod
     def kkt_solve(K_upper, J, rhs, kkt="host"):
         """[K J^T; J 0] sol = rhs with K given by its upper triangle."""
         return _KKT(K_upper, J, kkt).solve(rhs)
@@ -612,6 +627,7 @@ class ContinuationSolver:
                 d[:] = d0
                 return False
             K, _ = prob.assemble(d)
+            K = self.with_load_stiffness(prob, K, d, lam)
             xb = proj.corrector(c_ind, ns)
             Kxb = K @ xb + sp.triu(K, k=1).T @ xb         # selfadjointView<Upper> * xb
             rhs = np.zeros(ns + nc)
