@@ -132,3 +132,19 @@ def test_arc_length_follower_torque_passes_the_barrier_only_with_load_stiffness(
         reached[with_kl] = last[0]
     assert reached[True] > 3.0
     assert reached[False] < 2.6245 + 0.05
+
+
+def test_kmax_is_a_pure_step_cap():
+    """kmax caps the continuation's accepted steps and nothing else (the reference's
+    tests/regression/kmax_check.py): a capped run is the uncapped run's prefix, and the
+    LineSearch iteration cap (ls_max_iters) is a separate setting."""
+    full, capped = [], []
+    A.ArcLengthSolver(psi=1.0, ds=0.2, dsmax=0.5).arc_length(
+        CubicSpring(), 0.0, np.zeros(2), 5.0, on_converged=lambda k, lam, x, w: full.append((lam, x.copy())))
+    A.ArcLengthSolver(psi=1.0, ds=0.2, dsmax=0.5, kmax=3).arc_length(
+        CubicSpring(), 0.0, np.zeros(2), 5.0, on_converged=lambda k, lam, x, w: capped.append((lam, x.copy())))
+    assert len(capped) == 3 < len(full)
+    for (l1, x1), (l2, x2) in zip(capped, full):
+        assert l1 == l2 and np.array_equal(x1, x2)
+    s = S.ContinuationSolver(ls_max_iters=7)
+    assert s.ls_max_iters == 7 and not hasattr(s, "kmax")
