@@ -22,7 +22,12 @@ and the no-progress stall test at dsmin. ``fold_gradient`` restates ComputeFoldG
 (NonLinearSolver.h:417-493) and ``fold_angle_deg`` ComputeFoldAngleDeg (NonLinearSolver.h:
 62-90, with the FoldAngle averages of plate/FoldAngleUtil.h).
 
-Not restated: the restart file (RestartManager) and the inertia count. The reference reads
+Restart records (``restart_file``) follow RestartManager: loaded at the start of a run, written
+after every accepted step, in the reference's binary layout (restart.py). As in the reference,
+KinematicArcLength's first predictor after a restart takes the pseudo-load at the plate's
+kinematics when the record was loaded (the initial state), so a restarted kinematic run leaves
+the uninterrupted path; ArcLength and TargetDirectedArcLength evaluate their load at the loaded
+state and continue it exactly. Not restated: the inertia count. The reference reads
 the reduced Hessian's negative modes from MUMPS's factorisation (INFOG(12)) and uses them
 only with the opt-in snap-back veto (off by default, StepController.h:41). The KKT here is
 an LU, so a requested reversal is always taken, as the reference does with the veto off.
@@ -40,6 +45,7 @@ from dataclasses import dataclass
 import numpy as np
 import scipy.sparse as sp
 
+from . import restart as RM
 from . import solver as S
 from .creasing import weighted_mean_about_circular_mean_rad
 
@@ -209,11 +215,13 @@ class ArcLengthSolver(S.ContinuationSolver):
 
     def __init__(self, ds=0.1, dsmin=1e-6, dsmax=10.0, Id=6, max_iters=100, psi=1.0, kmax=5000,
                  asla_hold_after_reversal=False, no_progress_window=24, no_progress_efficiency=0.15,
-                 no_progress_abort=True, exact_fold_gradient=False, **kw):
+                 no_progress_abort=True, exact_fold_gradient=False, restart_file="", **kw):
         """exact_fold_gradient: the drivers' load direction from the exact fold-angle gradient
         (fold_gradient(exact=True)), an extension; False is the reference's algorithm."""
         super().__init__(**kw)
         self.exact_fold_gradient = bool(exact_fold_gradient)
+        self.restart_file = restart_file
+        self.restarted_from = None   # step k the last run resumed at, when it did
         self.ds, self.dsmin, self.dsmax = float(ds), float(dsmin), float(dsmax)
         self.Id, self.max_iters, self.psi, self.kmax = int(Id), int(max_iters), float(psi), int(kmax)
         self.asla_hold_after_reversal = asla_hold_after_reversal
@@ -369,6 +377,12 @@ class ArcLengthSolver(S.ContinuationSolver):
         W_ext = 0.0
         F_ref = np.asarray(prob.external_force(x), np.float64)
         x_prev = x.copy()
+        if self.restart_file:
+            r = RM.load(self.restart_file, ns)
+            if r is not None:
+                k, lam, self.ds, dl_old, W_ext, x, dU_old = r
+                x_prev = x.copy()
+                self.restarted_from = k
         while k <= self.kmax and lam <= lambda_tot:
             Fext = np.asarray(prob.external_force(x), np.float64)
             K, _ = self._assemble(prob, x)
@@ -441,6 +455,8 @@ class ArcLengthSolver(S.ContinuationSolver):
                 if on_converged is not None:
                     on_converged(k, lam, x, W_ext)
                 k += 1
+                if self.restart_file:
+                    RM.save(self.restart_file, k, lam, self.ds, dl_old, W_ext, x, dU_old)
                 if self.stalled_at_dsmin(x, dU):
                     break
             else:
@@ -462,6 +478,11 @@ class ArcLengthSolver(S.ContinuationSolver):
         self.reset_inertia_tracking()
         nc = len(self.ind_rows)
         state = x.copy()      # the plate's kinematics: the last state assembled or constrained
+        if self.restart_file:
+            r = RM.load(self.restart_file, ns)
+            if r is not None:
+                k, mu, self.ds, dmu_old, _, x, dU_old = r
+                self.restarted_from = k
 
         def update_driver_angles(m):
             for d in drivers:
@@ -545,6 +566,8 @@ class ArcLengthSolver(S.ContinuationSolver):
                 if on_converged is not None:
                     on_converged(k, mu, x, angles)
                 k += 1
+                if self.restart_file:
+                    RM.save(self.restart_file, k, mu, self.ds, dmu_old, 0.0, x, dU_old)
                 if mu >= 1.0:
                     break
             else:
@@ -578,6 +601,15 @@ class ArcLengthSolver(S.ContinuationSolver):
             for r, d in zip(ratios, drivers):
                 F += r * self._fold_gradient(prob, d.fold, xe)
             return F
+
+        W_ext = 0.0
+        x_prev = x.copy()
+        if self.restart_file:
+            rr = RM.load(self.restart_file, ns)
+            if rr is not None:
+                k, lam, self.ds, dl_old, W_ext, x, dU_old = rr
+                x_prev = x.copy()
+                self.restarted_from = k
 
         while k <= self.kmax and lam <= lambda_tot:
             F_ref = follower(x)
@@ -644,11 +676,15 @@ class ArcLengthSolver(S.ContinuationSolver):
                 dU_old, dl_old = dU, dl
                 x = x + dU
                 lam += dl
+                W_ext += 0.5 * ((lam - dl) + lam) * float(F_ref @ (x - x_prev))
+                x_prev = x.copy()
                 angles = [fold_angle_deg(f, x) for f in prob.folds]
                 self.steps.append(Step(k, lam, k_corr, self.ds, angles))
                 if on_converged is not None:
                     on_converged(k, lam, x, angles)
                 k += 1
+                if self.restart_file:
+                    RM.save(self.restart_file, k, lam, self.ds, dl_old, W_ext, x, dU_old)
                 reached = all(abs(wrapped_distance_deg(angles[d.fold], d.angle_target * 180.0 / math.pi))
                               <= target_tol_deg for d in drivers)
                 if reached:

@@ -214,3 +214,28 @@ def test_dense_kkt_formation_and_solve(mode):
     ref = spla.spsolve(full, b)
     got = S._KKT(K_upper, J, mode, device="cpu").solve(b)
     assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+def test_target_directed_restart(o, tmp_path):
+    """TargetDirectedArcLength cut by kmax and restarted from its record (the reference's
+    restart_check cuts tdal_arccrease by kmax) continues exactly as the uninterrupted run."""
+    p, doms, drivers = four_crease_case(target_deg=20.0)
+
+    def run(kmax, path=""):
+        prob = oracle_arc_problem(o, p, doms)
+        prob.backend.threads = 1      # the oracle's OpenMP merge is bitwise only on one thread
+        sol = A.ArcLengthSolver(kmax=kmax, max_iters=30, ds=6.25e-3, dsmax=0.5, psi=0.0,
+                                exact_fold_gradient=True, restart_file=path)
+        out = []
+        sol.target_directed_arc_length(prob, 0.0, np.zeros(prob.ns), 500.0, drivers, target_tol_deg=1.0,
+                                       on_converged=lambda k, lam, x, ang: out.append((k, lam, x.copy())))
+        return sol, out
+
+    _, full = run(2)
+    path = str(tmp_path / "t.res")
+    _, a = run(1, path)
+    s2, b = run(2, path)
+    assert s2.restarted_from == 2
+    assert [r[0] for r in a + b] == [r[0] for r in full] == [1, 2]
+    for u, v in zip(a + b, full):
+        assert u[1] == v[1] and np.array_equal(u[2], v[2])

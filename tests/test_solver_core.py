@@ -148,3 +148,45 @@ def test_kmax_is_a_pure_step_cap():
         assert l1 == l2 and np.array_equal(x1, x2)
     s = S.ContinuationSolver(ls_max_iters=7)
     assert s.ls_max_iters == 7 and not hasattr(s, "kmax")
+
+
+def test_restart_continues_the_uninterrupted_run(tmp_path):
+    """A run cut short (lambda_tot, as the reference's restart_check cuts al_arccrease by
+    max_load) and restarted from its record to the end gives the uninterrupted run's steps,
+    bitwise, including the external work."""
+    from curvami_gb300 import restart as RM
+
+    full = []
+    A.ArcLengthSolver(psi=1.0, ds=0.2, dsmax=0.5).arc_length(
+        CubicSpring(), 0.0, np.zeros(2), 5.0, on_converged=lambda k, lam, x, w: full.append((k, lam, x.copy(), w)))
+    path = str(tmp_path / "run.res")
+    first, second = [], []
+    A.ArcLengthSolver(psi=1.0, ds=0.2, dsmax=0.5, restart_file=path).arc_length(
+        CubicSpring(), 0.0, np.zeros(2), 2.5, on_converged=lambda k, lam, x, w: first.append((k, lam, x.copy(), w)))
+    s2 = A.ArcLengthSolver(psi=1.0, ds=0.2, dsmax=0.5, restart_file=path)
+    s2.arc_length(CubicSpring(), 0.0, np.zeros(2), 5.0,
+                  on_converged=lambda k, lam, x, w: second.append((k, lam, x.copy(), w)))
+    assert s2.restarted_from == len(first) + 1
+    both = first + second
+    assert len(both) == len(full)
+    for a, b in zip(both, full):
+        assert a[0] == b[0] and a[1] == b[1] and np.array_equal(a[2], b[2]) and a[3] == b[3]
+
+
+def test_restart_record_layout_and_rejections(tmp_path):
+    from curvami_gb300 import restart as RM
+
+    p = str(tmp_path / "r.res")
+    x = np.array([1.0, -2.0, 3.5])
+    assert RM.save(p, 7, 0.25, 0.1, 0.01, 3.0, x, 2 * x)
+    raw = open(p, "rb").read()
+    assert raw[:8] == b"CURVRES\x00" and len(raw) == 8 + 4 + 4 + 32 + 4 + 48
+    k, lam, ds, dl, W, xr, dU = RM.load(p, 3)
+    assert (k, lam, ds, dl, W) == (7, 0.25, 0.1, 0.01, 3.0) and np.array_equal(xr, x) and np.array_equal(dU, 2 * x)
+    assert RM.load(p, 4) is None                       # another problem's record
+    open(p, "wb").write(raw[:-5])
+    assert RM.load(p) is None                           # truncated
+    open(p, "wb").write(b"XXXXXXXX" + raw[8:])
+    assert RM.load(p) is None                           # not a record
+    assert RM.load(str(tmp_path / "none.res")) is None
+    assert not RM.save(p, 1, 0.0, 0.1, 0.0, 0.0, x, x[:2])
