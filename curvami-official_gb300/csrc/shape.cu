@@ -36,15 +36,30 @@ struct GridDev {
   const int32_t* cell_nodes;
 };
 
+// FP32 pre-test of the FRNN distance test. Coordinates relative to the grid's lower corner
+// are rounded to float (node32, per node; the point's in the kernel), the squared distance
+// is formed in float, and `margin` bounds its difference from the exact squared distance
+// (coordinate rounding, float arithmetic, the float radius; computed on the host from the
+// extent of the nodes and points). A candidate beyond r^2 + margin is outside and one
+// below r^2 - margin inside whatever FP64 gives; only those within the margin take the
+// exact FP64 test, so every decision is the FP64 one.
+struct FrnnPre {
+  const float2* node32;   // per node, (x - minx, y - miny) in float
+  const float* r2n32;     // per node r^2 in float, or nullptr for the single radius
+  float r2f;              // the single radius squared, in float
+  float margin;
+};
+
 // Thread per Gauss point: count (out_idx == nullptr) or fill the neighbour list.
 __global__ void frnn_kernel(int n_gp, const double* __restrict__ gp_xy,
                             const double* __restrict__ node_xy, const double* __restrict__ rho_node,
-                            double rho, double rho2, GridDev G, const int64_t* __restrict__ ptr,
+                            double rho, double rho2, GridDev G, FrnnPre pre, const int64_t* __restrict__ ptr,
                             int32_t* __restrict__ count, int32_t* __restrict__ out_idx,
                             double* __restrict__ out_s) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n_gp) return;
   const double gx = gp_xy[2 * g], gy = gp_xy[2 * g + 1];
+  const float gxf = __double2float_rn(gx - G.minx), gyf = __double2float_rn(gy - G.miny);
   const int qx = static_cast<int>(floor(__ddiv_rn(__dsub_rn(gx, G.minx), G.cell)));
   const int qy = static_cast<int>(floor(__ddiv_rn(__dsub_rn(gy, G.miny), G.cell)));
   int64_t pos = out_idx ? ptr[g] : 0;
@@ -56,12 +71,22 @@ __global__ void frnn_kernel(int n_gp, const double* __restrict__ gp_xy,
       const int k0 = G.cell_start[key], k1 = G.cell_start[key + 1];
       for (int k = k0; k < k1; ++k) {
         const int j = G.cell_nodes[k];
-        const double ddx = __dsub_rn(node_xy[2 * j], gx);
-        const double ddy = __dsub_rn(node_xy[2 * j + 1], gy);
-        const double dist2 = __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy));
-        double r = rho, r2 = rho2;
-        if (rho_node) { r = rho_node[j]; r2 = __dmul_rn(r, r); }
-        if (dist2 <= r2) {
+        const float2 nf = pre.node32[j];
+        const float fdx = nf.x - gxf, fdy = nf.y - gyf;
+        const float d2f = fdx * fdx + fdy * fdy;
+        const float r2f = pre.r2n32 ? pre.r2n32[j] : pre.r2f;
+        if (d2f > r2f + pre.margin) continue;          // outside, whatever FP64 gives
+        bool inside = d2f < r2f - pre.margin;          // inside, whatever FP64 gives
+        double dist2 = 0.0, r = rho;
+        if (!inside || out_s) {
+          const double ddx = __dsub_rn(node_xy[2 * j], gx);
+          const double ddy = __dsub_rn(node_xy[2 * j + 1], gy);
+          dist2 = __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy));
+          double r2 = rho2;
+          if (rho_node) { r = rho_node[j]; r2 = __dmul_rn(r, r); }
+          if (!inside) inside = dist2 <= r2;
+        }
+        if (inside) {
           if (out_idx) {
             out_idx[pos] = j;
             if (out_s) out_s[pos] = __ddiv_rn(__dsqrt_rn(dist2), r);
@@ -971,11 +996,42 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
 
   upload(out->gp_xy, gp_xy, 2 * static_cast<size_t>(n_gp), st);
   const double rho2 = prm.rho * prm.rho;
+  // The FP32 pre-test (FrnnPre): float coordinates relative to (minx, miny) and the margin.
+  // e = 2^-23 X (X the largest relative coordinate) bounds the rounding of one coordinate
+  // with room to spare; c = cell = the largest radius. A candidate at distance d >= 2c (the
+  // wrapped cell keys can bring far nodes) is outside under both tests: its float distance
+  // is off by a relative 2^-22 at most, far above r^2 + margin. Every other candidate has
+  // |dx|, |dy| < 2c and d^2 < 8 c^2; its float differences are off by eps <= 2e + 2^-24 2c
+  // each, so the float d^2 is off by <= 2 (|dx| + |dy|) eps + 2 eps^2 <= 16 c e + 8 e^2 +
+  // 2^-20 c^2 (+ lower order), its arithmetic by <= 2 ulp(8 c^2) = 2^-20 c^2 and the float
+  // radius by <= 2^-24 c^2: below 16 c e + 8 e^2 + 64 2^-24 c^2.
+  // X may be taken over the node box widened by two cells: a point farther out is more than
+  // 2c from every node, truly outside, and its float distance (off by a relative 2^-23) stays
+  // above 4 c^2 (1 - 2^-22)^2 > r^2 + margin, so it is classified outside too.
+  double maxy = miny;
+  for (int i = 0; i < n_nodes; ++i) maxy = std::max(maxy, nxy[2 * i + 1]);
+  const double ext = std::max(maxx - minx, maxy - miny) + 2.0 * cell;
+  const double e = std::ldexp(ext, -23), fu = std::ldexp(1.0, -24);
+  const double margin = 16.0 * cell * e + 8.0 * e * e + 64.0 * fu * cell * cell;
+  std::vector<float> n32(2 * static_cast<size_t>(n_nodes)), r32;
+  for (int i = 0; i < n_nodes; ++i) {
+    n32[2 * i] = static_cast<float>(nxy[2 * i] - minx);
+    n32[2 * i + 1] = static_cast<float>(nxy[2 * i + 1] - miny);
+  }
+  DevBuf<float> d_n32, d_r32;
+  upload(d_n32, n32.data(), n32.size(), st);
+  if (prm.rho_node) {
+    r32.resize(n_nodes);
+    for (int i = 0; i < n_nodes; ++i) r32[i] = static_cast<float>(rn[i] * rn[i]);
+    upload(d_r32, r32.data(), r32.size(), st);
+  }
+  const FrnnPre pre{reinterpret_cast<const float2*>(d_n32.p), prm.rho_node ? d_r32.p : nullptr,
+                    static_cast<float>(rho2), static_cast<float>(margin)};
   DevBuf<int32_t> d_cnt(n_gp);
   prof_begin(ctx, CGB_PHASE_FRNN);
   if (n_gp > 0)
     frnn_kernel<<<blocks_for(n_gp), kThreads, 0, st>>>(n_gp, out->gp_xy.p, ctx->node_xy.p,
-                                                        d_rn, prm.rho, rho2, G,
+                                                        d_rn, prm.rho, rho2, G, pre,
                                                         nullptr, d_cnt.p, nullptr, nullptr);
   CGB_CUDA(cudaGetLastError());
   prof_end(ctx, CGB_PHASE_FRNN, n_gp > 0 ? 1 : 0);
@@ -1008,7 +1064,7 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
   prof_begin(ctx, CGB_PHASE_FRNN);
   if (n_gp > 0)
     frnn_kernel<<<blocks_for(n_gp), kThreads, 0, st>>>(n_gp, out->gp_xy.p, ctx->node_xy.p,
-                                                        d_rn, prm.rho, rho2, G,
+                                                        d_rn, prm.rho, rho2, G, pre,
                                                         out->nbr_ptr.p, nullptr, out->nbr_idx.p,
                                                         want_s ? out->s.p : nullptr);
   prof_end(ctx, CGB_PHASE_FRNN, n_gp > 0 ? 1 : 0);
