@@ -1,6 +1,6 @@
 // pipe_peaks.cu — measures the FP64 and FP32 FMA throughput of the current GPU, the
-// roofline denominators of the compute-bound kernels (the driver's measured peaks cover
-// only HBM copy bandwidth and bf16 tensor throughput). Built as its own small library
+// roofline denominators of the compute-bound kernels (the machine's measured peaks file
+// covers only HBM copy bandwidth and bf16 tensor throughput). Built as its own small library
 // (libcgb_peaks.so) used by the benchmark; it is not part of the hot-path ABI.
 #include <cuda_runtime.h>
 
