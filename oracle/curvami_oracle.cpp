@@ -946,8 +946,9 @@ int orc_hinge(int n_nodes, const double* x, int n_folds, const orc_fold* folds, 
   // plate/Constraints.h:341-436, folds in order, crease points in order; triplets are
   // summed into K in the order they are generated (setFromTriplets sums duplicates,
   // then K += K_fold, Meshless.h:119-125).
-  const int64_t nnz = outer[3 * n_nodes];
-  std::vector<double> Kf(K_values ? nnz : 0, 0.0);
+  // The pattern is read only when K is wanted (F-only calls pass no pattern).
+  const int64_t nnz = (K_values && outer) ? outer[3 * n_nodes] : 0;
+  std::vector<double> Kf(nnz, 0.0);
   for (int f = 0; f < n_folds; ++f) {
     const orc_fold& fd = folds[f];
     for (int i = 0; i < fd.n_gp; ++i) {
