@@ -27,7 +27,7 @@ def _rank(rank, world, port, out):
 
 def test_two_replicas_agree_on_the_slowest_rank():
     port = _free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:   # no fork of a threaded process
         out = mgr.dict()
         mp.start_processes(_rank, args=(2, port, out), nprocs=2, join=True, start_method="spawn")
         res = dict(out)
