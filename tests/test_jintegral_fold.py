@@ -235,3 +235,27 @@ def test_gpu_fold_terms_match_oracle(o, folded):
             assert abs(a[k] - b[k]) <= 1e-10 * max(abs(b[k]), scale), k
     for k in ("theta", "psi", "fn", "fT", "dpsi_ds"):
         assert np.allclose(gpu_c[0][k], ref_c[0][k], rtol=1e-10, atol=1e-14), k
+
+
+def test_q_analytic_is_the_derivative_of_q_value():
+    """qAnalytic's gradient and second gradient against central differences of qValue,
+    inside the ring (cubic and linear q), and zero outside it."""
+    ring = J.Ring(1.0, 2.5)
+    rng = np.random.default_rng(15)
+    ang = rng.uniform(0.0, 2.0 * math.pi, 40)
+    rad = rng.uniform(1.05, 2.45, 40)
+    P = np.stack([rad * np.cos(ang), rad * np.sin(ang)], 1)
+    hstep = 1e-5
+    for linear in (False, True):
+        q, g, H = J.q_analytic(P, ring, linear)
+        assert np.array_equal(q, J.q_value(np.linalg.norm(P, axis=1), ring, linear))
+        for c in range(2):
+            e = np.zeros(2); e[c] = hstep
+            qp = J.q_value(np.linalg.norm(P + e, axis=1), ring, linear)
+            qm = J.q_value(np.linalg.norm(P - e, axis=1), ring, linear)
+            assert np.abs((qp - qm) / (2 * hstep) - g[:, c]).max() <= 1e-8
+            _, gp, _ = J.q_analytic(P + e, ring, linear)
+            _, gm, _ = J.q_analytic(P - e, ring, linear)
+            assert np.abs((gp - gm) / (2 * hstep) - H[:, :, c]).max() <= 1e-7
+    q, g, H = J.q_analytic(np.array([[0.5, 0.0], [3.0, 0.0]]), ring, False)
+    assert np.array_equal(q, [1.0, 0.0]) and not g.any() and not H.any()
