@@ -13,6 +13,7 @@ fold from the oracle's Kinematics::compute + Constitutive.
   is the rotation everywhere, and every G form vanishes, the line terms by the symmetry of
   the crease points about the tip;
 - the _fold.csv and _crease.csv files carry the reference's columns;
+- qAnalytic's gradient and second gradient are the derivatives of qValue;
 - the GPU point states give the oracle states' fold terms (GPU test).
 """
 import math
