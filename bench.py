@@ -63,8 +63,8 @@ def parse():
     ap.add_argument("--plates", type=int, default=64, help="plates of the batched workload")
     ap.add_argument("--no-shape-stage", action="store_true",
                     help="skip the shape-function stage object (shorter runs under a profiler)")
-    ap.add_argument("--cpu-sample-rows", type=int, default=20,
-                    help="cell rows of the plate in the CPU sample (200 rows = the whole plate)")
+    ap.add_argument("--cpu-rows", type=int, default=None,
+                    help="only the first CPU_ROWS cell rows on the CPU (a quick check; default: the whole plate)")
     return ap.parse_args()
 
 
@@ -87,21 +87,25 @@ def build_workload(n_side):
 # CPU side (the oracle's restatement of the reference's OpenMP assembly)
 # ---------------------------------------------------------------------------------
 
-def cpu_sample(plate, x, rows):
-    """A bounded sample of the same workload: the Gauss points of the first `rows` cell
-    rows of the plate, with their own pattern, shape functions from the oracle."""
+def cpu_workload(plate, x, rows=None):
+    """The workload on the oracle: shape functions of the faces and of both sides of the
+    crease (GlobalFRNN + GlobalRKPM restated), the union pattern and csrMapping
+    (initSparsityPattern restated), the material; then cpu_step assembles. rows=None
+    takes the whole plate; rows=r only the Gauss points of the first r cell rows, with
+    their own pattern (a quick check, not a measurement of the workload)."""
     from oracle import Oracle
 
     h = plate.meta["h"]
-    keep = plate.faces.xy[:, 1] < rows * h
+    keep = np.ones(len(plate.faces.xy), bool) if rows is None else plate.faces.xy[:, 1] < rows * h
     o = Oracle(native=True)
     gp = plate.faces.xy[keep]
     w = plate.faces.weight[keep]
+    t0 = time.perf_counter()
     ptr, idx, s = o.frnn(plate.node_xy, gp, plate.rho)
     psi, dpsi, ddpsi, bad, rc = o.rkpm(plate.node_xy, gp, ptr, idx, s, plate.rho, plate.order, plate.creases)
     folds = []
     for f in plate.folds:
-        sel = f.left.xy[:, 1] < rows * h
+        sel = np.ones(len(f.left.xy), bool) if rows is None else f.left.xy[:, 1] < rows * h
         side = {}
         for nm, ps in (("left", f.left), ("right", f.right)):
             fp, fi, fs = o.frnn(plate.node_xy, ps.xy[sel], plate.rho)
@@ -111,16 +115,18 @@ def cpu_sample(plate, x, rows):
                       "tangent": f.left.tangent[sel], "Kt": f.Kt, "theta0": f.theta0})
     outer, inner, col_ptr, col_nodes, mp = o.pattern(plate.n_nodes, ptr, idx, folds)
     A, B, D = o.abd(plate.E, plate.nu, plate.thickness)
-    return dict(o=o, n_gp=int(keep.sum()), w=w, ptr=ptr, idx=idx, dpsi=dpsi, ddpsi=ddpsi, folds=folds,
-                outer=outer, col_ptr=col_ptr, col_nodes=col_nodes, mp=mp, A=A, B=B, D=D, x=x,
-                n_nodes=plate.n_nodes)
+    return dict(o=o, n_gp=int(keep.sum()), w=w, ptr=ptr, idx=idx, psi=psi, dpsi=dpsi, ddpsi=ddpsi, folds=folds,
+                outer=outer, inner=inner, col_ptr=col_ptr, col_nodes=col_nodes, mp=mp, A=A, B=B, D=D, x=x,
+                n_nodes=plate.n_nodes, whole=rows is None, setup_s=time.perf_counter() - t0)
 
 
 def cpu_step(S, threads):
+    """NonLinearAssembler::updateStiffness + Constraints::evaluateElasticFold restated
+    (the reference's OpenMP loops), K and F of the workload at S["x"]."""
     o = S["o"]
     K, F = o.update_stiffness(S["n_nodes"], S["w"], S["ptr"], S["idx"], S["dpsi"], S["ddpsi"], S["outer"],
                               S["mp"], S["x"], S["A"], S["B"], S["D"], want_K=True, n_threads=threads)
-    o.hinge(S["n_nodes"], S["x"], S["folds"], S["outer"], S["col_ptr"], S["col_nodes"], K, F)
+    return o.hinge(S["n_nodes"], S["x"], S["folds"], S["outer"], S["col_ptr"], S["col_nodes"], K, F)
 
 
 def cpu_time(S, threads, steps, warmup=1):
@@ -128,8 +134,16 @@ def cpu_time(S, threads, steps, warmup=1):
         cpu_step(S, threads)
     t0 = time.perf_counter()
     for _ in range(steps):
-        cpu_step(S, threads)
-    return (time.perf_counter() - t0) / steps
+        out = cpu_step(S, threads)
+    return (time.perf_counter() - t0) / steps, out
+
+
+def cpu_sample_text(S):
+    what = ("the whole workload (640,000 Gauss points, its pattern and hinge points)" if S["whole"] else
+            f"{S['n_gp']} Gauss points of the first cell rows, with their own pattern and hinge points")
+    return (f"{what}; per step NonLinearAssembler::updateStiffness + Constraints::evaluateElasticFold restated "
+            f"(OpenMP, the reference's -O2 native release flags); shape functions and pattern built once by the "
+            f"oracle ({S['setup_s']:.1f} s, not timed)")
 
 
 def run_reference(args):
@@ -137,21 +151,72 @@ def run_reference(args):
     if rank != 0:
         return
     plate, x = build_workload(args.n_side)
-    S = cpu_sample(plate, x, args.cpu_sample_rows)
+    S = cpu_workload(plate, x, args.cpu_rows)
     cores = os.cpu_count() or 1
-    t = cpu_time(S, cores, max(args.steps, 1), max(args.warmup, 1))
+    t, _ = cpu_time(S, cores, max(args.steps, 1), max(args.warmup, 1))
     v = S["n_gp"] / t
-    sample = (f"first {args.cpu_sample_rows} of 200 cell rows of the workload ({S['n_gp']} Gauss points, "
-              f"their own pattern and hinge points); per step NonLinearAssembler::updateStiffness + "
-              f"evaluateElasticFold")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "seed": SEED, "threads": cores},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "config": {"workload": WORKLOAD, "seed": SEED, "threads": cores, "n_gauss_points": S["n_gp"],
+                   "same_config": S["whole"]},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": cpu_sample_text(S)},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
+
+
+def rel_errors(K, F, Ko, Fo):
+    """||dF||_inf / ||F_o||_inf, ||dK||_F / ||K_o||_F and max |dK| / max |K_o| against the
+    oracle's K and F (the same CSC pattern, index by index)."""
+    return {"F_rel_inf": float(np.abs(F - Fo).max() / np.abs(Fo).max()),
+            "K_rel_fro": float(np.linalg.norm(K - Ko) / np.linalg.norm(Ko)),
+            "K_rel_max": float(np.abs(K - Ko).max() / np.abs(Ko).max())}
+
+
+def errors_vs_oracle(cg, ctx, plate, model, S, Ko, Fo):
+    """The GPU's K and F against the oracle's on the whole workload at the same x:
+    - on_oracle_shape_functions: the GPU assembly fed the oracle's Phi derivatives (faces
+      and both crease sides), i.e. stage B alone on identical inputs -- the error the
+      metric states;
+    - on_gpu_shape_functions: the library end to end (its own stage A, then stage B);
+      near the crease the FP64 shape functions of two implementations differ by about
+      cond(M) eps (crease-truncated supports), which this includes."""
+    g_outer, g_inner = model.asm.pattern()
+    same = bool(np.array_equal(g_outer, S["outer"]) and np.array_equal(g_inner, S["inner"]))
+    out = {"pattern_bit_exact": same, "n_gauss_points": S["n_gp"], "bar": "F_rel_inf <= 1e-10 (mixed, stage B)"}
+    if not same:
+        return out
+    MIX = cg.TANGENT | cg.HINGE | cg.MIXED
+    F64 = cg.TANGENT | cg.HINGE
+    x = S["x"]
+    gpu = {}
+    for name, fl in (("mixed", MIX), ("fp64", F64)):
+        K, F = model.asm.assemble(x, fl)
+        gpu[name] = rel_errors(K, F, Ko, Fo)
+    out["on_gpu_shape_functions"] = gpu
+    faces = cg.shape_from_host(ctx, S["ptr"], S["idx"], S["dpsi"], S["ddpsi"], S["psi"])
+    folds = []
+    for f in S["folds"]:
+        sides = {}
+        for nm in ("left", "right"):
+            d = f[nm]
+            sides[nm] = cg.shape_from_host(ctx, d["ptr"], d["idx"], d["dpsi"], np.zeros((len(d["idx"]), 3)))
+        folds.append({"left": sides["left"], "right": sides["right"], "weight": f["weight"],
+                      "tangent": f["tangent"], "Kt": f["Kt"], "theta0": f["theta0"]})
+    asm = cg.NonLinearAssembler(ctx, faces, S["w"], folds)
+    asm.set_material(*cg.abd_isotropic(plate.E, plate.nu, plate.thickness))
+    o_outer, _ = asm.pattern()
+    stage_b = {}
+    for name, fl in (("mixed", MIX), ("fp64", F64)):
+        K, F = asm.assemble(x, fl)
+        stage_b[name] = rel_errors(K, F, Ko, Fo)
+    out["on_oracle_shape_functions"] = stage_b
+    asm.close()
+    for f in folds:
+        f["left"].close(); f["right"].close()
+    faces.close()
+    return out
 
 
 # ---------------------------------------------------------------------------------
@@ -390,14 +455,16 @@ def run_gpu(args):
     }
 
     cpu = None
+    err_oracle = None
     if rank == 0 and not args.no_cpu_baseline:
-        S = cpu_sample(plate, x, args.cpu_sample_rows)
+        S = cpu_workload(plate, x, args.cpu_rows)
         cores = os.cpu_count() or 1
-        t_all = cpu_time(S, cores, 2)
+        t_all, (Ko, Fo) = cpu_time(S, cores, 2)
         cpu = {"value": S["n_gp"] / t_all, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": (f"first {args.cpu_sample_rows} of 200 cell rows ({S['n_gp']} Gauss points, own "
-                          f"pattern and hinge points), updateStiffness + evaluateElasticFold, OpenMP "
-                          f"restatement built with the reference's -O2 native flags, mean of 2 runs")}
+               "sample": cpu_sample_text(S) + ", mean of 2 steps after 1 warm-up", "same_config": S["whole"]}
+        if S["whole"]:
+            err_oracle = errors_vs_oracle(cg, ctx, plate, model, S, Ko, Fo)
+        del S, Ko, Fo
 
     v_mix = world * n_gp / (ms_mix * 1e-3)
     v_f64 = world * n_gp / (ms_f64 * 1e-3)
@@ -432,6 +499,7 @@ def run_gpu(args):
         "deterministic_mixed": {"value": world * n_gp / (ms_det * 1e-3), "ms_per_step": ms_det},
         "residual_only": {"value": world * n_gp / (ms_res * 1e-3), "ms_per_step": ms_res},
         "error_mixed_vs_fp64": err,
+        "error_vs_oracle": err_oracle,
         "phases_ms": {k: v / max(args.steps, 1) for k, v in ph_ms.items()},
         "e2e": {"value": world * n_gp / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": int(asm.n_dofs * 8),

@@ -30,11 +30,13 @@
 // deterministic: every block value goes to a contribution array and a second kernel
 // sums each block's contributions in ascending Gauss-point order.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <string>
 
 #include "cgb_device.cuh"
 #include "cgb_internal.h"
+#include "cgb_umma.cuh"
 
 namespace cgb {
 namespace {
@@ -43,6 +45,9 @@ constexpr int kFaceWarps = 4;
 constexpr int kRecI = 9;   // dx dy beta0 beta1 beta2 Tu g0 g1 g2
 constexpr int kRecJ = 23;  // P(9) Q(9) cW0 cW1 nW0 nW1 TuW
 constexpr int kRec = kRecI + kRecJ;
+// Device error word bit: an index of caller-owned arrays was out of range (allocation-free
+// entry point); the access was skipped.
+constexpr int kErrIndex = 8;
 
 struct Material {
   double A[9], B[9], D[9];
@@ -78,6 +83,11 @@ struct FaceArgs {
   const int64_t* map_ptr;
   const int32_t* map_slot;
   const int32_t* outer;  // scalar CSC column starts (POS_MAP only)
+  // POS_MAP only (caller-owned arrays): the bounds every index is checked against, and
+  // the error word that records a violation (the access is skipped).
+  int64_t n_blocks;
+  int n_nodes;
+  int* err;
   // Phase-1 copy of the neighbour data in sliced-ELL order: Gauss point 32 W + l, entry
   // q at sell_ptr[W] + 32 q + l (null: read the CSR arrays).
   const int64_t* sell_ptr;
@@ -85,6 +95,8 @@ struct FaceArgs {
   const double* sdpsi;
   const double* sddpsi;
   Material mat;
+  NatCurv nc;               // natural curvature (inactive by default)
+  const double* gp_xy;      // the points' reference coordinates (set when nc is active)
   double* F;         // atomic F (3 n_nodes)
   double* Fc;        // deterministic F contributions (3 per entry)
   void* Kacc;        // atomic block accumulator
@@ -99,9 +111,20 @@ struct PointState {
   double pXY[2];
   double bv;
   double e0[3], e1[3];
+  double e1el[3];  // elastic bending strain E1_el = E1 + kappa_bar (Voigt), what N and M see
 };
 
-__device__ __forceinline__ void point_state(const double s[15], const Material& m, PointState& P) {
+// kappa_bar_XX of the natural-curvature band at reference X (plate/Kinematics.h:25-34).
+__device__ __forceinline__ double natcurv_kappa(const NatCurv& nc, double X) {
+  if (!nc.active) return 0.0;
+  const double t = (X - nc.x0) / nc.width;
+  return nc.amp * exp(-t * t);
+}
+
+// kbar: the natural curvature's kappa_bar_XX at the point (0 without one); it enters E1_el
+// only (Kinematics.h:110-111, Constitutive.h:65).
+__device__ __forceinline__ void point_state(const double s[15], const Material& m, PointState& P,
+                                            double kbar = 0.0) {
   P.a1[0] = 1.0 + s[0]; P.a1[1] = s[1]; P.a1[2] = s[2];
   P.a2[0] = s[3]; P.a2[1] = 1.0 + s[4]; P.a2[2] = s[5];
 #pragma unroll
@@ -123,12 +146,13 @@ __device__ __forceinline__ void point_state(const double s[15], const Material& 
   P.e1[0] = -(P.rxx[0] * P.b[0] + P.rxx[1] * P.b[1] + P.rxx[2] * P.b[2]);
   P.e1[1] = -(P.ryy[0] * P.b[0] + P.ryy[1] * P.b[1] + P.ryy[2] * P.b[2]);
   P.e1[2] = 2.0 * -(P.rxy[0] * P.b[0] + P.rxy[1] * P.b[1] + P.rxy[2] * P.b[2]);
+  P.e1el[0] = P.e1[0] + kbar; P.e1el[1] = P.e1[1]; P.e1el[2] = P.e1[2];
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     P.N[r] = m.A[3 * r] * P.e0[0] + m.A[3 * r + 1] * P.e0[1] + m.A[3 * r + 2] * P.e0[2] +
-             (m.B[3 * r] * P.e1[0] + m.B[3 * r + 1] * P.e1[1] + m.B[3 * r + 2] * P.e1[2]);
+             (m.B[3 * r] * P.e1el[0] + m.B[3 * r + 1] * P.e1el[1] + m.B[3 * r + 2] * P.e1el[2]);
     P.M[r] = m.B[r] * P.e0[0] + m.B[3 + r] * P.e0[1] + m.B[6 + r] * P.e0[2] +
-             (m.D[3 * r] * P.e1[0] + m.D[3 * r + 1] * P.e1[1] + m.D[3 * r + 2] * P.e1[2]);
+             (m.D[3 * r] * P.e1el[0] + m.D[3 * r + 1] * P.e1el[1] + m.D[3 * r + 2] * P.e1el[2]);
   }
   double vc[3];
 #pragma unroll
@@ -214,7 +238,9 @@ enum : int { S_A1 = 0, S_A2 = 3, S_B = 6, S_RXX = 9, S_RYY = 12, S_RXY = 15, S_C
 // Phase 1 for the Gauss point g0 + lane (g0 a multiple of 32): FP64 kinematics,
 // resultants and residual (F atomics, or per-entry contributions when DET); when st is
 // not null the point's state goes to st[field * st_stride + st_idx] in TK.
-template <typename TK, bool DET>
+// CHECK (caller-owned arrays only): a neighbour id outside [0, n_nodes) is flagged in the
+// error word and the neighbour is left out.
+template <typename TK, bool DET, bool CHECK = false>
 __device__ __forceinline__ void phase1_point(const FaceArgs& a, int g0, int lane, TK* st, int64_t st_stride,
                                              int64_t st_idx) {
   const Material& m = a.mat;
@@ -237,6 +263,10 @@ __device__ __forceinline__ void phase1_point(const FaceArgs& a, int g0, int lane
       for (int q = 0; q < n; ++q) {
         const int64_t e = sb + q * stride;
         const int64_t j = Ix[e];
+        if (CHECK && (j < 0 || j >= a.n_nodes)) {
+          atomicOr(a.err, kErrIndex);
+          continue;
+        }
         const double u0 = a.x[3 * j], u1 = a.x[3 * j + 1], u2 = a.x[3 * j + 2];
         const double2 d = reinterpret_cast<const double2*>(Dp)[e];
         const double dxx = Ddp[3 * e], dyy = Ddp[3 * e + 1], dxy = Ddp[3 * e + 2];
@@ -247,7 +277,7 @@ __device__ __forceinline__ void phase1_point(const FaceArgs& a, int g0, int lane
         s[12] += u0 * dxy; s[13] += u1 * dxy; s[14] += u2 * dxy;
       }
       PointState P;
-      point_state(s, m, P);
+      point_state(s, m, P, a.gp_xy ? natcurv_kappa(a.nc, a.gp_xy[2 * static_cast<int64_t>(g)]) : 0.0);
       const double W = a.weight[g];
       // f_I = W (Bm_I^T N + Bb_I^T M) (Assembly.h:249) = W (a1 u1 + a2 u2 + b Tu_I), since
       // beta_I . M = dPhi_I . pXY - (Phi_XX M0 + 2 Phi_XY M2 + Phi_YY M1) = Tu_I.
@@ -272,6 +302,7 @@ __device__ __forceinline__ void phase1_point(const FaceArgs& a, int g0, int lane
             for (int c = 0; c < 3; ++c) a.Fc[3 * e + c] = f[c];
           } else {
             const int64_t node = Ix[es];
+            if (CHECK && (node < 0 || node >= a.n_nodes)) continue;
 #pragma unroll
             for (int c = 0; c < 3; ++c) atomicAdd(a.F + 3 * node + c, f[c]);
           }
@@ -314,6 +345,10 @@ __device__ __forceinline__ void phase2_group(const FaceArgs& a, int g0, int lane
     const int64_t p0 = a.ptr[gg];
     const int n = static_cast<int>(a.ptr[gg + 1] - p0);
     if (n == 0) continue;  // Assembly.h:208
+    if (POS_MAP && n > nmax) {  // the records are staged for nmax neighbours
+      if (lane == 0) atomicOr(a.err, kErrIndex);
+      continue;
+    }
     TK a1t[3], a2t[3], bt[3], rxx[3], ryy[3], rxy[3], Nt[3], Mt[3], Ci[4];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -457,7 +492,10 @@ __device__ __forceinline__ void phase2_group(const FaceArgs& a, int g0, int lane
         store_contrib<TK>(a.Kc, m0 + p, flip, v);
       } else if (POS_MAP) {
         const int hi = flip ? nid[i] : nid[j];
-        scatter_atomic<TK>(a.Kacc, a.outer[3 * static_cast<int64_t>(hi)] / 9 + a.map_slot[m0 + p], flip, v);
+        const int64_t slot = hi >= 0 && hi < a.n_nodes
+                                 ? a.outer[3 * static_cast<int64_t>(hi)] / 9 + a.map_slot[m0 + p] : -1;
+        if (slot >= 0 && slot < a.n_blocks) scatter_atomic<TK>(a.Kacc, static_cast<int32_t>(slot), flip, v);
+        else atomicOr(a.err, kErrIndex);
       } else {
         scatter_atomic<TK>(a.Kacc, a.map_slot[m0 + p], flip, v);
       }
@@ -483,7 +521,7 @@ __global__ void __launch_bounds__(32 * kFaceWarps, sizeof(TK) == 4 ? 5 : 3) face
     // Phase 1: one Gauss point per lane, FP64. Every lane does distinct work, so no FP64
     // issue slot is spent on a redundant or masked copy (on GB300 an FP64 warp
     // instruction costs the same with 1 or 32 lanes).
-    phase1_point<TK, DET>(a, g0, lane, WANT_K ? st : static_cast<TK*>(nullptr), 32, lane);
+    phase1_point<TK, DET, POS_MAP>(a, g0, lane, WANT_K ? st : static_cast<TK*>(nullptr), 32, lane);
     if (!WANT_K) continue;
     __syncwarp();
     phase2_group<TK, DET, TIN, POS_MAP, BZERO>(a, g0, lane, st, rec, nid);
@@ -786,16 +824,22 @@ __global__ void blocks_to_csc(int n_nodes, const int64_t* __restrict__ col_ptr, 
 
 // The same output step with the block columns taken from the scalar CSC outer index:
 // column node j starts at block outer[3j] / 9 and holds (outer[3j+1] - outer[3j]) / 3 blocks.
+// A column whose blocks would fall outside [0, n_blocks) is skipped and flagged.
 template <typename TA, int STRIDE>
-__global__ void blocks_to_csc_outer(int n_nodes, const int32_t* __restrict__ outer, const TA* __restrict__ acc,
-                                    double* __restrict__ K) {
+__global__ void blocks_to_csc_outer(int n_nodes, int64_t n_blocks, const int32_t* __restrict__ outer,
+                                    const TA* __restrict__ acc, double* __restrict__ K, int* err) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   for (int64_t j = warp; j < n_nodes; j += nw) {
-    const int64_t b0 = outer[3 * j] / 9;
+    const int64_t o = outer[3 * j];
+    const int64_t b0 = o / 9;
     const int len = (outer[3 * j + 1] - outer[3 * j]) / 3;
-    double* col = K + outer[3 * j];
+    if (o < 0 || o % 9 != 0 || len < 0 || b0 + len > n_blocks) {
+      if (lane == 0) atomicOr(err, kErrIndex);
+      continue;
+    }
+    double* col = K + o;
     for (int t = lane; t < 9 * len; t += 32) {
       const int c = t / (3 * len), rem = t - c * 3 * len, pos = rem / 3, r = rem - 3 * pos;
       col[t] = static_cast<double>(acc[(b0 + pos) * STRIDE + 3 * r + c]);
@@ -844,7 +888,7 @@ __global__ void det_reduce_F(int n_nodes, const int64_t* __restrict__ lptr, cons
 __global__ void __launch_bounds__(128) face_energy_kernel(int n_gp, const int64_t* ptr, const int32_t* idx,
                                                           const double* dpsi, const double* ddpsi,
                                                           const double* weight, const double* x, Material m,
-                                                          double* out) {
+                                                          NatCurv nc, const double* gp_xy, double* out) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
@@ -855,10 +899,10 @@ __global__ void __launch_bounds__(128) face_energy_kernel(int n_gp, const int64_
     double s[15];
     kin_sums(lane, p0, n, idx, dpsi, ddpsi, x, s);
     PointState P;
-    point_state(s, m, P);
-    if (lane == 0) {
+    point_state(s, m, P, gp_xy ? natcurv_kappa(nc, gp_xy[2 * g]) : 0.0);
+    if (lane == 0) {   // Meshless.h:204-220, with E1_el (Meshless.h:212)
       em += 0.5 * weight[g] * (P.e0[0] * P.N[0] + P.e0[1] * P.N[1] + P.e0[2] * P.N[2]);
-      eb += 0.5 * weight[g] * (P.e1[0] * P.M[0] + P.e1[1] * P.M[1] + P.e1[2] * P.M[2]);
+      eb += 0.5 * weight[g] * (P.e1el[0] * P.M[0] + P.e1el[1] * P.M[1] + P.e1el[2] * P.M[2]);
     }
   }
   if (lane == 0) { atomicAdd(out, em); atomicAdd(out + 1, eb); }
@@ -876,6 +920,7 @@ __global__ void __launch_bounds__(128) point_state_kernel(int n, const int64_t* 
                                                           const double* __restrict__ dpsi,
                                                           const double* __restrict__ ddpsi,
                                                           const double* __restrict__ x, Material m,
+                                                          NatCurv nc, const double* __restrict__ gp_xy,
                                                           double* __restrict__ out) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
@@ -894,7 +939,7 @@ __global__ void __launch_bounds__(128) point_state_kernel(int n, const int64_t* 
     s[12] += u0 * dxy; s[13] += u1 * dxy; s[14] += u2 * dxy;
   }
   PointState P;
-  point_state(s, m, P);
+  point_state(s, m, P, gp_xy ? natcurv_kappa(nc, gp_xy[2 * static_cast<int64_t>(g)]) : 0.0);
   double* o = out + static_cast<int64_t>(g) * kPointStateCols;
   for (int c = 0; c < 3; ++c) {
     o[c] = u[c];
@@ -945,6 +990,10 @@ struct MergeArgs {
   const uint16_t* code;       // point (4) | i (6) | j (6)
   int* err;                   // set to kErrStage when a staging copy never completes
   uint32_t extra_tx;          // 0; the failure-detection test expects bytes that never arrive
+  // The merged kernel's groups: glist[0 .. gcount) when glist is set (the groups the tensor
+  // tangent does not take), else every group of [g_begin, g_end).
+  const int32_t* glist;
+  int gcount;
 };
 
 // ---- bulk-copy (TMA) staging --------------------------------------------------------
@@ -1077,8 +1126,9 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
   const Material& m = a.mat;
   // Groups of this launch: [g_begin, g_end) are multiples of kMG apart (chunk bounds are
   // multiples of 32), so a group never straddles two launches.
-  const int G1 = (a.g_end + kMG - 1) / kMG;
-  const int Gfirst = a.g_begin / kMG + blockIdx.x;
+  const int G0 = a.g_begin / kMG;
+  const int nG = mg.glist ? mg.gcount : (a.g_end + kMG - 1) / kMG - G0;
+  auto group = [&](int gi) { return mg.glist ? mg.glist[gi] : G0 + gi; };
   // Thread 0 starts the copies of group G's ranges; every thread later waits on the phase.
   auto stage = [&](int G) {
     const int g0 = G * kMG, g1 = min(g0 + kMG, a.g_end);
@@ -1091,11 +1141,12 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
   };
   if (threadIdx.x == 0) {
     mbar_init(&stage_bar);
-    if (Gfirst < G1) stage(Gfirst);
+    if (static_cast<int>(blockIdx.x) < nG) stage(group(blockIdx.x));
   }
   __syncthreads();
   uint32_t phase = 0;
-  for (int G = Gfirst; G < G1; G += gridDim.x) {
+  for (int gi = blockIdx.x; gi < nG; gi += gridDim.x) {
+    const int G = group(gi);
     const int g0 = G * kMG;
     const int kn = min(kMG, a.g_end - g0);
     for (int t = threadIdx.x; t < kState * kMG; t += blockDim.x) {
@@ -1194,7 +1245,7 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
     __syncthreads();
     // The staging buffers are free again: start the next group's copies, which land while
     // this group's entries are summed.
-    if (threadIdx.x == 0 && G + static_cast<int>(gridDim.x) < G1) stage(G + gridDim.x);
+    if (threadIdx.x == 0 && gi + static_cast<int>(gridDim.x) < nG) stage(group(gi + gridDim.x));
     float4* acc4 = static_cast<float4*>(a.Kacc);
     const int64_t cbase = a.map_ptr[g0];
     if (!DET && mg.direct[G]) {
@@ -1251,16 +1302,25 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
   }
 }
 
+#include "tangent_tc.cuh"
+
 inline unsigned nb(int64_t n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
 
+// SM count per device ordinal, looked up once per device (grids are sized from it).
 int sm_count(int device) {
-  static int cached = -1;
-  if (cached < 0) {
+  constexpr int kMaxDev = 64;
+  static std::atomic<int> cached[kMaxDev];
+  if (device < 0 || device >= kMaxDev) {
     int v = 0;
     CGB_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device));
-    cached = v;
+    return v;
   }
-  return cached;
+  int v = cached[device].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    CGB_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device));
+    cached[device].store(v, std::memory_order_relaxed);
+  }
+  return v;
 }
 
 HingeArgs hinge_args(cgb_assembler* a, cgb_fold_dev& f, const double* d_x, int flags) {
@@ -1424,6 +1484,12 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
     merge_prepare(a);
     merged = !det || a->mrg_n_direct == 0;
   }
+  // The tensor-core tangent takes the merged path's cells whose node union fits one
+  // 128-row tile (its entries are the merged entries, so the deterministic lists are the
+  // same).
+  const size_t tcsm = tc_smem_bytes(std::max(S->max_n, 1));
+  const bool use_tc = merged && a->tuning.tangent_kind == CGB_TANGENT_TENSOR && tcsm <= kMergedSmemMax;
+  if (use_tc) tc_prepare(a);
   if (det && want_K) {
     if (merged) deterministic_entry_lists(a);
     else deterministic_pair_lists(a);
@@ -1473,6 +1539,8 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   ensure_sell(a);
   fa.sell_ptr = a->sell_ptr.p; fa.sidx = a->sidx.p; fa.sdpsi = a->sdpsi.p; fa.sddpsi = a->sddpsi.p;
   fa.mat = make_material(a->A, a->B, a->D);
+  fa.nc = ctx->natcurv;
+  fa.gp_xy = natcurv_points(ctx, S, "assemble");
   fa.F = d_F;
   fa.Fc = a->fcontrib.p;
   fa.Kacc = mixed ? static_cast<void*>(a->kacc32.p) : static_cast<void*>(a->kacc64.p);
@@ -1557,18 +1625,46 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
       if (tsm > 48 * 1024) CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tsm)));
       kern<<<tgrid, 32 * kTanWarps, tsm, a->side>>>(fa, stp);
     };
+    int ntan = 1;
     if (merged) {
       MergeArgs mg{a->mrg_ent_ptr.p, a->mrg_ent_slot.p, a->mrg_ent_cstart.p, a->mrg_direct.p, a->mrg_code.p,
-                   ctx->dev_err.p, a->test_stage_extra_tx};
+                   ctx->dev_err.p, a->test_stage_extra_tx, nullptr, 0};
       auto kern = det ? (bzero ? face_tangent_merged_kernel<true, true> : face_tangent_merged_kernel<false, true>)
                       : (bzero ? face_tangent_merged_kernel<true, false> : face_tangent_merged_kernel<false, false>);
       CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(msm)));
       int per_sm = 0;
       CGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMrgThreads, msm));
-      const int groups = (fa.g_end + kMG - 1) / kMG - fa.g_begin / kMG;
+      const int Gb = fa.g_begin / kMG, Ge = (fa.g_end + kMG - 1) / kMG;
+      const int groups = Ge - Gb;
       if (a->tuning.tangent_ctas_per_sm > 0) per_sm = std::min(per_sm, a->tuning.tangent_ctas_per_sm);
-      const unsigned mgrid = static_cast<unsigned>(std::max(1, std::min(groups, std::max(per_sm, 1) * sms)));
-      kern<<<mgrid, kMrgThreads, msm, a->side>>>(fa, st32, mg);
+      if (use_tc) {
+        // Cells whose node union fits one 128-row tile: one tensor-core product each; the
+        // others (sorted group list, this chunk's part) on the CUDA cores.
+        TcArgs tca{a->tc_nbr_u.p, a->tc_cell_U.p, a->tc_ent_uv.p};
+        auto tk = det ? (bzero ? face_tangent_tc_kernel<true, true> : face_tangent_tc_kernel<false, true>)
+                      : (bzero ? face_tangent_tc_kernel<true, false> : face_tangent_tc_kernel<false, false>);
+        CGB_CUDA(cudaFuncSetAttribute(tk, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tcsm)));
+        int tc_per_sm = 0;
+        CGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tc_per_sm, tk, kTcThreads, tcsm));
+        tc_per_sm = std::min(std::max(tc_per_sm, 1), 2);   // 2 x 128 tensor-memory columns per SM at most
+        const unsigned tgrid2 = static_cast<unsigned>(std::max(1, std::min(groups, tc_per_sm * sms)));
+        tk<<<tgrid2, kTcThreads, tcsm, a->side>>>(fa, st32, mg, tca);
+        const auto& fb = a->tc_fallback_h;
+        const int lo = static_cast<int>(std::lower_bound(fb.begin(), fb.end(), Gb) - fb.begin());
+        const int hi = static_cast<int>(std::lower_bound(fb.begin(), fb.end(), Ge) - fb.begin());
+        ntan = 1;
+        if (hi > lo) {
+          MergeArgs mf = mg;
+          mf.glist = a->tc_fallback.p + lo;
+          mf.gcount = hi - lo;
+          const unsigned fgrid = static_cast<unsigned>(std::max(1, std::min(hi - lo, std::max(per_sm, 1) * sms)));
+          kern<<<fgrid, kMrgThreads, msm, a->side>>>(fa, st32, mf);
+          ntan = 2;
+        }
+      } else {
+        const unsigned mgrid = static_cast<unsigned>(std::max(1, std::min(groups, std::max(per_sm, 1) * sms)));
+        kern<<<mgrid, kMrgThreads, msm, a->side>>>(fa, st32, mg);
+      }
     } else if (mixed) {
       if (det) { if (bzero) tl(face_tangent_kernel<float, true, true>, st32); else tl(face_tangent_kernel<float, true, false>, st32); }
       else { if (bzero) tl(face_tangent_kernel<float, false, true>, st32); else tl(face_tangent_kernel<float, false, false>, st32); }
@@ -1577,7 +1673,7 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
       else { if (bzero) tl(face_tangent_kernel<double, false, true>, st64); else tl(face_tangent_kernel<double, false, false>, st64); }
     }
     ++nface;
-    prof_end(ctx, CGB_PHASE_TANGENT, 1, a->side);
+    prof_end(ctx, CGB_PHASE_TANGENT, ntan, a->side);
     CGB_CUDA(cudaGetLastError());
   }
   (void)nface;
@@ -1638,7 +1734,7 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
 // Mixed-precision face assembly on caller-owned device arrays, with the FP32 block
 // accumulator supplied by the caller (the allocation-free entry point, noalloc.cu).
 void face_mixed_on_arrays(const cgb_face_problem& pr, const double* d_x, double* d_K, double* d_F,
-                          float* kacc, cudaStream_t st) {
+                          float* kacc, int* err, cudaStream_t st) {
   FaceArgs fa{};
   fa.n_gp = pr.n_gp;
   fa.g_begin = 0;
@@ -1652,7 +1748,14 @@ void face_mixed_on_arrays(const cgb_face_problem& pr, const double* d_x, double*
   fa.F = d_F;
   fa.Kacc = kacc;
   const int64_t n_blocks = static_cast<int64_t>(pr.nnz / 9);
+  fa.n_blocks = n_blocks;
+  fa.n_nodes = pr.n_nodes;
+  fa.err = err;
   CGB_CUDA(cudaMemsetAsync(d_F, 0, 3 * static_cast<size_t>(pr.n_nodes) * sizeof(double), st));
+  if (pr.n_gp == 0) {  // no face point: K is zero, and outer is not needed
+    if (pr.nnz > 0) CGB_CUDA(cudaMemsetAsync(d_K, 0, static_cast<size_t>(pr.nnz) * sizeof(double), st));
+    return;
+  }
   CGB_CUDA(cudaMemsetAsync(kacc, 0, 12 * static_cast<size_t>(n_blocks) * sizeof(float), st));
   const size_t smem = static_cast<size_t>(kFaceWarps) * ((kState * 32 + kRec * fa.nmax) * sizeof(float) +
                                                         fa.nmax * sizeof(int));
@@ -1661,12 +1764,10 @@ void face_mixed_on_arrays(const cgb_face_problem& pr, const double* d_x, double*
   int dev = 0;
   CGB_CUDA(cudaGetDevice(&dev));
   const int sms = sm_count(dev);
-  if (pr.n_gp > 0) {
-    const unsigned grid = std::max(1u, std::min(nb(pr.n_gp, 32 * kFaceWarps), static_cast<unsigned>(sms * 8)));
-    kern<<<grid, 32 * kFaceWarps, smem, st>>>(fa);
-  }
+  const unsigned grid = std::max(1u, std::min(nb(pr.n_gp, 32 * kFaceWarps), static_cast<unsigned>(sms * 8)));
+  kern<<<grid, 32 * kFaceWarps, smem, st>>>(fa);
   const unsigned cg = std::max(1u, std::min(nb(pr.n_nodes, 4), static_cast<unsigned>(sms * 32)));
-  blocks_to_csc_outer<float, 12><<<cg, 128, 0, st>>>(pr.n_nodes, pr.outer, kacc, d_K);
+  blocks_to_csc_outer<float, 12><<<cg, 128, 0, st>>>(pr.n_nodes, n_blocks, pr.outer, kacc, d_K, err);
   CGB_CUDA(cudaGetLastError());
 }
 
@@ -1676,8 +1777,10 @@ void point_state_device(cgb_context* ctx, const cgb_shape* S, const double* d_x,
   if (!S->psi.p || S->psi.n < static_cast<size_t>(std::max<int64_t>(S->nnz, 1)))
     throw Error(CGB_ERR_INVALID, "point state: the shape set has no Psi");
   const Material m = make_material(A, B, D);
+  const double* xy = natcurv_points(ctx, S, "point state");
   point_state_kernel<<<nb(S->n_gp, 128), 128, 0, ctx->stream>>>(S->n_gp, S->nbr_ptr.p, S->nbr_idx.p, S->psi.p,
-                                                                S->dpsi.p, S->ddpsi.p, d_x, m, d_out);
+                                                                S->dpsi.p, S->ddpsi.p, d_x, m, ctx->natcurv, xy,
+                                                                d_out);
   CGB_CUDA(cudaGetLastError());
 }
 
@@ -1689,8 +1792,9 @@ void energies_device(cgb_assembler* a, const double* d_x, double* out3) {
   const Material m = make_material(a->A, a->B, a->D);
   const cgb_shape* S = a->faces;
   if (S->n_gp)
-    face_energy_kernel<<<std::max(1u, std::min(nb(S->n_gp, 4), 152u * 32u)), 128, 0, st>>>(
-        S->n_gp, S->nbr_ptr.p, S->nbr_idx.p, S->dpsi.p, S->ddpsi.p, a->weight.p, d_x, m, a->energy.p);
+    face_energy_kernel<<<std::max(1u, std::min(nb(S->n_gp, 4), static_cast<unsigned>(sm_count(ctx->device) * 32))), 128, 0, st>>>(
+        S->n_gp, S->nbr_ptr.p, S->nbr_idx.p, S->dpsi.p, S->ddpsi.p, a->weight.p, d_x, m, ctx->natcurv,
+        natcurv_points(ctx, S, "energies"), a->energy.p);
   for (auto& f : a->folds) {
     if (!f.n_gp) continue;
     HingeArgs h = hinge_args(a, f, d_x, 0);

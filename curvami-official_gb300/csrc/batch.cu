@@ -61,6 +61,8 @@ void shape_concat(cgb_context* ctx, const cgb_shape* const* sets, const int32_t*
   out->nnz = nnz;
   out->max_n = max_n;
   out->gp_xy.alloc(2 * n_gp);
+  out->has_xy = true;
+  for (int k = 0; k < n_sets; ++k) out->has_xy = out->has_xy && (sets[k]->has_xy || sets[k]->n_gp == 0);
   out->nbr_ptr.alloc(n_gp + 1);
   out->nbr_idx.alloc(nnz);
   if (have_s) out->s.alloc(nnz);
@@ -146,6 +148,8 @@ int cgb_assembler_set_tuning(cgb_assembler* a, const cgb_tuning* t) {
       throw Error(CGB_ERR_INVALID, "cgb_assembler_set_tuning: residual_threads must be 0, 64, 128 or 256");
     if (t->tangent_ctas_per_sm < 0 || t->tangent_ctas_per_sm > 4)
       throw Error(CGB_ERR_INVALID, "cgb_assembler_set_tuning: tangent_ctas_per_sm must be 0..4");
+    if (t->tangent_kind != CGB_TANGENT_TENSOR && t->tangent_kind != CGB_TANGENT_CORES)
+      throw Error(CGB_ERR_INVALID, "cgb_assembler_set_tuning: tangent_kind must be CGB_TANGENT_TENSOR or CGB_TANGENT_CORES");
     a->tuning = *t;
   });
 }

@@ -39,12 +39,21 @@ void bind_device(cgb_context* ctx) { CGB_CUDA(cudaSetDevice(ctx->device)); }
 
 // The device error word after an assembly: a bounded wait of the tangent's staging
 // copies gave up (the kernel left its remaining groups undone). Cleared once reported.
+// Bit 8: an index in the caller-owned arrays of cgb_assemble_face_noalloc was out of range
+// (the access was skipped). Bit 16: the tensor-core tangent gave up waiting for an MMA.
 void check_device_word(cgb_context* ctx, int word) {
-  if (word & 4) {
+  if (word & (4 | 8 | 16)) {
     CGB_CUDA(cudaMemsetAsync(ctx->dev_err.p, 0, sizeof(int), ctx->stream));
     CGB_CUDA(cudaStreamSynchronize(ctx->stream));
-    throw Error(CGB_ERR_DEVICE, "assemble: a bulk copy of the tangent's neighbour data did not complete; "
-                                "K is incomplete");
+    if (word & 4)
+      throw Error(CGB_ERR_DEVICE, "assemble: a bulk copy of the tangent's neighbour data did not complete; "
+                                  "K is incomplete");
+    if (word & 16)
+      throw Error(CGB_ERR_DEVICE, "assemble: a tensor-core product of the tangent did not complete in time; "
+                                  "K is incomplete");
+    throw Error(CGB_ERR_DEVICE, "cgb_assemble_face_noalloc: an index in the caller's arrays was out of range "
+                                "(a neighbour count above max_neighbours, a node id outside [0, n_nodes), or a "
+                                "block beyond nnz); K and F are incomplete");
   }
 }
 
@@ -177,6 +186,17 @@ void ctx_release(cgb_context* ctx) {
 }
 }  // namespace cgb
 
+namespace cgb {
+const double* natcurv_points(const cgb_context* ctx, const cgb_shape* S, const char* what) {
+  if (!ctx->natcurv.active) return nullptr;
+  if (S->n_gp == 0) return nullptr;
+  if (!S->has_xy || S->gp_xy.n < 2 * static_cast<size_t>(S->n_gp))
+    throw Error(CGB_ERR_INVALID, std::string(what) + ": natural curvature needs the points' reference coordinates "
+                                                     "(a shape set made by cgb_shape_build)");
+  return S->gp_xy.p;
+}
+}  // namespace cgb
+
 extern "C" {
 
 const char* cgb_last_error(const cgb_context* ctx) {
@@ -201,6 +221,23 @@ int cgb_synchronize(cgb_context* ctx) {
     CGB_CUDA(cudaMemcpyAsync(&dev_err, ctx->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CGB_CUDA(cudaStreamSynchronize(ctx->stream));
     check_device_word(ctx, dev_err);
+  });
+}
+
+int cgb_set_natural_curvature(cgb_context* ctx, const cgb_natural_curvature* nc) {
+  if (!ctx) return CGB_ERR_INVALID;
+  return guarded(ctx, [&] {
+    cgb::NatCurv v;
+    if (nc && nc->active) {
+      // main.cpp:83-95: the band's width must be positive, sense mountain (-1) or valley (+1).
+      need(nc->width > 0.0, "natural_curvature.width must be > 0");
+      need(nc->sign == -1.0 || nc->sign == 1.0, "natural_curvature.sense must be mountain or valley");
+      v.active = 1;
+      v.x0 = nc->x0;
+      v.width = nc->width;
+      v.amp = nc->sign * nc->theta0 / (1.7724538509055160273 * nc->width);   // sign theta0 / (sqrt(pi) w)
+    }
+    ctx->natcurv = v;
   });
 }
 
@@ -506,6 +543,19 @@ int cgb_assembler_stats(cgb_assembler* a, int64_t out[4]) {
     out[1] = a->n_blocks;
     out[2] = a->mrg_n_ent;
     out[3] = a->mrg_n_direct;
+  });
+}
+
+int cgb_assembler_tensor_stats(cgb_assembler* a, int64_t out[4]) {
+  if (!a) return CGB_ERR_INVALID;
+  return guarded(a->ctx, [&] {
+    need(out != nullptr, "cgb_assembler_tensor_stats: out is NULL");
+    bind_device(a->ctx);
+    cgb::tc_prepare(a);
+    out[0] = a->tc_n_groups;
+    out[1] = static_cast<int64_t>(a->tc_fallback_h.size());
+    out[2] = a->tc_point_cols;
+    out[3] = 0;
   });
 }
 

@@ -67,6 +67,13 @@ struct Crease {
   int extend_start = 0, extend_end = 0, is_closed = 0;
 };
 
+// Kinematics::NaturalCurvature (plate/Kinematics.h:21-45) as the kernels take it: the band's
+// kappa_bar_XX(X) = amp * exp(-((X - x0) / width)^2), amp = sign * theta0 / (sqrt(pi) width).
+struct NatCurv {
+  int active = 0;
+  double x0 = 0.0, width = 1.0, amp = 0.0;
+};
+
 }  // namespace cgb
 
 // Opaque handles of the C ABI.
@@ -84,6 +91,7 @@ struct cgb_context {
   std::vector<double> h_node_xy;
   cgb::DevBuf<double> node_xy;
   uint64_t node_gen = 0;  // bumped whenever cgb_set_nodes changes the coordinates
+  cgb::NatCurv natcurv;   // natural curvature of every constitutive evaluation (inactive by default)
   // Device-side error word written by kernels (bounds checks, capacity).
   cgb::DevBuf<int> dev_err;
   int* h_err = nullptr;  // pinned mirror
@@ -102,6 +110,7 @@ struct cgb_shape {
   int64_t nnz = 0;
   int max_n = 0;  // largest neighbour count of the set
   cgb::DevBuf<double> gp_xy;      // 2 per point
+  bool has_xy = false;            // gp_xy holds the points' reference coordinates
   cgb::DevBuf<int64_t> nbr_ptr;   // n_gp + 1
   cgb::DevBuf<int32_t> nbr_idx;   // nnz
   cgb::DevBuf<double> s;          // nnz (normalised distance), may be empty
@@ -184,6 +193,18 @@ struct cgb_assembler {
   cgb::DevBuf<int32_t> mrg_ent_cstart;// (count << 16) | first contribution within its group
   cgb::DevBuf<int8_t> mrg_direct;     // 1: group too large, scatter directly
   cgb::DevBuf<uint16_t> mrg_code;     // per pair: point | i | j, grouped by entry
+  // Tensor-core tangent: per face entry the index of its node in its group's sorted node
+  // union, per group the union's size, per merged entry the union indices of its block's
+  // row and column nodes, and the groups the tensor path does not take (union above 42
+  // nodes, or too large to merge) on the device and on the host.
+  bool tc_ready = false;
+  cgb::DevBuf<uint8_t> tc_nbr_u;
+  cgb::DevBuf<int16_t> tc_cell_U;
+  cgb::DevBuf<uint16_t> tc_ent_uv;
+  cgb::DevBuf<int32_t> tc_fallback;
+  std::vector<int32_t> tc_fallback_h;
+  int64_t tc_n_groups = 0;            // groups on the tensor path
+  int64_t tc_point_cols = 0;          // sum over them of points x MMA columns (N)
   cgb_tuning tuning{};                // launch shape (0 = library default)
   cgb::DevBuf<int> work_ctr;          // per-chunk work counters of the residual kernel
   uint32_t test_stage_extra_tx = 0;   // failure-detection test only: bytes the staging never gets
@@ -247,6 +268,9 @@ void shape_concat(cgb_context* ctx, const cgb_shape* const* sets, const int32_t*
 void deterministic_pair_lists(cgb_assembler* a);
 void deterministic_entry_lists(cgb_assembler* a);
 void merge_prepare(cgb_assembler* a);
+// The tensor-core tangent's tables (needs merge_prepare; made once per assembler).
+constexpr int kTcMaxUnion = 42;
+void tc_prepare(cgb_assembler* a);
 // assemble.cu
 void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d_F, int flags);
 // Re-derive the assembler's copies of the face shape derivatives after a rebuild of the
@@ -256,6 +280,11 @@ void energies_device(cgb_assembler* a, const double* d_x, double* out3);
 // Kinematic state rows (CGB_POINT_STATE_COLS per point) of a shape set at device x.
 void point_state_device(cgb_context* ctx, const cgb_shape* S, const double* d_x, const double* A, const double* B,
                         const double* D, double* d_out);
+// The shape set's point coordinates when the context's natural curvature is active (the
+// kernels evaluate kappa_bar at each point's X), else null; refuses a set without them.
+const double* natcurv_points(const cgb_context* ctx, const cgb_shape* S, const char* what);
+// err: the context's device error word (bit 8: an index of the caller's arrays was out of
+// range and the access was skipped).
 void face_mixed_on_arrays(const cgb_face_problem& pr, const double* d_x, double* d_K, double* d_F,
-                          float* kacc, cudaStream_t st);
+                          float* kacc, int* err, cudaStream_t st);
 }  // namespace cgb

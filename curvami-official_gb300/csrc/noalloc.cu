@@ -23,7 +23,8 @@ static __device__ __align__(256) float g_block_scratch[kScratchFloats];
 
 // Device address of g_block_scratch per device ordinal, looked up once per device. In
 // host code the array's name is only a host-side stand-in, so the kernels get this
-// address, never &g_block_scratch.
+// address, never &g_block_scratch. The address is kept for the life of the process:
+// resetting a device (cudaDeviceReset) while the library is loaded is not supported.
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 float* g_scratch_addr[kMaxDevices] = {nullptr};
@@ -54,6 +55,7 @@ extern "C" int cgb_assemble_face_noalloc(cgb_context* ctx, const cgb_face_proble
     const cgb_face_problem& pr = *prob;
     if (pr.n_gp < 0 || pr.n_nodes <= 0 || pr.nnz < 0 || pr.nnz % 9 != 0 || pr.max_neighbours < 0)
       throw cgb::Error(CGB_ERR_INVALID, "cgb_assemble_face_noalloc: inconsistent sizes");
+    // Without face points K and F are zero and no input array is read.
     if (pr.n_gp > 0 && (!pr.nbr_ptr || !pr.nbr_idx || !pr.dpsi || !pr.ddpsi || !pr.weight || !pr.map_ptr ||
                         !pr.csr_map || !pr.outer))
       throw cgb::Error(CGB_ERR_INVALID, "cgb_assemble_face_noalloc: NULL input array");
@@ -67,9 +69,12 @@ extern "C" int cgb_assemble_face_noalloc(cgb_context* ctx, const cgb_face_proble
     if (4 * ((32 * 32 + 32 * static_cast<size_t>(pr.max_neighbours)) * sizeof(float) +
              static_cast<size_t>(pr.max_neighbours) * sizeof(int)) > 200 * 1024)
       throw cgb::Error(CGB_ERR_CAPACITY, "cgb_assemble_face_noalloc: too many neighbours per Gauss point");
+    if (ctx->natcurv.active)
+      throw cgb::Error(CGB_ERR_INVALID, "cgb_assemble_face_noalloc: natural curvature needs the Gauss points' "
+                                        "coordinates, which this entry point does not take; use cgb_assemble_device");
     CGB_CUDA(cudaSetDevice(ctx->device));
     float* scratch = scratch_for_current_device();
-    cgb::face_mixed_on_arrays(pr, d_x, d_K, d_F, scratch, ctx->stream);
+    cgb::face_mixed_on_arrays(pr, d_x, d_K, d_F, scratch, ctx->dev_err.p, ctx->stream);
     ctx->last_error.clear();
     return CGB_OK;
   } catch (const cgb::Error& e) {

@@ -468,6 +468,116 @@ void pattern_build(cgb_assembler* a) {
   CGB_CUDA(cudaStreamSynchronize(st));
 }
 
+// ---- tables of the tensor-core tangent --------------------------------------------------
+// One CTA per group of kMergeGroup points: the group's neighbour ids sorted and made unique
+// (the group's node union, ascending ids), every face entry's index in it, the union's size,
+// and for every merged entry (from its first contribution code, written row node first) the
+// union indices of the block's row and column nodes. Groups with more than kTcItems entries
+// get the size 32767 (not on the tensor path).
+constexpr int kTcItems = 1024;
+
+__global__ void __launch_bounds__(128) tc_cells_kernel(int n_gp, const int64_t* __restrict__ ptr,
+                                                       const int32_t* __restrict__ idx,
+                                                       const int64_t* __restrict__ map_ptr,
+                                                       const int64_t* __restrict__ ent_ptr,
+                                                       const int32_t* __restrict__ ent_cstart,
+                                                       const uint16_t* __restrict__ code, uint8_t* __restrict__ nbr_u,
+                                                       int16_t* __restrict__ cell_U, uint16_t* __restrict__ ent_uv) {
+  __shared__ int ids[kTcItems];
+  __shared__ int s_nu;
+  const int G = blockIdx.x, t = threadIdx.x;
+  const int g0 = G * kMergeGroup, g1 = min(n_gp, g0 + kMergeGroup);
+  const int64_t q0 = ptr[g0], q1 = ptr[g1];
+  const int items = static_cast<int>(q1 - q0);
+  if (items > kTcItems) {
+    for (int64_t e = q0 + t; e < q1; e += blockDim.x) nbr_u[e] = 255;
+    if (t == 0) cell_U[G] = 32767;
+    return;
+  }
+  int n2 = 1;
+  while (n2 < items) n2 <<= 1;
+  for (int i = t; i < n2; i += blockDim.x) ids[i] = i < items ? idx[q0 + i] : 0x7fffffff;
+  __syncthreads();
+  for (int k = 2; k <= n2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = t; i < n2; i += blockDim.x) {
+        const int u = i ^ j;
+        if (u > i) {
+          const bool up = (i & k) == 0;
+          const int x = ids[i], y = ids[u];
+          if ((x > y) == up) { ids[i] = y; ids[u] = x; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (t == 0) {  // unique, in place (items <= 1024)
+    int m = 0;
+    for (int i = 0; i < items; ++i)
+      if (m == 0 || ids[i] != ids[m - 1]) ids[m++] = ids[i];
+    s_nu = m;
+  }
+  __syncthreads();
+  const int U = s_nu;
+  if (t == 0) cell_U[G] = static_cast<int16_t>(U);
+  auto find = [&](int node) {
+    int lo = 0, hi = U;  // first position with ids[pos] >= node
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (ids[mid] < node) lo = mid + 1; else hi = mid;
+    }
+    return lo < 255 ? lo : 255;
+  };
+  for (int64_t e = q0 + t; e < q1; e += blockDim.x) nbr_u[e] = static_cast<uint8_t>(find(idx[e]));
+  const int64_t e0 = ent_ptr[G], e1 = ent_ptr[G + 1];
+  const int64_t cbase = map_ptr[g0];
+  for (int64_t e = e0 + t; e < e1; e += blockDim.x) {
+    const unsigned cd = code[cbase + (ent_cstart[e] & 0xffff)];
+    const int k = cd >> 12, i = (cd >> 6) & 63, j = cd & 63;
+    const int64_t p0 = ptr[g0 + k];
+    ent_uv[e] = static_cast<uint16_t>(find(idx[p0 + i]) | (find(idx[p0 + j]) << 8));
+  }
+}
+
+void tc_prepare(cgb_assembler* a) {
+  if (a->tc_ready) return;
+  merge_prepare(a);
+  cudaStream_t st = a->ctx->stream;
+  const cgb_shape* S = a->faces;
+  const int n_gp = S->n_gp;
+  const int ng = (n_gp + kMergeGroup - 1) / kMergeGroup;
+  a->tc_nbr_u.alloc(std::max<int64_t>(S->nnz, 1));
+  a->tc_cell_U.alloc(std::max(ng, 1));
+  a->tc_ent_uv.alloc(std::max<int64_t>(a->mrg_n_ent, 1));
+  if (ng > 0)
+    tc_cells_kernel<<<ng, 128, 0, st>>>(n_gp, S->nbr_ptr.p, S->nbr_idx.p, a->map_ptr.p, a->mrg_ent_ptr.p,
+                                        a->mrg_ent_cstart.p, a->mrg_code.p, a->tc_nbr_u.p, a->tc_cell_U.p,
+                                        a->tc_ent_uv.p);
+  CGB_CUDA(cudaGetLastError());
+  std::vector<int16_t> cu(std::max(ng, 1));
+  std::vector<int8_t> direct(std::max(ng, 1));
+  if (ng > 0) {
+    CGB_CUDA(cudaMemcpyAsync(cu.data(), a->tc_cell_U.p, ng * sizeof(int16_t), cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaMemcpyAsync(direct.data(), a->mrg_direct.p, ng * sizeof(int8_t), cudaMemcpyDeviceToHost, st));
+  }
+  CGB_CUDA(cudaStreamSynchronize(st));
+  a->tc_fallback_h.clear();
+  a->tc_n_groups = 0;
+  a->tc_point_cols = 0;
+  for (int G = 0; G < ng; ++G) {
+    if (direct[G] || cu[G] > kTcMaxUnion) {
+      a->tc_fallback_h.push_back(G);
+    } else {
+      const int n_cols = std::max(16, (3 * cu[G] + 15) & ~15);
+      ++a->tc_n_groups;
+      a->tc_point_cols += static_cast<int64_t>(std::min(kMergeGroup, n_gp - G * kMergeGroup)) * n_cols;
+    }
+  }
+  upload(a->tc_fallback, a->tc_fallback_h.data(), a->tc_fallback_h.size(), st);
+  CGB_CUDA(cudaStreamSynchronize(st));
+  a->tc_ready = true;
+}
+
 void merge_prepare(cgb_assembler* a) {
   if (a->mrg_ready) return;
   cudaStream_t st = a->ctx->stream;

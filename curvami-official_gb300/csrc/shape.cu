@@ -500,9 +500,14 @@ __global__ void __launch_bounds__(kThreads) rkpm_kernel(RkpmArgs a) {
   if (g >= a.n_gp) return;
   const int64_t p0 = a.ptr[g], p1 = a.ptr[g + 1];
   const double gx = a.gp_xy[2 * g], gy = a.gp_xy[2 * g + 1];
-  double gind[6 * 4];
-  const int nc = a.n_creases < 4 ? a.n_creases : 4;
-  for (int c = 0; c < 6 * nc; ++c) gind[c] = a.gind[static_cast<int64_t>(g) * 6 * a.n_creases + c];
+  // The point's crease indicators: a local copy for up to 4 creases, read in place beyond.
+  double gloc[6 * 4];
+  const int nc = a.n_creases;
+  const double* gind = a.gind + static_cast<int64_t>(g) * 6 * nc;
+  if (nc <= 4) {
+    for (int c = 0; c < 6 * nc; ++c) gloc[c] = gind[c];
+    gind = gloc;
+  }
 
   // Raw-moment sums S^g_ab of the six weight jets (see point_solve). Accumulating the
   // 6 x NR sums per neighbour (90 FMA for ORDER 2) replaces the 6 x NM jets of p_i p_j
@@ -731,7 +736,8 @@ struct PairPoint {
   float gx0, gx1, gx2, gy0, gy1, gy2;
   int nc;
   bool scaled;
-  fp2 gc[6 * 4];
+  fp2 gc[6 * 4];    // scaled crease indicators, up to 4 creases
+  const fp2* gcp;   // gc, or the point record's copy when there are more creases
 };
 
 __device__ __forceinline__ void pair_xi(const RkpmArgs& a, const PairPoint& P, int j, fp2& xi, fp2& eta, fp2& fac) {
@@ -757,7 +763,7 @@ __device__ __forceinline__ void pair_moment_sums(const RkpmArgs& a, const PairPo
     const int j = a.idx[e];
     fp2 xi, eta, fac;
     pair_xi(a, P, j, xi, eta, fac);
-    const JetsP J = weight_jets_pair(a.kernel, xi, eta, fac, P.scaled, P.nc, P.gc, a.node_side, a.n_nodes, j);
+    const JetsP J = weight_jets_pair(a.kernel, xi, eta, fac, P.scaled, P.nc, P.gcp, a.node_side, a.n_nodes, j);
     fp2 xp[RI::D + 1], yp[RI::D + 1];
     xp[0] = fp2{1.0f, 0.0f}; yp[0] = fp2{1.0f, 0.0f};
 #pragma unroll
@@ -816,18 +822,23 @@ __global__ void __launch_bounds__(kThreads, kPairMinBlocks) rkpm_pair_point_kern
   PairPoint P;
   split3(a.gp_xy[2 * g], P.gx0, P.gx1, P.gx2);
   split3(a.gp_xy[2 * g + 1], P.gy0, P.gy1, P.gy2);
-  P.nc = a.n_creases < 4 ? a.n_creases : 4;
+  P.nc = a.n_creases;
   P.scaled = a.rho_node != nullptr;
   const double r1 = 0.5 * a.rho, r2 = 0.5 * a.rho * a.rho;
+  float* out = rec + static_cast<int64_t>(g) * RS;
+  // The scaled indicators go to the point record first; with more than 4 creases the
+  // moment sums read them back from there (this thread's own writes).
   for (int c = 0; c < P.nc; ++c) {
     const double* I = a.gind + (static_cast<int64_t>(g) * a.n_creases + c) * 6;
-    P.gc[6 * c + 0] = fp2_from_double(0.5 * I[0]);
-    P.gc[6 * c + 1] = fp2_from_double(r1 * I[1]);
-    P.gc[6 * c + 2] = fp2_from_double(r1 * I[2]);
-    P.gc[6 * c + 3] = fp2_from_double(r2 * I[3]);
-    P.gc[6 * c + 4] = fp2_from_double(r2 * I[4]);
-    P.gc[6 * c + 5] = fp2_from_double(r2 * I[5]);
+    const fp2 v[6] = {fp2_from_double(0.5 * I[0]), fp2_from_double(r1 * I[1]), fp2_from_double(r1 * I[2]),
+                      fp2_from_double(r2 * I[3]), fp2_from_double(r2 * I[4]), fp2_from_double(r2 * I[5])};
+    for (int q = 0; q < 6; ++q) {
+      if (c < 4) P.gc[6 * c + q] = v[q];
+      out[6 + 2 * (6 * c + q)] = v[q].hi;
+      out[7 + 2 * (6 * c + q)] = v[q].lo;
+    }
   }
+  P.gcp = P.nc <= 4 ? P.gc : reinterpret_cast<const fp2*>(out + 6);
   double Sd[6][RI::NR];
   if constexpr (ORDER < kPairSplitOrder) {
     pair_moment_sums<ORDER, 0, 6>(a, P, p0, p1, Sd);
@@ -837,13 +848,8 @@ __global__ void __launch_bounds__(kThreads, kPairMinBlocks) rkpm_pair_point_kern
   }
   RowJets<ORDER> R;
   a.bad[g] = static_cast<int8_t>(point_solve<ORDER>(Sd[0], Sd[1], Sd[2], Sd[3], Sd[4], Sd[5], R));
-  float* out = rec + static_cast<int64_t>(g) * RS;
   out[0] = P.gx0; out[1] = P.gx1; out[2] = P.gx2;
   out[3] = P.gy0; out[4] = P.gy1; out[5] = P.gy2;
-  for (int c = 0; c < 6 * P.nc; ++c) {
-    out[6 + 2 * c] = P.gc[c].hi;
-    out[7 + 2 * c] = P.gc[c].lo;
-  }
   float2* cj = reinterpret_cast<float2*>(out + 6 + 12 * P.nc);
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
@@ -880,7 +886,7 @@ __global__ void __launch_bounds__(kPairValueThreads) rkpm_pair_value_kernel(Rkpm
   int g = g0;
   while (__ldg(a.ptr + g + 1) <= e) ++g;
   const float* R = rec + static_cast<int64_t>(g) * RS;
-  const int nc = a.n_creases < 4 ? a.n_creases : 4;
+  const int nc = a.n_creases;
   const fp2* gc = reinterpret_cast<const fp2*>(R + 6);
   const fp2* cj = reinterpret_cast<const fp2*>(R + 6 + 12 * nc);
   const int j = a.idx[e];
@@ -938,7 +944,6 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
   if (prm.order < 1 || prm.order > 3)
     throw Error(CGB_ERR_INVALID, "cgb_shape_build: order must be 1, 2 or 3");
   if (!(prm.rho > 0.0)) throw Error(CGB_ERR_INVALID, "cgb_shape_build: rho must be > 0");
-  if (creases.size() > 4) throw Error(CGB_ERR_CAPACITY, "cgb_shape_build: at most 4 creases per call");
   out->ctx = ctx;
   out->n_gp = n_gp;
   out->rho = prm.rho;
@@ -995,6 +1000,7 @@ void shape_build(cgb_context* ctx, const double* gp_xy, int n_gp, const cgb_shap
   GridDev G{minx, miny, cell, cols, ncells, d_cstart.p, d_cnodes.p};
 
   upload(out->gp_xy, gp_xy, 2 * static_cast<size_t>(n_gp), st);
+  out->has_xy = true;
   const double rho2 = prm.rho * prm.rho;
   // The FP32 pre-test (FrnnPre): float coordinates relative to (minx, miny) and the margin.
   // e = 2^-23 X (X the largest relative coordinate) bounds the rounding of one coordinate
@@ -1083,7 +1089,6 @@ void shape_values(cgb_context* ctx, cgb_shape* out, const std::vector<Crease>& c
   const int n_nodes = ctx->n_nodes;
   const int n_gp = out->n_gp;
   const int64_t nnz = out->nnz;
-  if (creases.size() > 4) throw Error(CGB_ERR_CAPACITY, "cgb_shape_build: at most 4 creases per call");
   const int nc = static_cast<int>(creases.size());
   std::vector<double> all_xy;
   std::vector<size_t> off(nc + 1, 0);

@@ -7,7 +7,7 @@ hand-written CUDA kernels in ``libcurvami_gb300.so`` behind the C ABI of
 interface over that ABI (ctypes). There is no CPU fallback.
 """
 from ._lib import (CGBError, DETERMINISTIC, HINGE, HINGE_EXACT, MIXED, TANGENT,  # noqa: F401
-                   load_library, LIB_PATH)
+                   TANGENT_CORES, TANGENT_TENSOR, load_library, LIB_PATH)
 from .api import (AssemblyGraph, Context, NonLinearAssembler, PlateBatch, PlateModel, ShapeSet,  # noqa: F401
                   abd_isotropic, abd_laminate, concat_shapes, shape_from_host, shape_functions)
 from . import synth  # noqa: F401

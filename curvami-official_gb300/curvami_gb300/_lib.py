@@ -35,6 +35,7 @@ SIGNATURES = {
     "cgb_set_stream": (i32, [vp, vp]),
     "cgb_synchronize": (i32, [vp]),
     "cgb_set_nodes": (i32, [vp, vp, i32]),
+    "cgb_set_natural_curvature": (i32, [vp, vp]),
     "cgb_shape_build": (i32, [vp, vp, i32, vp, vp, i32, C.POINTER(vp)]),
     "cgb_shape_rebuild": (i32, [vp, vp, i32]),
     "cgb_shape_from_host": (i32, [vp, i32, vp, vp, vp, vp, vp, C.POINTER(vp)]),
@@ -48,6 +49,7 @@ SIGNATURES = {
     "cgb_assembler_download_pattern": (i32, [vp, vp, vp]),
     "cgb_assembler_download_map": (i32, [vp, vp, i64]),
     "cgb_assembler_stats": (i32, [vp, vp]),
+    "cgb_assembler_tensor_stats": (i32, [vp, vp]),
     "cgb_shape_concat": (i32, [vp, vp, vp, i32, vp]),
     "cgb_assembler_set_tuning": (i32, [vp, vp]),
     "cgb_graph_create": (i32, [vp, vp, vp, vp, i32, vp]),
@@ -78,8 +80,19 @@ class ShapeParams(C.Structure):
     _fields_ = [("rho", dbl), ("rho_node", vp), ("order", i32), ("kernel", i32), ("precision", i32)]
 
 
+TANGENT_TENSOR = 0
+TANGENT_CORES = 1
+
+
+class NaturalCurvature(C.Structure):
+    """cgb_natural_curvature: the band of Kinematics::NaturalCurvature (theta0 in radians,
+    sign -1 mountain / +1 valley)."""
+    _fields_ = [("active", i32), ("x0", dbl), ("width", dbl), ("theta0", dbl), ("sign", dbl)]
+
+
 class Tuning(C.Structure):
-    _fields_ = [("n_chunks", i32), ("residual_threads", i32), ("tangent_ctas_per_sm", i32)]
+    _fields_ = [("n_chunks", i32), ("residual_threads", i32), ("tangent_ctas_per_sm", i32),
+                ("tangent_kind", i32)]
 
 
 class Fold(C.Structure):

@@ -51,6 +51,23 @@ class Context:
     def synchronize(self):
         self.check(self.lib.cgb_synchronize(self.h))
 
+    def set_natural_curvature(self, nc=None):
+        """Kinematics::naturalCurvature() for every constitutive evaluation of this context
+        (cgb_set_natural_curvature): nc is the config's "natural_curvature" object
+        (main.cpp:83-95: {"x0", "width", "angle_deg", "sense": "mountain" | "valley"}), or
+        None to switch it off."""
+        v = L.NaturalCurvature()
+        if nc is not None:
+            sense = nc.get("sense", "mountain")
+            if sense not in ("mountain", "valley"):
+                raise ValueError("natural_curvature.sense must be mountain or valley")
+            v.active = 1
+            v.x0, v.width = float(nc["x0"]), float(nc["width"])
+            v.theta0 = float(nc["angle_deg"]) * np.pi / 180.0
+            v.sign = -1.0 if sense == "mountain" else 1.0
+        self.check(self.lib.cgb_set_natural_curvature(self.h, C.byref(v)))
+        self.natural_curvature = None if nc is None else dict(nc)
+
     def set_stream(self, stream_ptr: int):
         """Launch on the caller's cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
         self.check(self.lib.cgb_set_stream(self.h, C.c_void_p(stream_ptr)))
@@ -245,6 +262,14 @@ class NonLinearAssembler:
         self.ctx.check(self.ctx.lib.cgb_assembler_stats(self.h, _p(out)))
         return dict(zip(("pairs", "blocks", "entries", "direct_groups"), (int(v) for v in out)))
 
+    def tensor_stats(self):
+        """{"tensor_groups", "core_groups", "point_cols"}: the tensor-core tangent's share
+        (groups of 16 points as one tensor-core product, groups left to the CUDA cores, and
+        the sum of points x MMA columns, i.e. 10,240 x point_cols TF32 flops per assembly)."""
+        out = np.zeros(4, np.int64)
+        self.ctx.check(self.ctx.lib.cgb_assembler_tensor_stats(self.h, _p(out)))
+        return dict(zip(("tensor_groups", "core_groups", "point_cols"), (int(v) for v in out[:3])))
+
     def csr_mapping(self):
         n = np.diff(self.faces.download()["ptr"])
         total = int((n * (n + 1) // 2).sum())
@@ -268,11 +293,12 @@ class NonLinearAssembler:
                                                         C.c_void_p(d_K) if d_K else None,
                                                         C.c_void_p(d_F), int(flags)))
 
-    def set_tuning(self, n_chunks=0, residual_threads=0, tangent_ctas_per_sm=0):
-        """cgb_assembler_set_tuning (0 = the library's default)."""
-        t = L.Tuning(int(n_chunks), int(residual_threads), int(tangent_ctas_per_sm))
+    def set_tuning(self, n_chunks=0, residual_threads=0, tangent_ctas_per_sm=0, tangent_kind=0):
+        """cgb_assembler_set_tuning (0 = the library's default; tangent_kind 0 the tensor-core
+        tangent, 1 the CUDA-core one)."""
+        t = L.Tuning(int(n_chunks), int(residual_threads), int(tangent_ctas_per_sm), int(tangent_kind))
         self.ctx.check(self.ctx.lib.cgb_assembler_set_tuning(self.h, C.byref(t)))
-        self.tuning = (int(n_chunks), int(residual_threads), int(tangent_ctas_per_sm))
+        self.tuning = (int(n_chunks), int(residual_threads), int(tangent_ctas_per_sm), int(tangent_kind))
 
     def graph(self, d_x: int, d_K: int | None, d_F: int, flags) -> "AssemblyGraph":
         """One cgb_assemble_device call on these device buffers captured as a CUDA graph."""

@@ -1,8 +1,9 @@
 """Autotuner for the assembly's launch shape (cgb_assembler_set_tuning).
 
-The knobs: the number of Gauss-point chunks whose FP64 residual and FP32 tangent kernels
-overlap on two streams, the residual kernel's block size, and the resident CTAs per SM of
-the merged tangent. The best setting depends on the problem's size and neighbour counts
+The knobs: the number of Gauss-point chunks whose FP64 residual and FP32-class tangent
+kernels overlap on two streams, the residual kernel's block size, the resident CTAs per SM
+of the CUDA-core merged tangent, and which tangent forms the cells (tensor cores or CUDA
+cores). The best setting depends on the problem's size and neighbour counts
 (a batch of small plates wants fewer, larger chunks than one big plate). ``autotune``
 times every candidate on the caller's own problem and device buffers, keeps the fastest,
 and caches it in a JSON file keyed by the device, the problem's size and the flags, so a
@@ -21,6 +22,7 @@ DEFAULT_CANDIDATES = {
     "n_chunks": (1, 2, 4, 8, 16),
     "residual_threads": (128, 256),
     "tangent_ctas_per_sm": (0, 2),
+    "tangent_kind": (0,),
 }
 
 
@@ -69,7 +71,7 @@ def autotune(asm, d_x: int, d_K: int | None, d_F: int, flags: int, device_name: 
              candidates=None, cache_path: str | None = None, repeats: int = 5, force: bool = False) -> dict:
     """Pick the fastest launch shape for this assembler and flags on the given device
     buffers (x already holding a representative state), apply it, and return
-    {"tuning": (n_chunks, residual_threads, tangent_ctas_per_sm), "ms": ..., "cached": bool,
+    {"tuning": (n_chunks, residual_threads, tangent_ctas_per_sm, tangent_kind), "ms": ..., "cached": bool,
     "tried": {...}}."""
     path = cache_path or default_cache_path()
     key = problem_key(asm, flags, device_name)
@@ -80,7 +82,8 @@ def autotune(asm, d_x: int, d_K: int | None, d_F: int, flags: int, device_name: 
         return {"tuning": t, "ms": cache[key]["ms"], "cached": True, "key": key, "tried": {}}
     cand = candidates or DEFAULT_CANDIDATES
     tried = {}
-    for t in itertools.product(cand["n_chunks"], cand["residual_threads"], cand["tangent_ctas_per_sm"]):
+    for t in itertools.product(cand["n_chunks"], cand["residual_threads"], cand["tangent_ctas_per_sm"],
+                               cand.get("tangent_kind", (0,))):
         asm.set_tuning(*t)
         tried[t] = _time(asm, d_x, d_K, d_F, flags, repeats) * 1e3
     best = min(tried, key=tried.get)

@@ -561,6 +561,11 @@ class ContinuationSolver:
         self.last_ls_iters = 0
         self.last_ls_attempts = 0
         self.history = []   # (iteration, merit, energy change, geometry error, alpha)
+        # Per iteration of the last line_search, its decisions, for comparing runs: a dict with
+        # the iteration j, the merit (max projected force), the energy change and geometry
+        # error its convergence test saw, whether it converged there, and the halvings tried
+        # as (alpha, trial merit).
+        self.ls_trace = []
 
     def initialize_topology(self, J):
         """Independent rows of J: column-pivoted QR of J^T, |R_ii| above
@@ -606,6 +611,7 @@ class ContinuationSolver:
         d0 = d.copy()
         self.last_ls_iters = -1
         self.history = []
+        self.ls_trace = []
         c_all, J_all = prob.constraints(d)
         self.initialize_topology(J_all)
         nc = len(self.ind_rows)
@@ -622,6 +628,8 @@ class ContinuationSolver:
             if j > 1 and max_force <= self.tol_force and energy_change <= self.tol_energy and \
                     geom_error <= self.tol_geom:
                 self.last_ls_iters = j
+                self.ls_trace.append({"j": j, "merit": max_force, "energy_change": energy_change,
+                                      "geom_error": geom_error, "converged": True, "trials": []})
                 return True
             if max_force >= self.div or np.isnan(max_force):
                 d[:] = d0
@@ -656,11 +664,15 @@ class ContinuationSolver:
                     mu += corr[ns:]
             alpha, descended = 1.0, False
             d_trial = d
+            tried = []
+            self.ls_trace.append({"j": j, "merit": max_force, "energy_change": energy_change if j > 1 else None,
+                                  "geom_error": geom_error, "converged": False, "trials": tried})
             for iarm in range(1, 7):
                 d_trial = d + xb + alpha * dx
                 R_trial = prob.internal_force(d_trial) - lam * prob.external_force(d_trial)
                 c_t, J_t = prob.constraints(d_trial)
                 trial = float(np.abs(_Projector(self.filter_rows(J_t)).project(R_trial)).max())
+                tried.append((alpha, trial))
                 if trial <= 1.05 * max_force:
                     descended = True
                     break
@@ -695,19 +707,58 @@ def tracking_displacement(prob: PlateProblem, x) -> float:
     return float(X[:, 2].mean())
 
 
-def load_steps(solver: ContinuationSolver, prob: PlateProblem, lambdas, x0=None):
+def load_steps(solver: ContinuationSolver, prob: PlateProblem, lambdas, x0=None, traces=None):
     """Static load stepping: one LineSearch per load factor, each starting from the
     previous solution. Returns the converged states and the Newton iterations per step
-    (LineSearch's count: the converging check is iteration j, so j - 1 tangent solves)."""
+    (LineSearch's count: the converging check is iteration j, so j - 1 tangent solves).
+    traces: a list that receives each step's line-search trace (solver.ls_trace)."""
     x = np.zeros(prob.num_dofs()) if x0 is None else np.array(x0, np.float64)
     states, iters = [], []
     for lam in lambdas:
         ok = solver.line_search(prob, float(lam), x)
+        if traces is not None:
+            traces.append(list(solver.ls_trace))
         if not ok:
             raise RuntimeError(f"LineSearch failed to converge at load factor {lam}")
         states.append(x.copy())
         iters.append(solver.last_ls_iters)
     return states, iters
+
+
+def first_divergence(ref_traces, traces, tol_force=None, tol_energy=None):
+    """Where two runs' line-search decisions first differ, from their traces (ls_trace per
+    load step): the load step and Newton iteration, and
+    - for a halving one run accepted and the other rejected: its index and, per run, the
+      ratio trial / (1.05 merit) that decided it (<= 1 accepts);
+    - for a convergence test one run passed and the other failed: each run's merit and
+      energy change there, and their ratios to the tolerances when given.
+    None when every decision agrees."""
+    def conv_info(e):
+        out = {"merit": e["merit"], "energy_change": e["energy_change"]}
+        if tol_force:
+            out["merit_over_tol"] = e["merit"] / tol_force
+        if tol_energy and e["energy_change"] is not None:
+            out["energy_over_tol"] = e["energy_change"] / tol_energy
+        return out
+
+    for k, (ra, rb) in enumerate(zip(ref_traces, traces)):
+        for ea, eb in zip(ra, rb):
+            if ea["converged"] != eb["converged"]:
+                return {"step": k, "iteration": ea["j"], "kind": "convergence test",
+                        "ref": conv_info(ea), "run": conv_info(eb)}
+            if ea["converged"]:
+                break
+            ta, tb = ea["trials"], eb["trials"]
+            ma, mb = ea["merit"], eb["merit"]
+            for h in range(max(len(ta), len(tb))):
+                acc_a = h < len(ta) and ta[h][1] <= 1.05 * ma
+                acc_b = h < len(tb) and tb[h][1] <= 1.05 * mb
+                if h >= len(ta) or h >= len(tb) or acc_a != acc_b:
+                    ratio = lambda t, m: (t[h][1] / (1.05 * m)) if h < len(t) else None  # noqa: E731
+                    return {"step": k, "iteration": ea["j"], "kind": "halving", "halving": h,
+                            "ratio_ref": ratio(ta, ma), "ratio_run": ratio(tb, mb),
+                            "merit_rel_diff": abs(ma - mb) / abs(ma) if ma else None}
+    return None
 
 
 def gpu_problem(model, face_load=None, edges=(), mixed: bool = False, deterministic: bool = False,

@@ -443,6 +443,32 @@ def batched_plate(n_side: int, rng, h: float = 0.5, rule: int = 4, jitter: float
                                          "creases": len(creases), "split": nsplit})
 
 
+def many_cuts_plate(n_side: int = 61, n_cuts: int = 6, h: float = 0.5, rule: int = 3, jitter: float = 0.05,
+                    seed: int = 12) -> Plate:
+    """More creases than a plate usually carries (the reference loops over any number,
+    GlobalRKPM.h:86-112): n_cuts straight cuts parallel to y, half-way between node
+    columns and 8 columns apart; even-numbered cuts cross the plate, odd-numbered ones
+    start on the lower edge and stop at 60 % of the side, so their tips blend (Enrichment.h
+    tip terms). Quadratic basis, rho = 3h, quartic window."""
+    rng = np.random.default_rng(seed)
+    nodes = grid_nodes(n_side, n_side, h, jitter, rng)
+    faces = quad_gauss_points(nodes, n_side, n_side, rule)
+    hull = convex_hull(_hull_candidates(nodes))
+    side = (n_side - 1) * h
+    creases = []
+    for k in range(n_cuts):
+        x0 = (4 + 8 * k + 0.5) * h
+        if x0 > side - 3 * h:
+            break
+        top = side if k % 2 == 0 else 0.6 * side
+        nseg = max(4, int(math.ceil(top / h)))
+        verts = np.stack([np.full(nseg + 1, x0), np.linspace(0.0, top, nseg + 1)], axis=1)
+        creases.append(make_crease(verts, nodes, hull))
+    faces, nsplit = split_on_creases(faces, creases)
+    return Plate(name=f"cuts{len(creases)}", node_xy=nodes, faces=faces, creases=creases, folds=[], rho=3.0 * h,
+                 order=2, kernel=0, seed=seed, meta={"n_side": n_side, "h": h, "rule": rule, "split": nsplit})
+
+
 def config_batched(n_plates: int = 64, side_range=(21, 161), seed: int = 1004, rule: int = 4):
     """Batched uneven plates: n_plates independent plates with node sides drawn uniformly
     from side_range (the config's "21^2 to 161^2" read as the side), 1-3 non-crossing

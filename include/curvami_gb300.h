@@ -50,7 +50,8 @@ enum {
 /* ---- assembly flags ------------------------------------------------------------- */
 #define CGB_TANGENT 0x1       /* form K; without it only F (residual) is produced */
 #define CGB_HINGE 0x2         /* add elastic-hinge terms (the reference's flagRig == false) */
-#define CGB_MIXED 0x4         /* FP64 residual, FP32 tangent; default FP64 throughout */
+#define CGB_MIXED 0x4         /* FP64 residual, FP32-class tangent (3xTF32 tensor cores or FP32
+                                 CUDA cores, cgb_tuning.tangent_kind); default FP64 throughout */
 #define CGB_DETERMINISTIC 0x8 /* fixed-order segmented-reduction scatter; default atomics */
 #define CGB_HINGE_EXACT 0x10  /* hinge tangent with the dihedral Hessian (fold_exact_tangent) */
 
@@ -110,6 +111,24 @@ int cgb_synchronize(cgb_context* ctx);
 /* Reference node coordinates (Node::X_ref, core/include/curvami/MeshfreeData.h:7-14). */
 int cgb_set_nodes(cgb_context* ctx, const double* node_xy, int n_nodes);
 
+/* Natural curvature, Kinematics::NaturalCurvature (plate/Kinematics.h:21-45), set from the
+ * config's "natural_curvature" band (main.cpp:83-95): kappa_bar(X) = sign * theta0 * g(X) eX (x) eX,
+ * g(X) = exp(-((X - x0) / width)^2) / (sqrt(pi) width); sign -1 mountain, +1 valley. The
+ * elastic bending strain E1_el = E1 + kappa_bar (Kinematics.h:110-111) replaces E1 in the
+ * constitutive law (Constitutive.h:65) wherever this context evaluates it: the residual and
+ * the tangent's resultants of every assembly, the strain energies (Meshless.h:212) and the
+ * point state's N and M (its E1 columns stay the geometric curvature, as the exporter's).
+ * It needs each point's reference X: shape sets made by cgb_shape_build carry it; an
+ * assembly over a set made by cgb_shape_from_host is refused while it is active. Like the
+ * reference's single static field, one setting per context, applied from the next call
+ * (a graph captured earlier replays the setting it was captured with); active = 0 (or a
+ * NULL pointer) switches it off. */
+typedef struct {
+  int active;
+  double x0, width, theta0, sign;
+} cgb_natural_curvature;
+int cgb_set_natural_curvature(cgb_context* ctx, const cgb_natural_curvature* nc);
+
 /* ---- stage A: shape functions ---------------------------------------------------- */
 /* GlobalFRNN::execute + GlobalRKPM::solve for one set of Gauss points
  * (core/include/curvami/FRNN.h:23, core/include/curvami/GlobalRKPM.h:19), as called
@@ -167,6 +186,13 @@ int cgb_assembler_download_map(const cgb_assembler* a, int32_t* map, int64_t n_e
  * entries of the FP32 tangent (distinct blocks per group of 16 consecutive Gauss points),
  * out[3] groups too large to merge. The first call builds the merge tables. */
 int cgb_assembler_stats(cgb_assembler* a, int64_t out[4]);
+/* The tensor-core tangent's share of the work (no reference counterpart; for measurement):
+ * out[0] groups of 16 points formed as one tensor-core product, out[1] groups left to the
+ * CUDA cores (node union above 42 nodes, or too large to merge), out[2] the sum over the
+ * tensor groups of points x MMA columns N (each point is five 128 x N x 8 TF32 MMAs, so
+ * the tensor pipe executes 10,240 x out[2] flops per assembly), out[3] 0. The first call
+ * builds the tables. */
+int cgb_assembler_tensor_stats(cgb_assembler* a, int64_t out[4]);
 /* Fold::gp_theta0 and Fold::gp_active of fold `fold` (plate/PlateData.h:54-76), which
  * progressive creasing rewrites at every step (plate/ProgressiveCreasing.h:621-639):
  * theta0_gp NULL = every point at the scalar theta0, active NULL = every point active.
@@ -226,7 +252,16 @@ int cgb_point_state_device(cgb_context* ctx, const cgb_shape* pts, const double*
  * Every call shares the one array: calls whose executions overlap on the GPU (other
  * streams, other contexts of the process on the same device) race and corrupt each
  * other's K, so serialise them. All pointers in prob and the x / K / F arguments are
- * device pointers; the call is asynchronous on ctx's stream. */
+ * device pointers; the call is asynchronous on ctx's stream. The address of the array
+ * is kept per device for the life of the process, so a device reset (cudaDeviceReset)
+ * while the library is loaded is not supported.
+ * With n_gp == 0 no input array is read (they may be NULL) and K and F are set to zero.
+ * The sizes must describe the arrays: nnz == outer[3 n_nodes] and max_neighbours >= every
+ * neighbour count. The kernels check the indices that reach the library's array or its
+ * shared-memory staging (a point with more than max_neighbours neighbours, a node id
+ * outside [0, n_nodes), a block beyond nnz / 9): such an access is skipped and the next
+ * cgb_synchronize returns CGB_ERR_DEVICE. Other inconsistencies between the arrays (a
+ * map_ptr or csr_map that does not match nbr_ptr) are undefined behaviour. */
 #define CGB_NOALLOC_MAX_BLOCKS 699050
 typedef struct {
   int n_gp;                /* face Gauss points */
@@ -259,11 +294,18 @@ int cgb_shape_concat(cgb_context* ctx, const cgb_shape* const* sets, const int32
  * chunks whose residual and tangent kernels overlap on two streams (default 4 from 65,536
  * points, else 1); residual_threads (64, 128, 256): block size of the residual kernel
  * (default 256); tangent_ctas_per_sm (1..4): resident CTAs per SM of the merged FP32
- * tangent (default: as many as fit). */
+ * tangent (default: as many as fit); tangent_kind, the mixed-precision tangent:
+ * CGB_TANGENT_TENSOR (the default) forms each quadrature cell's blocks as one tensor-core
+ * product (tcgen05, 3xTF32, FP32 accumulation) where the cell's neighbour union has at
+ * most 42 nodes, the rest on the CUDA cores; CGB_TANGENT_CORES every cell on the CUDA
+ * cores (FP32, merged contributions). */
+#define CGB_TANGENT_TENSOR 0
+#define CGB_TANGENT_CORES 1
 typedef struct cgb_tuning {
   int n_chunks;
   int residual_threads;
   int tangent_ctas_per_sm;
+  int tangent_kind;
 } cgb_tuning;
 int cgb_assembler_set_tuning(cgb_assembler* a, const cgb_tuning* t);
 

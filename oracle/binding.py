@@ -90,9 +90,15 @@ def load_oracle(native: bool = False) -> C.CDLL:
         lib.orc_abd_isotropic.argtypes = [dbl, dbl, dbl, vp, vp, vp]
         lib.orc_pattern.restype = i64
         lib.orc_pattern.argtypes = [i32, i32, vp, vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        lib.orc_pattern_new.restype = vp
+        lib.orc_pattern_new.argtypes = [i32, i32, vp, vp, i32, vp, vp, vp, vp, C.POINTER(i64)]
+        lib.orc_pattern_fill.restype = i64
+        lib.orc_pattern_fill.argtypes = [vp, i32, i32, vp, vp, vp, vp, vp, vp, vp]
+        lib.orc_pattern_free.restype = None
+        lib.orc_pattern_free.argtypes = [vp]
         lib.orc_update_stiffness.restype = i32
         lib.orc_update_stiffness.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
-                                             vp, i32, i32, vp, vp]
+                                             vp, i32, i32, vp, vp, vp]
         lib.orc_hinge.restype = i32
         lib.orc_hinge.argtypes = [i32, vp, i32, vp, i32, vp, vp, vp, vp, vp]
         lib.orc_fold_angle.restype = dbl
@@ -100,9 +106,13 @@ def load_oracle(native: bool = False) -> C.CDLL:
         lib.orc_hinge_energy.restype = dbl
         lib.orc_hinge_energy.argtypes = [vp, i32, vp]
         lib.orc_strain_energies.restype = None
-        lib.orc_strain_energies.argtypes = [i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        lib.orc_strain_energies.argtypes = [i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         lib.orc_kinematics.restype = None
-        lib.orc_kinematics.argtypes = [i32, vp, vp, vp, vp, vp, vp]
+        lib.orc_kinematics.argtypes = [i32, vp, vp, vp, vp, vp, vp, vp]
+        lib.orc_set_static_schedule.restype = None
+        lib.orc_set_static_schedule.argtypes = [i32]
+        lib.orc_set_natural_curvature.restype = None
+        lib.orc_set_natural_curvature.argtypes = [i32, dbl, dbl, dbl, dbl]
         _libs[name] = lib
         return lib
 
@@ -199,25 +209,45 @@ class Oracle:
         fl_ptr, fl_idx, fr_ptr, fr_idx, nf = _fold_lists(folds)
         outer = np.zeros(3 * n_nodes + 1, np.int32)
         n_gp = len(ptr) - 1
-        nnz = self.lib.orc_pattern(n_nodes, n_gp, _p(ptr), _p(idx), nf, _p(fl_ptr), _p(fl_idx),
-                                   _p(fr_ptr), _p(fr_idx), _p(outer), None, None, None, None)
-        inner = np.zeros(max(nnz, 1), np.int32)
-        col_ptr = np.zeros(n_nodes + 1, np.int64)
-        nblk = nnz // 9
-        col_nodes = np.zeros(max(nblk, 1), np.int32)
-        n = np.diff(ptr)
-        npairs = int((n * (n + 1) // 2).sum())
-        mp = np.zeros(max(npairs, 1), np.int32)
-        rc = self.lib.orc_pattern(n_nodes, n_gp, _p(ptr), _p(idx), nf, _p(fl_ptr), _p(fl_idx),
-                                  _p(fr_ptr), _p(fr_idx), _p(outer), _p(inner), _p(col_ptr),
-                                  _p(col_nodes), _p(mp))
+        nnz_c = C.c_int64(0)
+        h = self.lib.orc_pattern_new(n_nodes, n_gp, _p(ptr), _p(idx), nf, _p(fl_ptr), _p(fl_idx),
+                                     _p(fr_ptr), _p(fr_idx), C.byref(nnz_c))
+        try:
+            nnz = int(nnz_c.value)
+            inner = np.zeros(max(nnz, 1), np.int32)
+            col_ptr = np.zeros(n_nodes + 1, np.int64)
+            nblk = nnz // 9
+            col_nodes = np.zeros(max(nblk, 1), np.int32)
+            n = np.diff(ptr)
+            npairs = int((n * (n + 1) // 2).sum())
+            mp = np.zeros(max(npairs, 1), np.int32)
+            rc = self.lib.orc_pattern_fill(h, n_nodes, n_gp, _p(ptr), _p(idx), _p(outer), _p(inner), _p(col_ptr),
+                                           _p(col_nodes), _p(mp))
+        finally:
+            self.lib.orc_pattern_free(h)
         if rc < 0:
             raise RuntimeError("Assembly: Gauss-point neighbour missing from the sparsity pattern; "
                                "CSR mapping is inconsistent.")
         return outer, inner[:nnz], col_ptr, col_nodes[:nblk], mp[:npairs]
 
+    def set_natural_curvature(self, nc=None):
+        """Kinematics::naturalCurvature() of the oracle (one field per process, as in the
+        reference): nc = {"x0", "width", "angle_deg", "sense": "mountain" | "valley"} (the
+        config's "natural_curvature" object, main.cpp:83-95), or None to switch it off.
+        Assemblies, energies and kinematics given the points' coordinates (gp_xy) then use
+        E1_el = E1 + kappa_bar(X)."""
+        if nc is None:
+            self.lib.orc_set_natural_curvature(0, 0.0, 1.0, 0.0, -1.0)
+            return
+        sign = -1.0 if nc.get("sense", "mountain") == "mountain" else 1.0
+        self.lib.orc_set_natural_curvature(1, float(nc["x0"]), float(nc["width"]),
+                                           float(nc["angle_deg"]) * np.pi / 180.0, sign)
+
     def update_stiffness(self, n_nodes, weight, ptr, idx, dpsi, ddpsi, outer, mp, x, A, B, D,
-                         want_K=True, n_threads=1):
+                         want_K=True, n_threads=1, gp_xy=None, static_schedule=False):
+        """NonLinearAssembler::updateStiffness restated. static_schedule: a static split of
+        the Gauss points over the threads instead of the reference's guided schedule, so
+        that K and F are bitwise the same on every run with the same thread count."""
         weight = _c(weight, np.float64)
         ptr = _c(ptr, np.int64)
         idx = _c(idx, np.int32)
@@ -228,10 +258,12 @@ class Oracle:
         nnz = int(outer[-1])
         K = np.zeros(max(nnz, 1)) if want_K else None
         F = np.zeros(3 * n_nodes)
+        self.lib.orc_set_static_schedule(int(bool(static_schedule)))
         self.lib.orc_update_stiffness(n_nodes, len(ptr) - 1, _p(weight), _p(ptr), _p(idx),
                                       _p(dpsi), _p(ddpsi), _p(_c(outer, np.int32)),
                                       _p(_c(mp, np.int32)), _p(x), _p(A), _p(B), _p(D),
-                                      int(want_K), int(n_threads), _p(K), _p(F))
+                                      int(want_K), int(n_threads), _p(K), _p(F),
+                                      _p(None if gp_xy is None else _c(gp_xy, np.float64)))
         return (K[:nnz] if want_K else None), F
 
     def hinge(self, n_nodes, x, folds, outer=None, col_ptr=None, col_nodes=None, K=None, F=None,
@@ -262,20 +294,23 @@ class Oracle:
         del keep
         return e
 
-    def strain_energies(self, weight, ptr, idx, dpsi, ddpsi, x, A, B, D):
+    def strain_energies(self, weight, ptr, idx, dpsi, ddpsi, x, A, B, D, gp_xy=None):
         em = C.c_double(); eb = C.c_double()
         self.lib.orc_strain_energies(len(ptr) - 1, _p(_c(weight, np.float64)), _p(_c(ptr, np.int64)),
                                      _p(_c(idx, np.int32)), _p(_c(dpsi, np.float64)),
                                      _p(_c(ddpsi, np.float64)), _p(_c(x, np.float64)),
                                      _p(_c(A, np.float64)), _p(_c(B, np.float64)),
-                                     _p(_c(D, np.float64)), C.byref(em), C.byref(eb))
+                                     _p(_c(D, np.float64)), C.byref(em), C.byref(eb),
+                                     _p(None if gp_xy is None else _c(gp_xy, np.float64)))
         return em.value, eb.value
 
-    def kinematics(self, g, ptr, idx, dpsi, ddpsi, x):
-        out = np.zeros(28)
+    def kinematics(self, g, ptr, idx, dpsi, ddpsi, x, X=None):
+        """Kinematics::compute at point g: r0X r0Y r0XX r0YY r0XY b (3 each), C0^-1 (4), E0
+        (xx yy xy), E1 (xx yy xy), E1_el (xx yy xy; X = the point's reference coordinates)."""
+        out = np.zeros(31)
         self.lib.orc_kinematics(int(g), _p(_c(ptr, np.int64)), _p(_c(idx, np.int32)),
                                 _p(_c(dpsi, np.float64)), _p(_c(ddpsi, np.float64)),
-                                _p(_c(x, np.float64)), _p(out))
+                                _p(_c(x, np.float64)), _p(out), _p(None if X is None else _c(X, np.float64)))
         return out
 
 

@@ -221,17 +221,37 @@ void mul3(const M3 a, const M3 b, M3 c) {
 }
 
 // ---------------------------------------------------------------------------------
-// Kinematics::compute (plate/Kinematics.h:61-120), natural curvature inactive.
+// Kinematics::NaturalCurvature (plate/Kinematics.h:21-45): one field for the whole run
+// (the reference's function-local static), set by orc_set_natural_curvature.
+// ---------------------------------------------------------------------------------
+struct NaturalCurvature {
+  bool active = false;
+  double x0 = 0.0, width = 1.0, theta0 = 0.0, sign = -1.0;
+  double g(double X) const {
+    const double t = (X - x0) / width;
+    return std::exp(-t * t) / (1.7724538509055160273 * width);
+  }
+  double kappa_xx(double X) const { return active ? sign * theta0 * g(X) : 0.0; }
+};
+NaturalCurvature g_natural;
+// The face assembly's loop schedule: the reference's guided one (rounding varies from run to
+// run with more than one thread), or static (the same rounding on every run).
+bool g_static_schedule = false;
+
+// ---------------------------------------------------------------------------------
+// Kinematics::compute (plate/Kinematics.h:61-120). X: the point's reference coordinates
+// (for the natural curvature; NULL when the caller has none, then E1_el = E1).
 // ---------------------------------------------------------------------------------
 struct Kin {
   double r0X[3], r0Y[3], r0XX[3], r0YY[3], r0XY[3];
   double C0inv[2][2];
   double b[3];
   double E0[2][2], E1[2][2];
+  double E1el[2][2];  // E1 + kappa_bar (Kinematics.h:110-111)
 };
 
 void kinematics(int64_t p0, int64_t p1, const int32_t* nbr_idx, const double* dpsi,
-                const double* ddpsi, const double* x, Kin& k) {
+                const double* ddpsi, const double* x, Kin& k, const double* X = nullptr) {
   double r0X[3] = {1.0, 0.0, 0.0}, r0Y[3] = {0.0, 1.0, 0.0};
   double r0XX[3] = {0, 0, 0}, r0YY[3] = {0, 0, 0}, r0XY[3] = {0, 0, 0};
   for (int64_t e = p0; e < p1; ++e) {
@@ -267,12 +287,15 @@ void kinematics(int64_t p0, int64_t p1, const int32_t* nbr_idx, const double* dp
   k.E1[0][0] = -dot3(r0XX, k.b);
   k.E1[1][1] = -dot3(r0YY, k.b);
   k.E1[0][1] = k.E1[1][0] = -dot3(r0XY, k.b);
+  std::memcpy(k.E1el, k.E1, sizeof k.E1);
+  if (g_natural.active && X) k.E1el[0][0] += g_natural.kappa_xx(X[0]);
 }
 
-// Constitutive::evaluate (plate/Constitutive.h:57-70): N = A e0 + B e1, M = B^T e0 + D e1.
+// Constitutive::evaluate (plate/Constitutive.h:57-70): N = A e0 + B e1, M = B^T e0 + D e1,
+// e1 from E1_el (Constitutive.h:65).
 void resultants(const Kin& k, const double* A, const double* B, const double* D, double* N, double* M) {
   const double e0[3] = {k.E0[0][0], k.E0[1][1], 2.0 * k.E0[0][1]};
-  const double e1[3] = {k.E1[0][0], k.E1[1][1], 2.0 * k.E1[0][1]};
+  const double e1[3] = {k.E1el[0][0], k.E1el[1][1], 2.0 * k.E1el[0][1]};
   for (int r = 0; r < 3; ++r) {
     const double Ae = A[3 * r] * e0[0] + A[3 * r + 1] * e0[1] + A[3 * r + 2] * e0[2];
     const double Be = B[3 * r] * e1[0] + B[3 * r + 1] * e1[1] + B[3 * r + 2] * e1[2];
@@ -643,20 +666,37 @@ void orc_abd_isotropic(double E, double nu, double h, double* A, double* B, doub
     }
 }
 
-int64_t orc_pattern(int n_nodes, int n_gp, const int64_t* nbr_ptr, const int32_t* nbr_idx,
-                    int n_fold_gp, const int64_t* fl_ptr, const int32_t* fl_idx,
-                    const int64_t* fr_ptr, const int32_t* fr_idx,
-                    int32_t* outer, int32_t* inner, int64_t* col_ptr, int32_t* col_nodes,
-                    int32_t* map) {
-  // plate/Assembly.h:62-99: col_nodes[nj] = sorted unique {ni <= nj} over every pair of
-  // neighbours of every Gauss point; columns 3j+c hold 3 rows per block row.
-  std::vector<std::vector<int>> cols(n_nodes);
-  for (int g = 0; g < n_gp; ++g)
-    for (int64_t a = nbr_ptr[g]; a < nbr_ptr[g + 1]; ++a)
-      for (int64_t b = nbr_ptr[g]; b < nbr_ptr[g + 1]; ++b)
-        if (nbr_idx[a] <= nbr_idx[b]) cols[nbr_idx[b]].push_back(nbr_idx[a]);
-  // Hinge triplets (Constraints.h:376-433): every ordered pair of the concatenated
-  // left+right neighbour lists with node_k <= node_m; K += K_fold widens the pattern.
+namespace {
+
+// plate/Assembly.h:62-82: col_nodes[nj] = sorted unique {ni <= nj} over every pair of
+// neighbours of every Gauss point; plus the hinge triplets (Constraints.h:376-433): every
+// ordered pair of the concatenated left+right neighbour lists with node_k <= node_m, since
+// K += K_fold widens the pattern. The reference collects the pairs in one thread; here
+// each thread collects its share of the Gauss points and the per-column lists are then
+// merged, sorted and made unique column by column. A sorted unique set does not depend on
+// the order its members were collected in, so the columns are the reference's.
+std::vector<std::vector<int>> pattern_columns(int n_nodes, int n_gp, const int64_t* nbr_ptr,
+                                              const int32_t* nbr_idx, int n_fold_gp, const int64_t* fl_ptr,
+                                              const int32_t* fl_idx, const int64_t* fr_ptr,
+                                              const int32_t* fr_idx) {
+  int T = 1;
+#ifdef _OPENMP
+  T = omp_get_max_threads();
+#endif
+  std::vector<std::vector<std::vector<int>>> loc(T, std::vector<std::vector<int>>(n_nodes));
+#pragma omp parallel num_threads(T)
+  {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    auto& L = loc[t];
+#pragma omp for schedule(static)
+    for (int g = 0; g < n_gp; ++g)
+      for (int64_t a = nbr_ptr[g]; a < nbr_ptr[g + 1]; ++a)
+        for (int64_t b = nbr_ptr[g]; b < nbr_ptr[g + 1]; ++b)
+          if (nbr_idx[a] <= nbr_idx[b]) L[nbr_idx[b]].push_back(nbr_idx[a]);
+  }
   std::vector<int> ids;
   for (int g = 0; g < n_fold_gp; ++g) {
     ids.clear();
@@ -664,13 +704,66 @@ int64_t orc_pattern(int n_nodes, int n_gp, const int64_t* nbr_ptr, const int32_t
     for (int64_t a = fr_ptr[g]; a < fr_ptr[g + 1]; ++a) ids.push_back(fr_idx[a]);
     for (int a : ids)
       for (int b : ids)
-        if (a <= b) cols[b].push_back(a);
+        if (a <= b) loc[0][b].push_back(a);
   }
-  int64_t nnz = 0;
+  std::vector<std::vector<int>> cols(n_nodes);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(T)
   for (int j = 0; j < n_nodes; ++j) {
-    std::sort(cols[j].begin(), cols[j].end());
-    cols[j].erase(std::unique(cols[j].begin(), cols[j].end()), cols[j].end());
+    auto& c = cols[j];
+    for (int t = 0; t < T; ++t) {
+      c.insert(c.end(), loc[t][j].begin(), loc[t][j].end());
+      std::vector<int>().swap(loc[t][j]);
+    }
+    std::sort(c.begin(), c.end());
+    c.erase(std::unique(c.begin(), c.end()), c.end());
   }
+  return cols;
+}
+
+int64_t pattern_fill(const std::vector<std::vector<int>>& cols, int n_nodes, int n_gp, const int64_t* nbr_ptr,
+                     const int32_t* nbr_idx, int32_t* outer, int32_t* inner, int64_t* col_ptr,
+                     int32_t* col_nodes, int32_t* map);
+
+}  // namespace
+
+struct orc_pattern_state {
+  std::vector<std::vector<int>> cols;
+};
+
+orc_pattern_state* orc_pattern_new(int n_nodes, int n_gp, const int64_t* nbr_ptr, const int32_t* nbr_idx,
+                                   int n_fold_gp, const int64_t* fl_ptr, const int32_t* fl_idx,
+                                   const int64_t* fr_ptr, const int32_t* fr_idx, int64_t* nnz) {
+  auto* h = new orc_pattern_state;
+  h->cols = pattern_columns(n_nodes, n_gp, nbr_ptr, nbr_idx, n_fold_gp, fl_ptr, fl_idx, fr_ptr, fr_idx);
+  int64_t blocks = 0;
+  for (const auto& c : h->cols) blocks += static_cast<int64_t>(c.size());
+  *nnz = 9 * blocks;
+  return h;
+}
+
+int64_t orc_pattern_fill(const orc_pattern_state* h, int n_nodes, int n_gp, const int64_t* nbr_ptr,
+                         const int32_t* nbr_idx, int32_t* outer, int32_t* inner, int64_t* col_ptr,
+                         int32_t* col_nodes, int32_t* map) {
+  return pattern_fill(h->cols, n_nodes, n_gp, nbr_ptr, nbr_idx, outer, inner, col_ptr, col_nodes, map);
+}
+
+void orc_pattern_free(orc_pattern_state* h) { delete h; }
+
+int64_t orc_pattern(int n_nodes, int n_gp, const int64_t* nbr_ptr, const int32_t* nbr_idx,
+                    int n_fold_gp, const int64_t* fl_ptr, const int32_t* fl_idx,
+                    const int64_t* fr_ptr, const int32_t* fr_idx,
+                    int32_t* outer, int32_t* inner, int64_t* col_ptr, int32_t* col_nodes,
+                    int32_t* map) {
+  const auto cols = pattern_columns(n_nodes, n_gp, nbr_ptr, nbr_idx, n_fold_gp, fl_ptr, fl_idx, fr_ptr, fr_idx);
+  return pattern_fill(cols, n_nodes, n_gp, nbr_ptr, nbr_idx, outer, inner, col_ptr, col_nodes, map);
+}
+
+namespace {
+
+int64_t pattern_fill(const std::vector<std::vector<int>>& cols, int n_nodes, int n_gp, const int64_t* nbr_ptr,
+                     const int32_t* nbr_idx, int32_t* outer, int32_t* inner, int64_t* col_ptr,
+                     int32_t* col_nodes, int32_t* map) {
+  int64_t nnz = 0;
   int64_t off = 0;
   for (int j = 0; j < n_nodes; ++j) {
     for (int c = 0; c < 3; ++c) {
@@ -696,31 +789,51 @@ int64_t orc_pattern(int n_nodes, int n_gp, const int64_t* nbr_ptr, const int32_t
   }
   bool ok = true;
   if (map) {
-    // plate/Assembly.h:112-144: per local pair (i <= j) the position of min(ni, nj)
-    // in col_nodes[max(ni, nj)].
-    int64_t mo = 0;
+    // plate/Assembly.h:112-144 (an OpenMP loop over the Gauss points there too): per
+    // local pair (i <= j) the position of min(ni, nj) in col_nodes[max(ni, nj)].
+    std::vector<int64_t> mptr(static_cast<size_t>(n_gp) + 1, 0);
+    for (int g = 0; g < n_gp; ++g) {
+      const int64_t n = nbr_ptr[g + 1] - nbr_ptr[g];
+      mptr[g + 1] = mptr[g] + n * (n + 1) / 2;
+    }
+    int miss = 0;
+#pragma omp parallel for schedule(guided, 64) reduction(| : miss)
     for (int g = 0; g < n_gp; ++g) {
       const int64_t p0 = nbr_ptr[g];
       const int n = static_cast<int>(nbr_ptr[g + 1] - p0);
+      int64_t mo = mptr[g];
       for (int i = 0; i < n; ++i)
         for (int j = i; j < n; ++j) {
           const int ni = nbr_idx[p0 + i], nj = nbr_idx[p0 + j];
           const int lo = std::min(ni, nj), hi = std::max(ni, nj);
           const auto& ch = cols[hi];
           auto it = std::lower_bound(ch.begin(), ch.end(), lo);
-          if (it == ch.end() || *it != lo) { map[mo++] = -1; ok = false; }
+          if (it == ch.end() || *it != lo) { map[mo++] = -1; miss = 1; }
           else map[mo++] = static_cast<int32_t>(it - ch.begin());
         }
     }
+    ok = miss == 0;
   }
   return ok ? nnz : -1;
+}
+
+}  // namespace
+
+void orc_set_static_schedule(int on) { g_static_schedule = on != 0; }
+
+void orc_set_natural_curvature(int active, double x0, double width, double theta0, double sign) {
+  g_natural.active = active != 0;
+  g_natural.x0 = x0;
+  g_natural.width = width;
+  g_natural.theta0 = theta0;
+  g_natural.sign = sign;
 }
 
 int orc_update_stiffness(int n_nodes, int n_gp, const double* gp_weight, const int64_t* nbr_ptr,
                          const int32_t* nbr_idx, const double* dpsi, const double* ddpsi,
                          const int32_t* outer, const int32_t* map, const double* x,
                          const double* A, const double* B, const double* D, int want_K, int n_threads,
-                         double* K_values, double* F) {
+                         double* K_values, double* F, const double* gp_xy) {
   // plate/Assembly.h:158-345.
   int max_threads = 1;
 #ifdef _OPENMP
@@ -743,6 +856,9 @@ int orc_update_stiffness(int n_nodes, int n_gp, const double* gp_weight, const i
     lf[t].assign(ndof, 0.0);
     if (want_K) lk[t].assign(nnz, 0.0);
   }
+#ifdef _OPENMP
+  omp_set_schedule(g_static_schedule ? omp_sched_static : omp_sched_guided, g_static_schedule ? 0 : 8);
+#endif
   #pragma omp parallel num_threads(max_threads)
   {
     int tid = 0;
@@ -750,13 +866,15 @@ int orc_update_stiffness(int n_nodes, int n_gp, const double* gp_weight, const i
     tid = omp_get_thread_num();
 #endif
     std::vector<double> Bm, Bb, P, Q, Db, N2, C0d, Tu;
-    #pragma omp for schedule(guided, 8)
+    // schedule(guided, 8) as the reference (Assembly.h:199); with g_static_schedule a static
+    // split, which fixes every thread's share and so the rounding for a given thread count.
+    #pragma omp for schedule(runtime)
     for (int g = 0; g < n_gp; ++g) {
       const int64_t p0 = nbr_ptr[g], p1 = nbr_ptr[g + 1];
       const int n = static_cast<int>(p1 - p0);
       if (n == 0) continue;
       Kin k;
-      kinematics(p0, p1, nbr_idx, dpsi, ddpsi, x, k);
+      kinematics(p0, p1, nbr_idx, dpsi, ddpsi, x, k, gp_xy ? gp_xy + 2 * static_cast<int64_t>(g) : nullptr);
       double Nr[3], Mr[3];
       resultants(k, A, B, D, Nr, Mr);
       const double W = gp_weight[g];
@@ -1068,16 +1186,16 @@ double orc_hinge_energy(const double* x, int n_folds, const orc_fold* folds) {
 
 void orc_strain_energies(int n_gp, const double* gp_weight, const int64_t* nbr_ptr, const int32_t* nbr_idx,
                          const double* dpsi, const double* ddpsi, const double* x, const double* A,
-                         const double* B, const double* D, double* E_mem, double* E_ben) {
-  // plate/Meshless.h:204-220.
+                         const double* B, const double* D, double* E_mem, double* E_ben, const double* gp_xy) {
+  // plate/Meshless.h:204-220 (e1 from E1_el, Meshless.h:212).
   double em = 0.0, eb = 0.0;
   for (int g = 0; g < n_gp; ++g) {
     Kin k;
-    kinematics(nbr_ptr[g], nbr_ptr[g + 1], nbr_idx, dpsi, ddpsi, x, k);
+    kinematics(nbr_ptr[g], nbr_ptr[g + 1], nbr_idx, dpsi, ddpsi, x, k, gp_xy ? gp_xy + 2 * g : nullptr);
     double Nr[3], Mr[3];
     resultants(k, A, B, D, Nr, Mr);
     const double e0[3] = {k.E0[0][0], k.E0[1][1], 2.0 * k.E0[0][1]};
-    const double e1[3] = {k.E1[0][0], k.E1[1][1], 2.0 * k.E1[0][1]};
+    const double e1[3] = {k.E1el[0][0], k.E1el[1][1], 2.0 * k.E1el[0][1]};
     em += 0.5 * gp_weight[g] * dot3(e0, Nr);
     eb += 0.5 * gp_weight[g] * dot3(e1, Mr);
   }
@@ -1086,15 +1204,16 @@ void orc_strain_energies(int n_gp, const double* gp_weight, const int64_t* nbr_p
 }
 
 void orc_kinematics(int g, const int64_t* nbr_ptr, const int32_t* nbr_idx, const double* dpsi,
-                    const double* ddpsi, const double* x, double* out) {
+                    const double* ddpsi, const double* x, double* out, const double* X) {
   Kin k;
-  kinematics(nbr_ptr[g], nbr_ptr[g + 1], nbr_idx, dpsi, ddpsi, x, k);
+  kinematics(nbr_ptr[g], nbr_ptr[g + 1], nbr_idx, dpsi, ddpsi, x, k, X);
   std::memcpy(out, k.r0X, 24); std::memcpy(out + 3, k.r0Y, 24);
   std::memcpy(out + 6, k.r0XX, 24); std::memcpy(out + 9, k.r0YY, 24);
   std::memcpy(out + 12, k.r0XY, 24); std::memcpy(out + 15, k.b, 24);
   out[18] = k.C0inv[0][0]; out[19] = k.C0inv[0][1]; out[20] = k.C0inv[1][0]; out[21] = k.C0inv[1][1];
   out[22] = k.E0[0][0]; out[23] = k.E0[1][1]; out[24] = k.E0[0][1];
   out[25] = k.E1[0][0]; out[26] = k.E1[1][1]; out[27] = k.E1[0][1];
+  out[28] = k.E1el[0][0]; out[29] = k.E1el[1][1]; out[30] = k.E1el[0][1];
 }
 
 }  // extern "C"

@@ -90,6 +90,17 @@ int64_t orc_pattern(int n_nodes, int n_gp, const int64_t* nbr_ptr, const int32_t
                     const int64_t* fr_ptr, const int32_t* fr_idx,
                     int32_t* outer, int32_t* inner, int64_t* col_ptr, int32_t* col_nodes,
                     int32_t* map);
+/* The same in two steps over one column build: orc_pattern_new collects the columns and
+ * returns nnz; orc_pattern_fill fills the arrays as call 2 above (outer included);
+ * orc_pattern_free releases the columns. */
+typedef struct orc_pattern_state orc_pattern_state;
+orc_pattern_state* orc_pattern_new(int n_nodes, int n_gp, const int64_t* nbr_ptr, const int32_t* nbr_idx,
+                                   int n_fold_gp, const int64_t* fl_ptr, const int32_t* fl_idx,
+                                   const int64_t* fr_ptr, const int32_t* fr_idx, int64_t* nnz);
+int64_t orc_pattern_fill(const orc_pattern_state* h, int n_nodes, int n_gp, const int64_t* nbr_ptr,
+                         const int32_t* nbr_idx, int32_t* outer, int32_t* inner, int64_t* col_ptr,
+                         int32_t* col_nodes, int32_t* map);
+void orc_pattern_free(orc_pattern_state* h);
 
 /* Face assembly: NonLinearAssembler::updateStiffness (plate/Assembly.h:158-345) with
  * the reference's OpenMP structure (per-thread K and F scratch, guided schedule,
@@ -101,7 +112,7 @@ int orc_update_stiffness(int n_nodes, int n_gp, const double* gp_weight,
                          const double* dpsi, const double* ddpsi,
                          const int32_t* outer, const int32_t* map, const double* x,
                          const double* A, const double* B, const double* D, int want_K,
-                         int n_threads, double* K_values, double* F);
+                         int n_threads, double* K_values, double* F, const double* gp_xy);
 
 /* One fold (plate/PlateData.h:54-76): n_gp crease Gauss point pairs. */
 typedef struct {
@@ -134,13 +145,24 @@ double orc_hinge_energy(const double* x, int n_folds, const orc_fold* folds);
 void orc_strain_energies(int n_gp, const double* gp_weight, const int64_t* nbr_ptr,
                          const int32_t* nbr_idx, const double* dpsi, const double* ddpsi,
                          const double* x, const double* A, const double* B, const double* D,
-                         double* E_mem, double* E_ben);
+                         double* E_mem, double* E_ben, const double* gp_xy);
 
 /* Per-Gauss-point kinematics (plate/Kinematics.h:61-120) for inspection:
  * out[0..27] = r0X(3) r0Y(3) r0XX(3) r0YY(3) r0XY(3) b(3) C0inv(4, row-major)
  * E0(3: xx yy xy) E1(3). */
 void orc_kinematics(int g, const int64_t* nbr_ptr, const int32_t* nbr_idx,
-                    const double* dpsi, const double* ddpsi, const double* x, double* out);
+                    const double* dpsi, const double* ddpsi, const double* x, double* out,
+                    const double* X);
+/* Kinematics::NaturalCurvature (plate/Kinematics.h:21-45), the one field of the run, as
+ * main.cpp:83-95 sets it (sign -1 mountain, +1 valley, theta0 in radians). The functions
+ * above add kappa_bar(X) to E1 (E1_el) at the points whose reference coordinates they are
+ * given (gp_xy, 2 per point; X for orc_kinematics, whose out[28..30] is E1_el); with NULL
+ * coordinates, or inactive, E1_el = E1. */
+void orc_set_natural_curvature(int active, double x0, double width, double theta0, double sign);
+/* The face assembly's OpenMP schedule: 0 the reference's schedule(guided, 8) (Assembly.h:199;
+ * with several threads the per-thread sums, and so the last bits of K and F, vary from run to
+ * run), 1 a static split (bitwise the same on every run with the same thread count). */
+void orc_set_static_schedule(int on);
 
 #ifdef __cplusplus
 }

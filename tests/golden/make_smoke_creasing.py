@@ -77,4 +77,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CURVAMI_REFERENCE")
+    if not root:
+        sys.exit("usage: make_smoke_creasing.py <reference root> (or set CURVAMI_REFERENCE)")
+    main(root)

@@ -38,7 +38,7 @@ class OracleAssembly:
         f = self.f
         K, F = self.o.update_stiffness(self.n, self.p.faces.weight, f["ptr"], f["idx"], f["dpsi"], f["ddpsi"],
                                        self.outer, self.mp, x, self.A, self.B, self.D, want_K=want_K,
-                                       n_threads=self.threads)
+                                       n_threads=self.threads, static_schedule=True)
         if hinge:
             K, F = self.o.hinge(self.n, x, self.folds, self.outer, self.col_ptr, self.col_nodes, K, F)
         return (K if want_K else None), F

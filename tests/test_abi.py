@@ -91,7 +91,8 @@ def test_ctypes_structs_match_the_header(tmp_path):
     if cc is None:
         pytest.skip("no C compiler")
     structs = {"cgb_crease": _lib.Crease, "cgb_shape_params": _lib.ShapeParams, "cgb_fold": _lib.Fold,
-               "cgb_face_problem": _lib.FaceProblem, "cgb_tuning": _lib.Tuning}
+               "cgb_face_problem": _lib.FaceProblem, "cgb_tuning": _lib.Tuning,
+               "cgb_natural_curvature": _lib.NaturalCurvature}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "curvami_gb300.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')

@@ -89,7 +89,7 @@ def test_tuning_changes_launch_shape_not_results(ctx):
     x = np.concatenate(fields(ps))
     fl = cg.TANGENT | cg.HINGE | cg.DETERMINISTIC
     K0, F0 = batch.asm.assemble(x, fl)
-    for t in [(1, 64, 1), (3, 128, 2), (8, 256, 3)]:
+    for t in [(1, 64, 1), (3, 128, 2), (8, 256, 3), (3, 128, 0, cg.TANGENT_CORES)]:
         batch.asm.set_tuning(*t)
         K, F = batch.asm.assemble(x, fl)
         assert np.array_equal(K, K0) and np.array_equal(F, F0)
@@ -99,6 +99,8 @@ def test_tuning_changes_launch_shape_not_results(ctx):
         batch.asm.set_tuning(17, 0, 0)
     with pytest.raises(cg.CGBError):
         batch.asm.set_tuning(0, 96, 0)
+    with pytest.raises(cg.CGBError):
+        batch.asm.set_tuning(0, 0, 0, 7)
 
 
 def test_autotune_picks_and_caches(ctx, tmp_path):
@@ -119,7 +121,8 @@ def test_autotune_picks_and_caches(ctx, tmp_path):
     cand = {"n_chunks": (1, 2), "residual_threads": (128, 256), "tangent_ctas_per_sm": (0,)}
     r1 = at.autotune(asm, d_x.data_ptr(), d_K.data_ptr(), d_F.data_ptr(), fl, candidates=cand,
                      cache_path=cache, repeats=2)
-    assert not r1["cached"] and len(r1["tried"]) == 4 and r1["tuning"] in [(c, r, 0) for c in (1, 2) for r in (128, 256)]
+    assert not r1["cached"] and len(r1["tried"]) == 4
+    assert tuple(r1["tuning"]) in [(c, r, 0, 0) for c in (1, 2) for r in (128, 256)]
     assert asm.tuning == tuple(r1["tuning"])
     r2 = at.autotune(asm, d_x.data_ptr(), d_K.data_ptr(), d_F.data_ptr(), fl, candidates=cand,
                      cache_path=cache, repeats=2)

@@ -78,9 +78,10 @@ def test_fold_angle_averages_across_the_cut():
 
 
 def test_fixture_nodes_are_the_reference_mesh():
-    src = "/root/reference/examples/smoke_centre_crease/CB_n20.msh"
-    if not os.path.exists(src):
-        pytest.skip("reference tree not present")
+    root = os.environ.get("CURVAMI_REFERENCE")
+    src = os.path.join(root or "", "examples", "smoke_centre_crease", "CB_n20.msh")
+    if not root or not os.path.exists(src):
+        pytest.skip("reference tree not present (set CURVAMI_REFERENCE to its root)")
     rxy, _ = mesh.read_msh41(src)
     fx = np.load(os.path.join(H.GOLDEN, "smoke_centre_crease_nodes.npy"))
     a = {tuple(p) for p in rxy.tolist()}

@@ -62,6 +62,7 @@ SHAPE_CASES = {
     "cubic_bspline": lambda: synth.square_plate(15, 0.5, 4, jitter=0.05, crease="row", kernel=1, seed=4),
     "three_arcs": lambda: synth.batched_plate(31, np.random.default_rng(6)),
     "three_cuts": lambda: synth.batched_plate(31, np.random.default_rng(7)),
+    "six_cuts_with_tips": lambda: synth.many_cuts_plate(61, 6),
 }
 
 

@@ -70,28 +70,28 @@ class _FakeAsm:
     def stats(self):
         return {"pairs": 50_000_000, "blocks": 400_000, "entries": 5_000_000, "direct_groups": 0}
 
-    def set_tuning(self, c, r, t):
-        self.tuning = (c, r, t)
+    def set_tuning(self, c, r, t, k=0):
+        self.tuning = (c, r, t, k)
 
     def assemble_device(self, *a):
         self.calls += 1
-        c, r, t = self.tuning
-        time.sleep(0.001 * (abs(c - 2) + (r == 128) + t))   # best: (2, 256, 0)
+        c, r, t, k = self.tuning
+        time.sleep(0.001 * (abs(c - 2) + (r == 128) + t + k))   # best: (2, 256, 0, 0)
 
 
 def test_autotune_search_and_cache(tmp_path):
     asm = _FakeAsm()
     cache = str(tmp_path / "t.json")
     r = at.autotune(asm, 1, 2, 3, flags=7, device_name="fake", cache_path=cache, repeats=2)
-    assert tuple(r["tuning"]) == (2, 256, 0) and asm.tuning == (2, 256, 0) and not r["cached"]
+    assert tuple(r["tuning"]) == (2, 256, 0, 0) and asm.tuning == (2, 256, 0, 0) and not r["cached"]
     assert len(r["tried"]) == 20 and at.spread(r) > 1.0
     calls = asm.calls
     r2 = at.autotune(asm, 1, 2, 3, flags=7, device_name="fake", cache_path=cache)
-    assert r2["cached"] and tuple(r2["tuning"]) == (2, 256, 0) and asm.calls == calls
+    assert r2["cached"] and tuple(r2["tuning"]) == (2, 256, 0, 0) and asm.calls == calls
     # another flag set is another key
     r3 = at.autotune(asm, 1, 2, 3, flags=3, device_name="fake", cache_path=cache, repeats=1,
                      candidates={"n_chunks": (1, 2), "residual_threads": (256,), "tangent_ctas_per_sm": (0,)})
-    assert not r3["cached"] and tuple(r3["tuning"]) == (2, 256, 0)
+    assert not r3["cached"] and tuple(r3["tuning"]) == (2, 256, 0, 0)
 
 
 def test_four_crease_plate_layout():

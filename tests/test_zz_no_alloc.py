@@ -7,8 +7,11 @@ library keeps its one scratch array (the FP32 block accumulator) in a fixed,
 file-scope device array. The test allocates the caller's arrays itself (torch), then
 checks two calls in a row against the allocating entry point (cgb_assemble_device with
 CGB_TANGENT | CGB_MIXED): the residual to 1e-13 and the FP32 tangent to 1e-5 of its
-scale (two FP32 atomic summation orders), the bars the mixed path meets elsewhere. Collected last, so a failure here
-leaves every other test already run.
+scale (two FP32 atomic summation orders), the bars the mixed path meets elsewhere. It
+then checks the refusals (bad sizes on the host; neighbour counts above max_neighbours
+on the device, reported at the next synchronisation without a fault) and that a call
+without face points reads no input and returns zero K and F. Collected last, so a
+failure here leaves every other test already run.
 """
 import ctypes as C
 
@@ -75,8 +78,56 @@ def test_noalloc_matches_allocating_path():
         assert np.abs(K - K_ref).max() <= 1e-5 * np.abs(K_ref).max(), call
 
     # Sizes beyond the fixed accumulator are refused with a clear error.
+    nnz = prob.nnz
     prob.nnz = 9 * (_lib.NOALLOC_MAX_BLOCKS + 1)
     rc = ctx.lib.cgb_assemble_face_noalloc(ctx.h, C.byref(prob), C.c_void_p(x_d.data_ptr()),
                                            C.c_void_p(1), C.c_void_p(1))
     assert rc == _lib.CGB_ERR_CAPACITY
     assert b"exceeds the fixed accumulator" in ctx.lib.cgb_last_error(ctx.h)
+    prob.nnz = nnz
+
+    def call(pr, K, F):
+        return ctx.lib.cgb_assemble_face_noalloc(ctx.h, C.byref(pr), C.c_void_p(x_d.data_ptr()),
+                                                 C.c_void_p(K.data_ptr()), C.c_void_p(F.data_ptr()))
+
+    K = torch.full((asm.nnz,), np.nan, dtype=torch.float64, device="cuda")
+    F = torch.full((3 * p.n_nodes,), np.nan, dtype=torch.float64, device="cuda")
+    # Refusals on the host: nothing is launched.
+    for field, bad in (("n_nodes", 0), ("n_gp", -1), ("nnz", -9), ("nnz", nnz + 1), ("max_neighbours", -1)):
+        good = getattr(prob, field)
+        setattr(prob, field, bad)
+        assert call(prob, K, F) == _lib.CGB_ERR_INVALID, field
+        setattr(prob, field, good)
+    prob.max_neighbours = 100000
+    assert call(prob, K, F) == _lib.CGB_ERR_CAPACITY
+    assert b"too many neighbours" in ctx.lib.cgb_last_error(ctx.h)
+    prob.max_neighbours = faces.max_n
+    outer_ptr = prob.outer
+    prob.outer = None
+    assert call(prob, K, F) == _lib.CGB_ERR_INVALID
+    assert b"NULL input array" in ctx.lib.cgb_last_error(ctx.h)
+    ctx.synchronize()
+
+    # No face point: no input array is read (all NULL here) and K and F come back zero.
+    empty = _lib.FaceProblem()
+    empty.n_gp = 0
+    empty.n_nodes = p.n_nodes
+    empty.max_neighbours = 0
+    empty.nnz = asm.nnz
+    assert call(empty, K, F) == 0, ctx.lib.cgb_last_error(ctx.h)
+    ctx.synchronize()
+    assert not K.cpu().numpy().any() and not F.cpu().numpy().any()
+    prob.outer = outer_ptr
+
+    # A max_neighbours below the true largest count: the points that do not fit the
+    # staging are skipped on the device and the next synchronisation reports it.
+    prob.max_neighbours = faces.max_n - 1
+    assert call(prob, K, F) == 0, ctx.lib.cgb_last_error(ctx.h)
+    with pytest.raises(cg.CGBError) as ei:
+        ctx.synchronize()
+    assert ei.value.code == _lib.CGB_ERR_DEVICE and "out of range" in str(ei.value)
+    # The context stays usable: the correct sizes give the allocating path's result again.
+    prob.max_neighbours = faces.max_n
+    assert call(prob, K, F) == 0
+    ctx.synchronize()
+    assert np.abs(F.cpu().numpy() - F_ref).max() <= 1e-13 * np.abs(F_ref).max()
