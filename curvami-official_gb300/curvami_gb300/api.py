@@ -37,6 +37,7 @@ class Context:
             raise L.CGBError(rc, f"cgb_create failed (status {rc}): no usable CUDA device")
         self.h = h
         self._keep = []
+        self.natural_curvature = None
 
     def check(self, rc: int):
         if rc != L.CGB_OK:

@@ -24,9 +24,14 @@ G_tip with the interpolated and the analytic q, the hinge virtual work, the form
 tie work removed (_r), the mixed and subtracted forms at a fold, and the band form
 (fold_band > 0), with the _fold.csv and _crease.csv files of ``JIntegral::report``.
 
-Not restated: the natural-curvature band term (the assembly here has no natural curvature, so
-Gband is zero and G1b_h = G1_h, as in the reference without one), the console summary and the
-HDF5 datasets (no HDF5 library here).
+With a natural curvature (Kinematics::NaturalCurvature, the context's
+cgb_set_natural_curvature), N, M and W_h come from the elastic bending strain E1_el = E1 +
+kappa_bar while the 2 E1 M term keeps the geometric E1, and the band term (JIntegral.h:
+145-166, 492-520) is added: Gband_h = -(1/h) sum_g w_g q_h M : d(kappa_bar)/dX . d, Gband2_h
+the same along d_perp, Gband_a with the analytic q; G1b_h = G1_h + Gband_h, G2b_h = G2_h +
+Gband2_h. Without one these are zero and G1b_h = G1_h, as in the reference.
+
+Not restated: the console summary and the HDF5 datasets (no HDF5 library here).
 """
 from __future__ import annotations
 
@@ -61,9 +66,24 @@ def q_value(rho, r: Ring, linear_q: bool):
     return np.where(rho <= r.rho1, 1.0, np.where(rho >= r.rho2, 0.0, q))
 
 
-def _tensors(state: np.ndarray):
+def natural_kappa(X, nc):
+    """kappa_bar_XX(X) of a natural-curvature band (Kinematics.h:25-34; nc as the config's
+    "natural_curvature" object) and its X-derivative; zeros without one."""
+    X = np.asarray(X, np.float64)
+    if nc is None:
+        return np.zeros_like(X), np.zeros_like(X)
+    sign = -1.0 if nc.get("sense", "mountain") == "mountain" else 1.0
+    w = float(nc["width"])
+    t = (X - float(nc["x0"])) / w
+    k = sign * math.radians(float(nc["angle_deg"])) * np.exp(-t * t) / (math.sqrt(math.pi) * w)
+    return k, k * (-2.0 * (X - float(nc["x0"])) / (w * w))
+
+
+def _tensors(state: np.ndarray, kbar=None):
     """Per-point F0 (n,3,2), C0, N, M, E1 (n,2,2), W_h, b, r_XX, r_YY, r_XY from cgb_point_state
-    rows: u, r_X, r_Y, r_XX, r_YY, r_XY, b, E0 (xx yy xy), E1 (xx yy xy), N, M (Voigt)."""
+    rows: u, r_X, r_Y, r_XX, r_YY, r_XY, b, E0 (xx yy xy), E1 (xx yy xy), N, M (Voigt). kbar:
+    the natural curvature kappa_bar_XX per point (W_h from E1_el = E1 + kappa_bar; E1 stays
+    the geometric curvature)."""
     st = np.asarray(state, np.float64)
     a1, a2 = st[:, 3:6], st[:, 6:9]
     F0 = np.stack([a1, a2], axis=2)
@@ -76,6 +96,9 @@ def _tensors(state: np.ndarray):
     E1 = sym(st[:, 24:27])
     e0 = st[:, 21:24] * np.array([1.0, 1.0, 2.0])
     e1 = st[:, 24:27] * np.array([1.0, 1.0, 2.0])
+    if kbar is not None:
+        e1 = e1.copy()
+        e1[:, 0] += kbar
     W = 0.5 * (np.einsum("ni,ni->n", st[:, 27:30], e0) + np.einsum("ni,ni->n", st[:, 30:33], e1))
     return dict(F0=F0, C0=C0, N=N, M=M, E1=E1, W=W, Nv=st[:, 27:30], Mv=st[:, 30:33], b=st[:, 18:21],
                 rXX=st[:, 9:12], rYY=st[:, 12:15], rXY=st[:, 15:18])
@@ -305,12 +328,14 @@ def crease_points(folds) -> list:
 
 
 def compute_from_state(state, face_xy, face_weight, node_xy, ptr, idx, dpsi, ddpsi, h: float, s: Settings,
-                       folds=(), F_int=None, crease_out: list | None = None):
+                       folds=(), F_int=None, crease_out: list | None = None, natural_curvature=None, psi=None):
     """JIntegral::compute from a point state (n, 33) and the faces' shape functions. Returns
     one dict per ring with the reference's RingResult names (the fold columns under their
     _fold.csv names). With folds (FoldState list), the fold terms are added; they need F_int,
     the plate's own nodal internal force at the same state (the face assembly without the
-    hinge), and fill crease_out, when given, with the crease points of crease_points()."""
+    hinge), and fill crease_out, when given, with the crease points of crease_points().
+    natural_curvature: the band the state was computed with (its N and M already include
+    it), for W_h and the band term; the band term's interpolated q needs psi."""
     X = np.asarray(face_xy, np.float64)
     w = np.asarray(face_weight, np.float64)
     node_xy = np.asarray(node_xy, np.float64)
@@ -325,7 +350,8 @@ def compute_from_state(state, face_xy, face_weight, node_xy, ptr, idx, dpsi, ddp
     d = d / np.linalg.norm(d)
     dperp = np.array([-d[1], d[0]])
     d3, dperp3 = np.array([d[0], d[1], 0.0]), np.array([dperp[0], dperp[1], 0.0])
-    T = _tensors(state)
+    kbar, dkbar = natural_kappa(X[:, 0], natural_curvature)
+    T = _tensors(state, kbar if natural_curvature is not None else None)
     B, Bd, CN = eshelby(T)
     rvec = X - tip
     rho = np.linalg.norm(rvec, axis=1)
@@ -388,7 +414,21 @@ def compute_from_state(state, face_xy, face_weight, node_xy, ptr, idx, dpsi, ddp
         R["angle_deg"] = math.degrees(math.atan2(R["G2"], R["G1"]))
         R["G1_s"], R["G2_s"] = R["G1"] - R["vw1_s"], R["G2"] - R["vw2_s"]
         R["Gband_h"] = R["Gband_a"] = R["Gband2_h"] = 0.0
-        R["G1b_h"], R["G2b_h"] = R["G1_h"], R["G2_h"]
+        if natural_curvature is not None:
+            # JIntegral.h:492-520: -(1/h) sum_g w_g q M_ab d_c d(kappa_bar_ab)/dX_c over the points
+            # where kappa_bar varies; only kappa_bar_XX is nonzero, so M : dk = M_XX dk_XX d_X.
+            thr = 1e-14 * math.radians(float(natural_curvature["angle_deg"])) / float(natural_curvature["width"]) ** 2
+            m1 = T["M"][:, 0, 0] * dkbar * d[0]
+            m2 = T["M"][:, 0, 0] * dkbar * dperp[0]
+            live = np.abs(dkbar * d[0]) + np.abs(dkbar * dperp[0]) >= thr
+            if psi is None:
+                raise ValueError("the natural-curvature band term needs the faces' Psi")
+            qh = np.bincount(rows, weights=qI * np.asarray(psi, np.float64), minlength=n)
+            qa = q_value(rho, r, s.linear_q)
+            R["Gband_h"] = float(-(w * qh * m1)[live].sum() / h)
+            R["Gband2_h"] = float(-(w * qh * m2)[live].sum() / h)
+            R["Gband_a"] = float(-(w * qa * m1)[live].sum() / h)
+        R["G1b_h"], R["G2b_h"] = R["G1_h"] + R["Gband_h"], R["G2_h"] + R["Gband2_h"]
         for k in FOLD_COLUMNS[4:]:
             R.setdefault(k, 0.0)
         R["plate_h"], R["plate_a"], R["abs_plate_h"] = R["G1_h"], R["G1"], R["abs_sum_h"]
@@ -583,7 +623,8 @@ def compute(model, x, s: Settings, h: float | None = None, fold_state=None, crea
     if folds:
         F_int = model.asm.assemble(x, 0)[1]
     return compute_from_state(st, p.faces.xy, p.faces.weight, p.node_xy, dn["ptr"], dn["idx"], dn["dpsi"],
-                              dn["ddpsi"], p.thickness if h is None else h, s, folds, F_int, crease_out)
+                              dn["ddpsi"], p.thickness if h is None else h, s, folds, F_int, crease_out,
+                              natural_curvature=getattr(model.ctx, "natural_curvature", None), psi=dn["psi"])
 
 
 CSV_COLUMNS = ["step", "ring", "rho1", "rho2", "G_x", "G_y", "G1", "G2", "G_abs", "angle_deg", "n_gp", "abs_sum",

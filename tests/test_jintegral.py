@@ -134,3 +134,34 @@ def test_gpu_state_matches_oracle(o, plate_shapes):
     for a, b in zip(gpu, ref):
         for k in J.CSV_COLUMNS[2:]:
             assert abs(a[k] - b[k]) <= 1e-10 * max(abs(b[k]), abs(b["abs_sum"]), 1e-30), k
+
+
+def test_natural_curvature_band_term_balances_the_plate_term(o, plate_shapes):
+    """A flat, unloaded plate with a natural-curvature band: E1 = 0, M = D kappa_bar and
+    W_h = 1/2 kappa_bar D11 kappa_bar depend on X only through the band, with
+    dW_h/dX = M : d(kappa_bar)/dX. So the plate term -(1/h) sum w W_h d.grad q and the band
+    term -(1/h) sum w q M : d(kappa_bar)/dX . d add up to -(1/h) int d.grad(q W_h), zero for a
+    q that vanishes on the outer ring: G1 + Gband_a and G1_h + Gband_h (G1b_h) vanish to the
+    quadrature error while each term does not (JIntegral.h:145-166, 492-520)."""
+    p, sh = plate_shapes
+    n = len(sh["ptr"]) - 1
+    c = p.node_xy.mean(0)
+    nc = {"x0": float(c[0]) + 0.3, "width": 0.8, "angle_deg": 20.0, "sense": "valley"}
+    kb, _ = J.natural_kappa(p.faces.xy[:, 0], nc)
+    D = np.asarray(o.abd(p.E, p.nu, p.thickness)[2]).reshape(3, 3)
+    st = np.zeros((n, 33))
+    st[:, 3] = 1.0                 # r_X = e_x
+    st[:, 7] = 1.0                 # r_Y = e_y
+    st[:, 20] = 1.0                # b = e_z
+    st[:, 30:33] = kb[:, None] * D[:, 0][None, :]   # M = D (kappa_bar, 0, 0)
+    s = J.Settings(tip=tuple(c), dir=(1.0, 0.0), rings=[J.Ring(1.0, 2.5)])
+    r = J.compute_from_state(st, p.faces.xy, p.faces.weight, p.node_xy, sh["ptr"], sh["idx"], sh["dpsi"],
+                             sh["ddpsi"], p.thickness, s, natural_curvature=nc, psi=sh["psi"])[0]
+    assert abs(r["Gband_a"]) > 0 and abs(r["G1"]) > 0
+    assert abs(r["G1"] + r["Gband_a"]) <= 5e-3 * abs(r["Gband_a"])
+    assert abs(r["G1b_h"]) <= 5e-3 * abs(r["Gband_h"])
+    # without the band every band column is zero and G1b_h is G1_h
+    st[:, 30:33] = 0.0
+    r0 = J.compute_from_state(st, p.faces.xy, p.faces.weight, p.node_xy, sh["ptr"], sh["idx"], sh["dpsi"],
+                              sh["ddpsi"], p.thickness, s)[0]
+    assert r0["Gband_h"] == 0.0 and r0["G1b_h"] == r0["G1_h"]
