@@ -38,9 +38,10 @@ for _p in (ROOT, PKG_DIR):
 METRIC = "Gauss-pt residual+tangent evals/s, mixed vs FP64 GPU at stated error"
 UNIT = "GP evals/s"
 SEED = 1003
-# DRAM bytes (read + write) per Gauss point of one face_tangent_merged_kernel launch, from
-# ncu on the 101 x 101 plate (profiles/face_tangent_merged_kernel_101.md).
-TANGENT_DRAM_BYTES_PER_GP = (81.53728e6 + 1.746432e6) / 40000
+# DRAM bytes (read + write) per Gauss point of the tensor-core tangent, from one ncu capture
+# of a 101 x 101 plate (160,000 Gauss points); None until measured.
+TENSOR_DRAM_BYTES_PER_GP = None
+TENSOR_TRAFFIC_SOURCE = "not captured yet"
 WORKLOAD = ("single-plate assembly at scale: 201x201 jittered nodes, 4x4 Gauss rule (640,000 "
             "Gauss points), quadratic RKPM, quartic window, rho = 3h, circular-arc crease R = 60 "
             "with elastic hinge Kt = 1e-3, seeded 8-mode Fourier displacement (rotations up to 60 "
@@ -373,6 +374,9 @@ def run_gpu(args):
     asm.set_tuning(*tune_mix["tuning"])
     ms_det = timed(DET, max(3, args.steps // 4), 3)
     ms_res = timed(cg.HINGE | cg.MIXED, args.steps, 3)  # residual only (line-search trials)
+    asm.set_tuning(*tune_mix["tuning"][:3], cg.TANGENT_CORES)   # the CUDA-core tangent, same launch shape
+    ms_cores = timed(MIX, args.steps, 3)
+    asm.set_tuning(*tune_mix["tuning"])
 
     # Per-phase device times of the mixed step (events inside the library).
     ctx.profile(True)
@@ -407,50 +411,56 @@ def run_gpu(args):
     barrier()
 
     # Roofline. The step runs two kernels per chunk: the FP64 residual kernel ("face") and,
-    # on a second stream, the FP32 tangent with merged contributions ("tangent"), which
-    # dominates. Times are sums over the step's chunk launches (events on each kernel's
-    # own stream).
+    # on a second stream, the FP32-class tangent ("tangent"): the tensor-core product per
+    # cell of 16 points (tcgen05, 3xTF32) and, for the cells whose node union exceeds one
+    # 128-row tile, the CUDA-core merged tangent. Times are sums over the step's chunk
+    # launches (events on each kernel's own stream).
     ptr = model.faces.download()["ptr"]
     n = np.diff(ptr).astype(np.float64)
     steps = max(args.steps, 1)
     tan_ms = ph_ms["tangent"] / steps
     res_ms = ph_ms["face"] / steps
-    # Compulsory bytes of the tangent per step: per-point state (32 floats), per neighbour
-    # the FP32 grad / Hessian Phi and its id (24 B), per pair its 2-byte contribution code,
-    # per merged entry its block slot and contribution range (8 B), and the FP32 block
-    # accumulator once (48 B per block: three 16-byte vectors).
     work = asm.stats()
-    alg_bytes = float((128 + 24 * n + n * (n + 1)).sum() + 8.0 * work["entries"] + 48.0 * work["blocks"])
+    tc = asm.tensor_stats()
     tan_launches = max(int(ph_n["tangent"]) // steps, 1)
-    # DRAM traffic of one tangent launch, from the ncu capture of the 101 x 101 plate
-    # (profiles/face_tangent_merged_kernel_101.md: 87.66 MB read + write for a launch of
-    # 40,000 Gauss points), scaled by the Gauss points of this launch; the traffic per point
-    # is the same at both sizes (the same n, the same per-point records).
-    traffic = TANGENT_DRAM_BYTES_PER_GP * len(n) / tan_launches
     flops_fp64 = float((121 * n + 200).sum())                 # residual path (FP64)
     flops_total = float((181 * n * (n + 1) / 2 + 364 * n + 200).sum())
-    flops_fp32 = flops_total - flops_fp64
+    flops_fp32 = flops_total - flops_fp64                       # the tangent's share of F_B(n)
+    # Compulsory bytes of the tangent per step: per-point state (32 floats), per neighbour
+    # the FP32 grad / Hessian Phi (20 B) and its node's union index (1 B), per merged entry its
+    # block slot and union indices (8 B), and the FP32 block accumulator once (48 B per block).
+    alg_bytes = float((128 + 21 * n).sum() + 8.0 * work["entries"] + 48.0 * work["blocks"])
+    # The tensor pipe's executed work: five 128 x N x 8 MMAs per point, 3xTF32 (10,240 N flops).
+    tensor_flops = 10240.0 * tc["point_cols"]
     peaks, peak_kind = measured_peaks()
     p64, p32 = fma_peaks(local)
-    achieved_gbs = alg_bytes / (tan_ms * 1e-3) / 1e9
+    tf32_peak = peaks["bf16_tflops"] / 2.0
+    tensor_path = asm.tuning is None or len(asm.tuning) < 4 or asm.tuning[3] == cg.TANGENT_TENSOR
+    ach = flops_fp32 / (tan_ms * 1e-3) / 1e12
     roofline = {
-        "bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-        "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": traffic,
-        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, 101x101 plate, scaled per Gauss point",
-        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-        "kernel": "face_tangent_merged_kernel (FP32 tangent, merged contributions)",
-        "launch_ms": tan_ms / tan_launches, "launches_per_step": tan_launches,
-        "algorithmic_bytes_per_launch": alg_bytes / tan_launches,
-        "step_ms": tan_ms, "algorithmic_bytes_per_step": alg_bytes, "work": work,
-        "binding_unit": "L1 / shared-memory data pipe (ncu: 82% of peak; FMA pipe 44%)",
+        "bound": "tensor", "achieved": ach, "peak": tf32_peak, "unit": "TFLOP/s", "frac": ach / tf32_peak,
+        "traffic": TENSOR_DRAM_BYTES_PER_GP * len(n) / tan_launches if TENSOR_DRAM_BYTES_PER_GP else None,
+        "traffic_source": TENSOR_TRAFFIC_SOURCE,
+        "peak_source": f"{peak_kind}: TF32 dense = half of MEASURED_PEAKS.json bf16_tflops (the tensor cores' "
+                       f"TF32:BF16 rate is 1:2)",
+        "kernel": ("face_tangent_tc_kernel (tcgen05.mma kind::tf32, 3xTF32, A in tensor memory, accumulator in "
+                   "tensor memory) + face_tangent_merged_kernel for the cells it does not take") if tensor_path else
+                  "face_tangent_merged_kernel (FP32 CUDA cores, merged contributions)",
+        "achieved_what": "the reference's hand-counted tangent flops, F_B(n) - F_R(n) per Gauss point, per second",
+        "launch_ms": tan_ms / tan_launches, "launches_per_step": tan_launches, "step_ms": tan_ms,
+        "algorithmic_flops_per_step": flops_fp32, "work": work, "tensor_work": tc,
+        "tensor_pipe": {"executed_tflops": tensor_flops / (tan_ms * 1e-3) / 1e12,
+                        "frac": tensor_flops / (tan_ms * 1e-3) / 1e12 / tf32_peak,
+                        "what": "MMA flops issued (3xTF32, zero rows of each point's support and both "
+                                "triangles of the symmetric cell product included) over the tangent's time"},
+        "hbm": {"achieved_gbs": alg_bytes / (tan_ms * 1e-3) / 1e9, "peak_gbs": peaks["hbm_gbs"],
+                "frac": alg_bytes / (tan_ms * 1e-3) / 1e9 / peaks["hbm_gbs"], "algorithmic_bytes_per_step": alg_bytes},
         "pipes": {
-            "fp32_tangent": {"achieved_tflops": flops_fp32 / (tan_ms * 1e-3) / 1e12, "peak_tflops": p32,
-                             "frac": flops_fp32 / (tan_ms * 1e-3) / 1e12 / p32 if p32 > 0 else None,
-                             "flops_per_step": flops_fp32, "peak_source": "measured live (FMA probe)"},
             "fp64_residual": {"kernel": "face_residual_kernel", "step_ms": res_ms,
                               "achieved_tflops": flops_fp64 / (res_ms * 1e-3) / 1e12, "peak_tflops": p64,
                               "frac": flops_fp64 / (res_ms * 1e-3) / 1e12 / p64 if p64 > 0 else None,
                               "flops_per_step": flops_fp64, "peak_source": "measured live (FMA probe)"},
+            "fp32_peak_tflops": p32,
         },
     }
 
@@ -473,17 +483,21 @@ def run_gpu(args):
     post = None if args.no_shape_stage else post_processing(cg, ctx, model, x_d, stream)
     four = None
     arc = None
+    batched = None
     if not args.no_shape_stage:
         try:
             four = four_creases_assembly(cg, ctx, stream)
         except cg.CGBError as e:   # a rank-deficient support at the junction is reported, not hidden
             four = {"error": str(e)}
         arc = arc_length_path(cg, ctx)
+        batched = batched_object(cg, ctx, args.plates, max(5, args.steps // 2), 3)
 
     line = {
         "metric": METRIC, "value": v_mix, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": W, "ms_per_step": ms_mix, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp64 residual + fp32 tangent",
+        "vs_baseline": None,
+        "dtype": "fp64 residual + 3xtf32 tensor-core tangent (fp32 accumulation)" if tensor_path else
+                 "fp64 residual + fp32 tangent",
         "data": "synthetic (seeded generator, no dataset)",
         "config": {"workload": WORKLOAD, "seed": SEED, "n_gauss_points": n_gp, "n_nodes": plate.n_nodes,
                    "nnz_K": asm.nnz, "mean_neighbours": float(n.mean()), "max_neighbours": int(n.max()),
@@ -498,6 +512,8 @@ def run_gpu(args):
                  "phases_ms": {k: v / max(3, args.steps // 4) for k, v in ph64_ms.items()}},
         "deterministic_mixed": {"value": world * n_gp / (ms_det * 1e-3), "ms_per_step": ms_det},
         "residual_only": {"value": world * n_gp / (ms_res * 1e-3), "ms_per_step": ms_res},
+        "mixed_cuda_core_tangent": {"value": world * n_gp / (ms_cores * 1e-3), "ms_per_step": ms_cores,
+                                    "what": "the same step with every cell's tangent on the CUDA cores (FP32)"},
         "error_mixed_vs_fp64": err,
         "error_vs_oracle": err_oracle,
         "phases_ms": {k: v / max(args.steps, 1) for k, v in ph_ms.items()},
@@ -512,6 +528,7 @@ def run_gpu(args):
         "progressive_creasing": creasing,
         "four_creases": four,
         "arc_length_path": arc,
+        "batched": batched,
         "post_processing": post,
     }
     if rank == 0:
@@ -968,22 +985,21 @@ def creasing_run(with_cpu):
 BATCH_SEED = 1004
 
 
-def run_batched(args):
+def batched_object(cg, ctx, n_plates, steps, warmup, reps=None, with_fp64=True):
+    """Config 4 (batched uneven plates): n_plates plates with node sides U{21..161}, 1-3
+    straight or arc creases each, assembled as one problem (PlateBatch); every step is one
+    CUDA-graph launch of the whole assembly (the residual kernel takes 32-point units from a
+    work counter and the tangent kernels stride over the cells of all plates: one global
+    work list), launch shape from the autotuner. The mixed step's residual is compared with
+    the FP64 assembly of the same batch."""
     import torch
 
-    import curvami_gb300 as cg
     from curvami_gb300 import autotune as at
     from curvami_gb300 import synth
 
-    from curvami_gb300.replicas import Replicas
-
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    reps = Replicas()
     t0 = time.perf_counter()
-    plates, xs = synth.config_batched(args.plates, seed=BATCH_SEED)   # the same batch on every rank
+    plates, xs = synth.config_batched(n_plates, seed=BATCH_SEED)   # the same batch on every rank
     gen_s = time.perf_counter() - t0
-    ctx = cg.Context(local)
     t0 = time.perf_counter()
     batch = cg.PlateBatch(plates, ctx)
     setup_s = time.perf_counter() - t0
@@ -996,48 +1012,71 @@ def run_batched(args):
     torch.cuda.synchronize()
     MIX = cg.TANGENT | cg.HINGE | cg.MIXED
     F64 = cg.TANGENT | cg.HINGE
-    name = torch.cuda.get_device_name(local).replace(" ", "_")
+    name = torch.cuda.get_device_name(torch.cuda.current_device()).replace(" ", "_")
     tune = at.autotune(asm, x_d.data_ptr(), K_d.data_ptr(), F_d.data_ptr(), MIX, device_name=name)
+    barrier = reps.barrier if reps else (lambda: None)
+    mx = reps.max if reps else (lambda v: v)
 
-    def timed_graph(flags, steps, warmup):
+    def timed_graph(flags, n, w):
         g = asm.graph(x_d.data_ptr(), K_d.data_ptr(), F_d.data_ptr(), flags)
-        for _ in range(warmup):
+        for _ in range(w):
             g.launch()
-        reps.barrier()
+        barrier()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(steps):
+        for _ in range(n):
             g.launch()
         e1.record(stream)
         torch.cuda.synchronize()
-        reps.barrier()
+        barrier()
         g.close()
-        return reps.max(e0.elapsed_time(e1) / steps)
+        return mx(e0.elapsed_time(e1) / n)
 
+    ms_mix = timed_graph(MIX, steps, warmup)
+    F_mix = F_d.cpu().numpy().copy()
+    out = {"workload": (f"batched uneven plates: {len(plates)} independent plates, node side U{{21..161}}, 4x4 rule, "
+                        "1-3 non-crossing straight or arc creases, Kt log-uniform [1e-4, 1e-1], seeded smooth "
+                        "displacement per plate; all plates in one assembler, one CUDA-graph launch per step"),
+           "seed": BATCH_SEED, "plates": len(plates), "n_gauss_points": batch.n_gp,
+           "n_nodes": int(batch.node_offset[-1]), "nnz_K": asm.nnz,
+           "sides_min_max": [min(int(p.meta["n_side"]) for p in plates), max(int(p.meta["n_side"]) for p in plates)],
+           "creases": int(sum(len(p.creases) for p in plates)), "generate_s": gen_s, "setup_s": setup_s,
+           "value": batch.n_gp / (ms_mix * 1e-3), "unit": UNIT, "ms_per_step": ms_mix,
+           "autotune": {"tuning": list(tune["tuning"]), "cached": tune["cached"], "ms": tune["ms"]},
+           "tensor_work": asm.tensor_stats()}
+    if with_fp64:
+        ms_f64 = timed_graph(F64, max(3, steps // 4), 3)
+        F_f64 = F_d.cpu().numpy()
+        out["fp64"] = {"value": batch.n_gp / (ms_f64 * 1e-3), "ms_per_step": ms_f64, "mixed_over_fp64": ms_f64 / ms_mix}
+        out["F_rel_diff_mixed_vs_fp64"] = float(np.abs(F_mix - F_f64).max() / np.abs(F_f64).max())
+    del batch, asm
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    return out
+
+
+def run_batched(args):
+    import torch
+
+    import curvami_gb300 as cg
+    from curvami_gb300.replicas import Replicas
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    reps = Replicas()
+    ctx = cg.Context(local)
     W = max(args.warmup, 3)
     with ClockSampler(local) as clk:
-        ms_mix = timed_graph(MIX, args.steps, W)
-    ms_f64 = timed_graph(F64, max(3, args.steps // 4), 3)
-    n = np.diff(batch.faces.download()["ptr"])
-    sides = [int(p.meta["n_side"]) for p in plates]
+        b = batched_object(cg, ctx, args.plates, args.steps, W, reps)
     line = {
-        "metric": METRIC, "value": world * batch.n_gp / (ms_mix * 1e-3), "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": W, "ms_per_step": ms_mix, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp64 residual + fp32 tangent", "data": "synthetic (seeded generator, no dataset)",
-        "config": {"workload": (f"batched uneven plates: {len(plates)} independent plates, node side U{{21..161}}, "
-                                "4x4 rule, 1-3 non-crossing straight or arc creases, Kt log-uniform [1e-4, 1e-1], "
-                                "seeded smooth displacement per plate; all plates in one assembler, one CUDA-graph "
-                                "launch per step"),
-                   "seed": BATCH_SEED, "plates": len(plates), "n_gauss_points": batch.n_gp,
-                   "n_nodes": int(batch.node_offset[-1]), "nnz_K": asm.nnz, "sides_min_max": [min(sides), max(sides)],
-                   "creases": int(sum(len(p.creases) for p in plates)), "mean_neighbours": float(n.mean()),
-                   "generate_s": gen_s, "setup_s": setup_s},
-        "fp64": {"value": world * batch.n_gp / (ms_f64 * 1e-3), "ms_per_step": ms_f64, "mixed_over_fp64": ms_f64 / ms_mix},
-        "autotune": {"tuning": list(tune["tuning"]), "cached": tune["cached"], "key": tune["key"],
-                     "ms": tune["ms"], "tried_ms": tune["tried"]},
-        "clocks": clk.summary(),
+        "metric": METRIC, "value": world * b["value"], "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": W, "ms_per_step": b["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64 residual + fp32-class tangent",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": {k: b[k] for k in ("workload", "seed", "plates", "n_gauss_points", "n_nodes", "nnz_K",
+                                     "sides_min_max", "creases", "generate_s", "setup_s")},
+        "fp64": b.get("fp64"), "autotune": b["autotune"], "clocks": clk.summary(),
     }
     if rank == 0:
         print(json.dumps(line))

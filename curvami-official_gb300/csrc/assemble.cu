@@ -1487,7 +1487,7 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
   // The tensor-core tangent takes the merged path's cells whose node union fits one
   // 128-row tile (its entries are the merged entries, so the deterministic lists are the
   // same).
-  const size_t tcsm = tc_smem_bytes(std::max(S->max_n, 1));
+  const size_t tcsm = tc_smem_bytes(std::max(S->max_n, 1), bzero);
   const bool use_tc = merged && a->tuning.tangent_kind == CGB_TANGENT_TENSOR && tcsm <= kMergedSmemMax;
   if (use_tc) tc_prepare(a);
   if (det && want_K) {
@@ -1644,9 +1644,11 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
         auto tk = det ? (bzero ? face_tangent_tc_kernel<true, true> : face_tangent_tc_kernel<false, true>)
                       : (bzero ? face_tangent_tc_kernel<true, false> : face_tangent_tc_kernel<false, false>);
         CGB_CUDA(cudaFuncSetAttribute(tk, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tcsm)));
+        CGB_CUDA(cudaFuncSetAttribute(tk, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         int tc_per_sm = 0;
         CGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tc_per_sm, tk, kTcThreads, tcsm));
-        tc_per_sm = std::min(std::max(tc_per_sm, 1), 2);   // 2 x 128 tensor-memory columns per SM at most
+        // Each CTA holds 256 of the SM's 512 tensor-memory columns: two CTAs per SM at most.
+        tc_per_sm = std::min(std::max(tc_per_sm, 1), 2);
         const unsigned tgrid2 = static_cast<unsigned>(std::max(1, std::min(groups, tc_per_sm * sms)));
         tk<<<tgrid2, kTcThreads, tcsm, a->side>>>(fa, st32, mg, tca);
         const auto& fb = a->tc_fallback_h;

@@ -1,7 +1,7 @@
 // cgb_umma.cuh — inline-PTX helpers for the 5th-generation tensor cores of sm_103a
 // (tcgen05): tensor-memory allocation, shared-memory matrix descriptors, the TF32 MMA
-// issued by one thread with its accumulator in tensor memory, completion through an
-// mbarrier, and the tensor-memory loads of the epilogue.
+// issued by one thread with its accumulator (and optionally its A operand) in tensor
+// memory, completion through an mbarrier, and the tensor-memory stores and loads.
 //
 // Encodings follow the PTX ISA's tcgen05 chapter:
 //  - shared-memory descriptor: start address >> 4 (bits 0-13), leading-dimension byte
@@ -59,6 +59,13 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64
                " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}"
                :: "r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate ? 1u : 0u) : "memory");
 }
+// The same with A in tensor memory (a_tmem: lanes = the 128 rows, one column per K element).
+__device__ __forceinline__ void mma_tf32_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                            bool accumulate) {
+  asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+               " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}"
+               :: "r"(d_tmem), "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate ? 1u : 0u) : "memory");
+}
 // The mbarrier receives one arrival when every MMA this thread issued before has completed.
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(saddr(bar))
@@ -77,6 +84,17 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
                : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+
+// 8 consecutive columns of this warp's 32 tensor-memory lanes from registers (one lane per
+// thread); tmem_st_wait() makes the stores complete before the tensor core reads them.
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+               :: "r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+                  "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+                  "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // x rounded to TF32 (round to nearest, ties away; the low 13 mantissa bits zero).
 __device__ __forceinline__ float to_tf32(float x) {
