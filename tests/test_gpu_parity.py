@@ -16,6 +16,9 @@ from oracle import Oracle
 
 pytestmark = pytest.mark.gpu
 
+# The mixed tangent's default is the tensor-core one (cgb_tuning.tangent_kind 0).
+TENSOR_DEFAULT = True
+
 
 @pytest.fixture(scope="module")
 def o():
@@ -198,8 +201,11 @@ def test_mixed_assembly(which, det, arc_case, row_case):
     fl = cg.TANGENT | cg.HINGE | cg.MIXED | (cg.DETERMINISTIC if det else 0)
     K, F = c.asm.assemble(c.x, fl)
     assert rel(F, Fo) < 1e-12  # FP64 residual
-    assert rel(K, Ko) < 1e-5   # FP32 tangent
-    assert np.linalg.norm(K - Ko) / np.linalg.norm(Ko) < 1e-6
+    assert rel(K, Ko) < 1e-5   # FP32-class tangent
+    # Frobenius: 1e-6 for FP32 CUDA cores (measured 1e-7); the default tensor-core tangent's
+    # 3xTF32 products (the lo x lo term dropped) accumulate in the tensor core's FP32: 3e-6
+    # (measured 0.9e-6 - 1.3e-6).
+    assert np.linalg.norm(K - Ko) / np.linalg.norm(Ko) < (3e-6 if TENSOR_DEFAULT else 1e-6)
 
 
 def test_residual_only_matches(arc_case):
