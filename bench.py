@@ -38,10 +38,13 @@ for _p in (ROOT, PKG_DIR):
 METRIC = "Gauss-pt residual+tangent evals/s, mixed vs FP64 GPU at stated error"
 UNIT = "GP evals/s"
 SEED = 1003
-# DRAM bytes (read + write) per Gauss point of the tensor-core tangent, from one ncu capture
-# of a 101 x 101 plate (160,000 Gauss points); None until measured.
-TENSOR_DRAM_BYTES_PER_GP = None
-TENSOR_TRAFFIC_SOURCE = "not captured yet"
+# DRAM bytes (read + write) per Gauss point of the merged FP32 tangent, from one ncu capture
+# of one 40,000-point launch on a 101 x 101 plate (the traffic per point does not depend on
+# the plate size, so it scales to the full launch by its points).
+TANGENT_DRAM_BYTES_PER_GP = 2082.0
+TANGENT_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one 40,000-point "
+                          "face_tangent_merged_kernel launch (101 x 101 plate), per Gauss point, times the "
+                          "points of one launch")
 WORKLOAD = ("single-plate assembly at scale: 201x201 jittered nodes, 4x4 Gauss rule (640,000 "
             "Gauss points), quadratic RKPM, quartic window, rho = 3h, circular-arc crease R = 60 "
             "with elastic hinge Kt = 1e-3, seeded 8-mode Fourier displacement (rotations up to 60 "
@@ -374,8 +377,16 @@ def run_gpu(args):
     asm.set_tuning(*tune_mix["tuning"])
     ms_det = timed(DET, max(3, args.steps // 4), 3)
     ms_res = timed(cg.HINGE | cg.MIXED, args.steps, 3)  # residual only (line-search trials)
-    asm.set_tuning(*tune_mix["tuning"][:3], cg.TANGENT_CORES)   # the CUDA-core tangent, same launch shape
-    ms_cores = timed(MIX, args.steps, 3)
+    asm.set_tuning(*tune_mix["tuning"][:3], cg.TANGENT_TENSOR)   # the tensor-core tangent, same launch shape
+    ms_tensor = timed(MIX, args.steps, 3)
+    ctx.profile(True)
+    ctx.profile_read(reset=True)
+    for _ in range(args.steps):
+        step(MIX)
+    torch.cuda.synchronize()
+    ph_tc_ms, ph_tc_n = ctx.profile_read(reset=True)
+    ctx.profile(False)
+    tc = asm.tensor_stats()
     asm.set_tuning(*tune_mix["tuning"])
 
     # Per-phase device times of the mixed step (events inside the library).
@@ -411,50 +422,55 @@ def run_gpu(args):
     barrier()
 
     # Roofline. The step runs two kernels per chunk: the FP64 residual kernel ("face") and,
-    # on a second stream, the FP32-class tangent ("tangent"): the tensor-core product per
-    # cell of 16 points (tcgen05, 3xTF32) and, for the cells whose node union exceeds one
-    # 128-row tile, the CUDA-core merged tangent. Times are sums over the step's chunk
-    # launches (events on each kernel's own stream).
+    # on a second stream, the FP32 tangent ("tangent", the merged CUDA-core kernel, which
+    # dominates). Its compute roof is the FP32 pipe; HBM is the secondary figure. Times are
+    # sums over the step's chunk launches (events on each kernel's own stream).
     ptr = model.faces.download()["ptr"]
     n = np.diff(ptr).astype(np.float64)
     steps = max(args.steps, 1)
     tan_ms = ph_ms["tangent"] / steps
     res_ms = ph_ms["face"] / steps
     work = asm.stats()
-    tc = asm.tensor_stats()
     tan_launches = max(int(ph_n["tangent"]) // steps, 1)
     flops_fp64 = float((121 * n + 200).sum())                 # residual path (FP64)
     flops_total = float((181 * n * (n + 1) / 2 + 364 * n + 200).sum())
     flops_fp32 = flops_total - flops_fp64                       # the tangent's share of F_B(n)
     # Compulsory bytes of the tangent per step: per-point state (32 floats), per neighbour
-    # the FP32 grad / Hessian Phi (20 B) and its node's union index (1 B), per merged entry its
-    # block slot and union indices (8 B), and the FP32 block accumulator once (48 B per block).
-    alg_bytes = float((128 + 21 * n).sum() + 8.0 * work["entries"] + 48.0 * work["blocks"])
-    # The tensor pipe's executed work: five 128 x N x 8 MMAs per point, 3xTF32 (10,240 N flops).
-    tensor_flops = 10240.0 * tc["point_cols"]
+    # the FP32 grad / Hessian Phi (20 B), per pair its 2-byte code, per merged entry its block
+    # slot and contribution range (8 B), and the FP32 block accumulator once (48 B per block).
+    alg_bytes = float((128 + 20 * n + n * (n + 1)).sum() + 8.0 * work["entries"] + 48.0 * work["blocks"])
     peaks, peak_kind = measured_peaks()
     p64, p32 = fma_peaks(local)
     tf32_peak = peaks["bf16_tflops"] / 2.0
-    tensor_path = asm.tuning is None or len(asm.tuning) < 4 or asm.tuning[3] == cg.TANGENT_TENSOR
     ach = flops_fp32 / (tan_ms * 1e-3) / 1e12
+    # The tensor-core tangent (tcgen05, 3xTF32), timed in the same step: its executed MMA work
+    # is five 128 x N x 8 MMAs per point (10,240 N flops).
+    tan_tc_ms = ph_tc_ms["tangent"] / steps
+    tensor_flops = 10240.0 * tc["point_cols"]
     roofline = {
-        "bound": "tensor", "achieved": ach, "peak": tf32_peak, "unit": "TFLOP/s", "frac": ach / tf32_peak,
-        "traffic": TENSOR_DRAM_BYTES_PER_GP * len(n) / tan_launches if TENSOR_DRAM_BYTES_PER_GP else None,
-        "traffic_source": TENSOR_TRAFFIC_SOURCE,
-        "peak_source": f"{peak_kind}: TF32 dense = half of MEASURED_PEAKS.json bf16_tflops (the tensor cores' "
-                       f"TF32:BF16 rate is 1:2)",
-        "kernel": ("face_tangent_tc_kernel (tcgen05.mma kind::tf32, 3xTF32, A in tensor memory, accumulator in "
-                   "tensor memory) + face_tangent_merged_kernel for the cells it does not take") if tensor_path else
-                  "face_tangent_merged_kernel (FP32 CUDA cores, merged contributions)",
+        "bound": "fp32", "achieved": ach, "peak": p32, "unit": "TFLOP/s", "frac": ach / p32,
+        "traffic": TANGENT_DRAM_BYTES_PER_GP * len(n) / tan_launches,
+        "traffic_source": TANGENT_TRAFFIC_SOURCE,
+        "peak_source": "measured live on this GPU (cgb_measure_fma_peaks: dependent FP32 FMA chains on "
+                       "every SM); MEASURED_PEAKS.json has no CUDA-core FP32 figure",
+        "kernel": "face_tangent_merged_kernel (FP32 CUDA cores, merged contributions)",
         "achieved_what": "the reference's hand-counted tangent flops, F_B(n) - F_R(n) per Gauss point, per second",
         "launch_ms": tan_ms / tan_launches, "launches_per_step": tan_launches, "step_ms": tan_ms,
-        "algorithmic_flops_per_step": flops_fp32, "work": work, "tensor_work": tc,
-        "tensor_pipe": {"executed_tflops": tensor_flops / (tan_ms * 1e-3) / 1e12,
-                        "frac": tensor_flops / (tan_ms * 1e-3) / 1e12 / tf32_peak,
-                        "what": "MMA flops issued (3xTF32, zero rows of each point's support and both "
-                                "triangles of the symmetric cell product included) over the tangent's time"},
+        "algorithmic_flops_per_step": flops_fp32, "work": work,
         "hbm": {"achieved_gbs": alg_bytes / (tan_ms * 1e-3) / 1e9, "peak_gbs": peaks["hbm_gbs"],
-                "frac": alg_bytes / (tan_ms * 1e-3) / 1e9 / peaks["hbm_gbs"], "algorithmic_bytes_per_step": alg_bytes},
+                "frac": alg_bytes / (tan_ms * 1e-3) / 1e9 / peaks["hbm_gbs"], "algorithmic_bytes_per_step": alg_bytes,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "tensor_core_tangent": {
+            "kernel": "face_tangent_tc_kernel (tcgen05.mma kind::tf32, 3xTF32, A in tensor memory, accumulator "
+                      "in tensor memory) + face_tangent_merged_kernel for the cells it does not take",
+            "step_ms": tan_tc_ms, "launches_per_step": max(int(ph_tc_n["tangent"]) // steps, 1),
+            "achieved_tflops": flops_fp32 / (tan_tc_ms * 1e-3) / 1e12,
+            "tensor_pipe": {"executed_tflops": tensor_flops / (tan_tc_ms * 1e-3) / 1e12, "peak": tf32_peak,
+                            "frac": tensor_flops / (tan_tc_ms * 1e-3) / 1e12 / tf32_peak,
+                            "peak_source": f"{peak_kind}: TF32 dense = half of MEASURED_PEAKS.json bf16_tflops",
+                            "what": "MMA flops issued (3xTF32, zero rows of each point's support and both "
+                                    "triangles of the symmetric cell product included) over the tangent's time"},
+            "work": tc},
         "pipes": {
             "fp64_residual": {"kernel": "face_residual_kernel", "step_ms": res_ms,
                               "achieved_tflops": flops_fp64 / (res_ms * 1e-3) / 1e12, "peak_tflops": p64,
@@ -496,8 +512,7 @@ def run_gpu(args):
         "metric": METRIC, "value": v_mix, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": W, "ms_per_step": ms_mix, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "fp64 residual + 3xtf32 tensor-core tangent (fp32 accumulation)" if tensor_path else
-                 "fp64 residual + fp32 tangent",
+        "dtype": "fp64 residual + fp32 tangent",
         "data": "synthetic (seeded generator, no dataset)",
         "config": {"workload": WORKLOAD, "seed": SEED, "n_gauss_points": n_gp, "n_nodes": plate.n_nodes,
                    "nnz_K": asm.nnz, "mean_neighbours": float(n.mean()), "max_neighbours": int(n.max()),
@@ -512,8 +527,9 @@ def run_gpu(args):
                  "phases_ms": {k: v / max(3, args.steps // 4) for k, v in ph64_ms.items()}},
         "deterministic_mixed": {"value": world * n_gp / (ms_det * 1e-3), "ms_per_step": ms_det},
         "residual_only": {"value": world * n_gp / (ms_res * 1e-3), "ms_per_step": ms_res},
-        "mixed_cuda_core_tangent": {"value": world * n_gp / (ms_cores * 1e-3), "ms_per_step": ms_cores,
-                                    "what": "the same step with every cell's tangent on the CUDA cores (FP32)"},
+        "mixed_tensor_core_tangent": {"value": world * n_gp / (ms_tensor * 1e-3), "ms_per_step": ms_tensor,
+                                      "what": "the same step with the tensor-core tangent (tcgen05, 3xTF32) for "
+                                              "every cell whose node union fits one 128-row tile"},
         "error_mixed_vs_fp64": err,
         "error_vs_oracle": err_oracle,
         "phases_ms": {k: v / max(args.steps, 1) for k, v in ph_ms.items()},

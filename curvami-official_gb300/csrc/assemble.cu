@@ -1645,10 +1645,16 @@ void assemble_device(cgb_assembler* a, const double* d_x, double* d_K, double* d
                       : (bzero ? face_tangent_tc_kernel<true, false> : face_tangent_tc_kernel<false, false>);
         CGB_CUDA(cudaFuncSetAttribute(tk, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tcsm)));
         CGB_CUDA(cudaFuncSetAttribute(tk, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-        int tc_per_sm = 0;
-        CGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tc_per_sm, tk, kTcThreads, tcsm));
-        // Each CTA holds 256 of the SM's 512 tensor-memory columns: two CTAs per SM at most.
-        tc_per_sm = std::min(std::max(tc_per_sm, 1), 2);
+        // Each CTA holds 256 of the SM's 512 tensor-memory columns: two CTAs per SM at most,
+        // when the shared memory of two (dynamic + static + the 1 KB the runtime reserves per
+        // CTA) fits the SM's.
+        cudaFuncAttributes fat{};
+        CGB_CUDA(cudaFuncGetAttributes(&fat, tk));
+        int smem_sm = 0;
+        CGB_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device));
+        int tc_per_sm = 2 * (tcsm + fat.sharedSizeBytes + 1024) <= static_cast<size_t>(smem_sm) ? 2 : 1;
+        if (a->tuning.tangent_ctas_per_sm > 0) tc_per_sm = std::min(tc_per_sm, a->tuning.tangent_ctas_per_sm);
+        a->tc_last_per_sm = tc_per_sm;
         const unsigned tgrid2 = static_cast<unsigned>(std::max(1, std::min(groups, tc_per_sm * sms)));
         tk<<<tgrid2, kTcThreads, tcsm, a->side>>>(fa, st32, mg, tca);
         const auto& fb = a->tc_fallback_h;

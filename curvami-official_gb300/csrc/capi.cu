@@ -555,7 +555,7 @@ int cgb_assembler_tensor_stats(cgb_assembler* a, int64_t out[4]) {
     out[0] = a->tc_n_groups;
     out[1] = static_cast<int64_t>(a->tc_fallback_h.size());
     out[2] = a->tc_point_cols;
-    out[3] = 0;
+    out[3] = a->tc_last_per_sm;
   });
 }
 

@@ -205,6 +205,7 @@ struct cgb_assembler {
   std::vector<int32_t> tc_fallback_h;
   int64_t tc_n_groups = 0;            // groups on the tensor path
   int64_t tc_point_cols = 0;          // sum over them of points x MMA columns (N)
+  int tc_last_per_sm = 0;             // CTAs per SM of the last tensor-core tangent launch
   cgb_tuning tuning{};                // launch shape (0 = library default)
   cgb::DevBuf<int> work_ctr;          // per-chunk work counters of the residual kernel
   uint32_t test_stage_extra_tx = 0;   // failure-detection test only: bytes the staging never gets

@@ -80,8 +80,8 @@ class ShapeParams(C.Structure):
     _fields_ = [("rho", dbl), ("rho_node", vp), ("order", i32), ("kernel", i32), ("precision", i32)]
 
 
-TANGENT_TENSOR = 0
-TANGENT_CORES = 1
+TANGENT_CORES = 0
+TANGENT_TENSOR = 1
 
 
 class NaturalCurvature(C.Structure):

@@ -264,12 +264,13 @@ class NonLinearAssembler:
         return dict(zip(("pairs", "blocks", "entries", "direct_groups"), (int(v) for v in out)))
 
     def tensor_stats(self):
-        """{"tensor_groups", "core_groups", "point_cols"}: the tensor-core tangent's share
-        (groups of 16 points as one tensor-core product, groups left to the CUDA cores, and
-        the sum of points x MMA columns, i.e. 10,240 x point_cols TF32 flops per assembly)."""
+        """{"tensor_groups", "core_groups", "point_cols", "ctas_per_sm"}: the tensor-core
+        tangent's share (groups of 16 points as one tensor-core product, groups left to the
+        CUDA cores, the sum of points x MMA columns, i.e. 10,240 x point_cols TF32 flops per
+        assembly) and the CTAs per SM of its last launch."""
         out = np.zeros(4, np.int64)
         self.ctx.check(self.ctx.lib.cgb_assembler_tensor_stats(self.h, _p(out)))
-        return dict(zip(("tensor_groups", "core_groups", "point_cols"), (int(v) for v in out[:3])))
+        return dict(zip(("tensor_groups", "core_groups", "point_cols", "ctas_per_sm"), (int(v) for v in out)))
 
     def csr_mapping(self):
         n = np.diff(self.faces.download()["ptr"])
@@ -295,8 +296,8 @@ class NonLinearAssembler:
                                                         C.c_void_p(d_F), int(flags)))
 
     def set_tuning(self, n_chunks=0, residual_threads=0, tangent_ctas_per_sm=0, tangent_kind=0):
-        """cgb_assembler_set_tuning (0 = the library's default; tangent_kind 0 the tensor-core
-        tangent, 1 the CUDA-core one)."""
+        """cgb_assembler_set_tuning (0 = the library's default; tangent_kind 0 the CUDA-core
+        tangent, 1 the tensor-core one)."""
         t = L.Tuning(int(n_chunks), int(residual_threads), int(tangent_ctas_per_sm), int(tangent_kind))
         self.ctx.check(self.ctx.lib.cgb_assembler_set_tuning(self.h, C.byref(t)))
         self.tuning = (int(n_chunks), int(residual_threads), int(tangent_ctas_per_sm), int(tangent_kind))

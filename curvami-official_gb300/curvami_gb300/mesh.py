@@ -249,34 +249,61 @@ def support_radius(node_xy, order):
 
 
 def plate_from_mesh(path, crease_tags=(), Kt=1e-3, order=2, kernel=0, rho=None, line_degree=1, face_degree=3,
-                    E=1.0, nu=0.3, thickness=0.05, theta0=0.0):
-    """A synth.Plate from a msh 4.1 file: the active nodes, the face Gauss points split on
-    the creases, one crease and one elastic fold per tag in `crease_tags`, rho from
-    support_radius (order 3, as main.cpp does) unless given."""
+                    E=1.0, nu=0.3, thickness=0.05, theta0=0.0, cuts=None, rigid=False):
+    """A synth.Plate from a msh 4.1 file (plate_from_elements of its nodes and elements)."""
     xy, elements = read_msh41(path)
+    return plate_from_elements(xy, elements, crease_tags, Kt, order, kernel, rho, line_degree, face_degree, E, nu,
+                               thickness, theta0, cuts, rigid, name=str(path))
+
+
+def plate_from_elements(xy, elements, crease_tags=(), Kt=1e-3, order=2, kernel=0, rho=None, line_degree=1,
+                        face_degree=3, E=1.0, nu=0.3, thickness=0.05, theta0=0.0, cuts=None, rigid=False,
+                        name="mesh"):
+    """A synth.Plate from mesh nodes and elements: the active nodes, the face Gauss points
+    split on the creases, one fold per tag in `crease_tags` from that tag's line Gauss points
+    (Kt, theta0 and rigid: one value for every fold or one per tag), rho from support_radius
+    (order 3, as main.cpp does) unless given. The crease curves that cut the supports are
+    `cuts` (lists of tags, each walked into one curve: main.cpp:171-176) or, without it, one
+    curve per crease tag (main.cpp:177-184)."""
+    xy = np.asarray(xy, np.float64)
     q = quadrature(xy, elements, line_degree, face_degree)
     active = q["active"]
     nodes = xy[active]
+    tags = [int(t) for t in crease_tags]
+
+    def per_tag(v, what):
+        if np.ndim(v) == 0:
+            return [v] * len(tags)
+        if len(v) != len(tags):
+            raise MeshError(f"{what}: one value per crease tag expected")
+        return list(v)
+
+    Kts, th0s, rigids = per_tag(Kt, "Kt"), per_tag(theta0, "theta0"), per_tag(rigid, "rigid")
     creases, folds = [], []
     exy, ew, et, en, etag = q["edge"]
-    for tag in crease_tags:
-        c = extract_curve(elements, xy, [tag])
-        if c is None:
-            raise MeshError(f"no line elements with entity tag {tag} in {path}")
-        creases.append({k: c[k] for k in ("vertices", "extend_start", "extend_end", "is_closed")})
+    for tag, kt, th, rg in zip(tags, Kts, th0s, rigids):
         sel = etag == tag
+        if not np.any(sel):
+            raise MeshError(f"no line elements with entity tag {tag} in {name}")
         s = 1e-7
         L = synth.PointSet(exy[sel] + s * en[sel], ew[sel].copy(), et[sel].copy())
         R = synth.PointSet(exy[sel] - s * en[sel], ew[sel].copy(), et[sel].copy())
-        folds.append(synth.Fold(L, R, float(Kt), float(theta0)))
+        folds.append(synth.Fold(L, R, float(kt), float(th), bool(rg)))
+    for cut in (cuts if cuts is not None else [[t] for t in tags]):
+        c = extract_curve(elements, xy, [int(t) for t in cut])
+        if c is None:
+            raise MeshError(f"no line elements with entity tags {list(cut)} in {name}")
+        creases.append({k: c[k] for k in ("vertices", "extend_start", "extend_end", "is_closed")})
     fxy, fw, _ = q["face"]
     faces, nsplit = synth.split_on_creases(synth.PointSet(fxy, fw), creases)
     r = support_radius(nodes, 3) if rho is None else float(rho)
     pxy, pw, ptag = q["point"]
     points = {int(t): synth.PointSet(pxy[ptag == t], pw[ptag == t]) for t in sorted(set(ptag.tolist()))}
-    return synth.Plate(name=str(path), node_xy=nodes, faces=faces, creases=creases, folds=folds, rho=r,
+    edges = {int(t): (exy[etag == t], ew[etag == t], et[etag == t], en[etag == t]) for t in sorted(set(etag.tolist()))}
+    return synth.Plate(name=name, node_xy=nodes, faces=faces, creases=creases, folds=folds, rho=r,
                        order=order, kernel=kernel, E=E, nu=nu, thickness=thickness,
-                       meta={"mesh": str(path), "split": nsplit, "elements": len(elements)}, points=points)
+                       meta={"mesh": name, "split": nsplit, "elements": len(elements), "edges": edges},
+                       points=points)
 
 
 def centre_crease_sheet(n_cells=20, half=1.0, crease_half=0.5, crease_segments=10, crease_tag=5):

@@ -25,8 +25,10 @@ def four_crease_case(n_side=13, Kt_driver=1e-1, Kt_passive=1e-3, target_deg=60.0
 
 
 class OracleAssemblyTheta(OracleAssembly):
-    """OracleAssembly with settable fold rest angles and the exact hinge tangent
+    """OracleAssembly with settable fold rest angles and, by default, the exact hinge tangent
     (Meshless::fold_exact_tangent), as the arc-length runs use it."""
+
+    exact_tangent = True
 
     def set_fold_theta0(self, f, theta0):
         self.folds[f]["theta0"] = float(theta0)
@@ -35,11 +37,11 @@ class OracleAssemblyTheta(OracleAssembly):
         K, F = super().assemble(x, want_K, hinge=False)
         if hinge:
             K, F = self.o.hinge(self.n, x, self.folds, self.outer, self.col_ptr, self.col_nodes, K, F,
-                                exact_tangent=True)
+                                exact_tangent=self.exact_tangent)
         return (K if want_K else None), F
 
 
-def oracle_arc_problem(o, p, doms):
+def oracle_arc_problem(o, p, doms, exact_tangent=True):
     n = len(p.node_xy)
 
     def shapes(pts):
@@ -61,5 +63,6 @@ def oracle_arc_problem(o, p, doms):
         sides.append(S.FoldSides(table(L), table(R), np.asarray(fd.left.tangent, np.float64), fd.theta0,
                                  Kt=fd.Kt, weight=np.asarray(fd.left.weight, np.float64)))
     backend = OracleAssemblyTheta(o, p, faces, folds_o)
+    backend.exact_tangent = bool(exact_tangent)
     points = [(dom, table(shapes(dom.xy))) for dom in doms]
     return S.PlateProblem(n, backend, table(faces), p.faces.weight, folds=sides, points=points)

@@ -165,7 +165,7 @@ def compare_with_oracle(o, p, load, lambdas, kkt="host", all_arms=True):
     arms = [("gpu_fp64", False, 0, None), ("gpu_fp64_oracle_shapes", False, 0, "oracle"),
             ("gpu_mixed_refined", True, 1, None)]
     if all_arms:
-        arms.append(("gpu_mixed", True, 0, None))
+        arms += [("gpu_mixed", True, 0, None), ("gpu_mixed_refined2", True, 2, None)]
     for name, mixed, refine, shapes in arms:
         # FP64 arms with the deterministic scatter: like the oracle's static schedule, every
         # run rounds the same way, so differences between the runs are reproducible.
@@ -245,7 +245,7 @@ def test_newton_config_small_plate(o):
             for side in ("ref", "run"):
                 assert 0.1 <= d[side]["merit_over_tol"] <= 10.0, (arm, out)
             assert all(abs(a - b) <= 1 for a, b in zip(it, ref)), (arm, out)
-    for arm in [a for a in ("gpu_mixed_refined", "gpu_mixed") if a in out]:
+    for arm in [a for a in ("gpu_mixed_refined", "gpu_mixed_refined2", "gpu_mixed") if a in out]:
         assert abs(sum(out[arm]["iters"]) - sum(ref)) <= 0.15 * sum(ref), (arm, out)
     for arm in [a for a in out if a.startswith("gpu")]:
         assert out[arm]["path_rel_diff"] <= 1e-6, (arm, out)
