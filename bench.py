@@ -1052,6 +1052,7 @@ def batched_object(cg, ctx, n_plates, steps, warmup, reps=None, with_fp64=True):
 
     ms_mix = timed_graph(MIX, steps, warmup)
     F_mix = F_d.cpu().numpy().copy()
+    K_mix = K_d.clone() if with_fp64 else None
     out = {"workload": (f"batched uneven plates: {len(plates)} independent plates, node side U{{21..161}}, 4x4 rule, "
                         "1-3 non-crossing straight or arc creases, Kt log-uniform [1e-4, 1e-1], seeded smooth "
                         "displacement per plate; all plates in one assembler, one CUDA-graph launch per step"),
@@ -1062,11 +1063,33 @@ def batched_object(cg, ctx, n_plates, steps, warmup, reps=None, with_fp64=True):
            "value": batch.n_gp / (ms_mix * 1e-3), "unit": UNIT, "ms_per_step": ms_mix,
            "autotune": {"tuning": list(tune["tuning"]), "cached": tune["cached"], "ms": tune["ms"]},
            "tensor_work": asm.tensor_stats()}
+    # Roofline of the graph step: the hand-counted flops of every point (F_B(n), the tangent's
+    # share on the FP32 pipe, F_R(n) on the FP64 pipe) over the whole step, in which the two
+    # kernels overlap; against the FP32 and FP64 peaks measured live on this GPU.
+    n = np.diff(batch.faces.download()["ptr"]).astype(np.float64)
+    fl64 = float((121 * n + 200).sum())
+    fl32 = float((181 * n * (n + 1) / 2 + 364 * n + 200).sum()) - fl64
+    p64, p32 = fma_peaks(torch.cuda.current_device())
+    a32 = fl32 / (ms_mix * 1e-3) / 1e12
+    a64 = fl64 / (ms_mix * 1e-3) / 1e12
+    out["roofline"] = {"bound": "fp32", "achieved": a32, "peak": p32, "unit": "TFLOP/s", "frac": a32 / p32,
+                       "what": "the reference's hand-counted tangent flops, F_B(n) - F_R(n) per Gauss point, over "
+                               "the whole graph step (the FP64 residual overlaps it)",
+                       "fp64_residual": {"achieved": a64, "peak": p64, "frac": a64 / p64 if p64 > 0 else None},
+                       "peak_source": "measured live on this GPU (cgb_measure_fma_peaks)",
+                       "mean_neighbours": float(n.mean())}
     if with_fp64:
         ms_f64 = timed_graph(F64, max(3, steps // 4), 3)
         F_f64 = F_d.cpu().numpy()
         out["fp64"] = {"value": batch.n_gp / (ms_f64 * 1e-3), "ms_per_step": ms_f64, "mixed_over_fp64": ms_f64 / ms_mix}
         out["F_rel_diff_mixed_vs_fp64"] = float(np.abs(F_mix - F_f64).max() / np.abs(F_f64).max())
+        # Per plate: each plate's block of F (its dofs) against the same plate's FP64 values.
+        off = 3 * np.asarray(batch.node_offset, np.int64)
+        per = [float(np.abs(F_mix[a:b] - F_f64[a:b]).max() / max(np.abs(F_f64[a:b]).max(), 1e-300))
+               for a, b in zip(off[:-1], off[1:])]
+        out["F_rel_inf_per_plate_max"] = max(per)
+        out["K_rel_fro_mixed_vs_fp64"] = float(torch.linalg.vector_norm(K_mix - K_d) / torch.linalg.vector_norm(K_d))
+        del K_mix
     del batch, asm
     ctx.set_stream(torch.cuda.current_stream().cuda_stream)
     return out

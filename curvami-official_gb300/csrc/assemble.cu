@@ -137,9 +137,9 @@ __device__ __forceinline__ void point_state(const double s[15], const Material& 
   P.Ci[0] = C11 * id; P.Ci[1] = -C01 * id; P.Ci[2] = -C01 * id; P.Ci[3] = C00 * id;
   double n[3] = {P.a1[1] * P.a2[2] - P.a1[2] * P.a2[1], P.a1[2] * P.a2[0] - P.a1[0] * P.a2[2],
                  P.a1[0] * P.a2[1] - P.a1[1] * P.a2[0]};
-  const double area = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  const double inv_area = 1.0 / sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);   // one division, not three
 #pragma unroll
-  for (int c = 0; c < 3; ++c) P.b[c] = n[c] / area;
+  for (int c = 0; c < 3; ++c) P.b[c] = n[c] * inv_area;
   P.e0[0] = 0.5 * (C00 - 1.0);
   P.e0[1] = 0.5 * (C11 - 1.0);
   P.e0[2] = 2.0 * (0.5 * C01);
@@ -279,35 +279,8 @@ __device__ __forceinline__ void phase1_point(const FaceArgs& a, int g0, int lane
       PointState P;
       point_state(s, m, P, a.gp_xy ? natcurv_kappa(a.nc, a.gp_xy[2 * static_cast<int64_t>(g)]) : 0.0);
       const double W = a.weight[g];
-      // f_I = W (Bm_I^T N + Bb_I^T M) (Assembly.h:249) = W (a1 u1 + a2 u2 + b Tu_I), since
-      // beta_I . M = dPhi_I . pXY - (Phi_XX M0 + 2 Phi_XY M2 + Phi_YY M1) = Tu_I.
-      const double NW0 = P.N[0] * W, NW1 = P.N[1] * W, NW2 = P.N[2] * W;
-      const double MW0 = P.M[0] * W, MW1 = P.M[1] * W, MW2 = 2.0 * P.M[2] * W;
-      const double pW0 = P.pXY[0] * W, pW1 = P.pXY[1] * W;
-      if (n > 0) {
-#pragma unroll 2
-        for (int q = 0; q < n; ++q) {
-          const int64_t es = sb + q * stride;
-          const int64_t e = p0 + q;
-          const double2 d = reinterpret_cast<const double2*>(Dp)[es];
-          const double dxx = Ddp[3 * es], dyy = Ddp[3 * es + 1], dxy = Ddp[3 * es + 2];
-          const double v1 = d.x * NW0 + d.y * NW2;
-          const double v2 = d.y * NW1 + d.x * NW2;
-          const double tu = d.x * pW0 + d.y * pW1 - (dxx * MW0 + dxy * MW2 + dyy * MW1);
-          double f[3];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) f[c] = P.a1[c] * v1 + P.a2[c] * v2 + P.b[c] * tu;
-          if (DET) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) a.Fc[3 * e + c] = f[c];
-          } else {
-            const int64_t node = Ix[es];
-            if (CHECK && (node < 0 || node >= a.n_nodes)) continue;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) atomicAdd(a.F + 3 * node + c, f[c]);
-          }
-        }
-      }
+      // The state the tangent needs goes out first, so that only the residual's coefficients
+      // stay live through the neighbour loop.
       if (st) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -326,6 +299,42 @@ __device__ __forceinline__ void phase1_point(const FaceArgs& a, int g0, int lane
         st[(S_P + 1) * st_stride + st_idx] = static_cast<TK>(P.pXY[1]);
         st[S_BV * st_stride + st_idx] = static_cast<TK>(P.bv);
         st[S_W * st_stride + st_idx] = static_cast<TK>(W);
+      }
+      // f_I = W (Bm_I^T N + Bb_I^T M) (Assembly.h:249) = W (a1 u1 + a2 u2 + b Tu_I), since
+      // beta_I . M = dPhi_I . pXY - (Phi_XX M0 + 2 Phi_XY M2 + Phi_YY M1) = Tu_I, with
+      // u1 = Phi_X N0 + Phi_Y N2 and u2 = Phi_Y N1 + Phi_X N2. It is linear in the five
+      // derivatives of Phi_I, so per point f_I[c] = Gx[c] Phi_X + Gy[c] Phi_Y + Hxx[c] Phi_XX +
+      // Hyy[c] Phi_YY + Hxy[c] Phi_XY: five FP64 FMAs per component and neighbour (GB300's
+      // FP64 pipe bounds this kernel).
+      double Gx[3], Gy[3], Hxx[3], Hyy[3], Hxy[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        Gx[c] = W * (P.a1[c] * P.N[0] + P.a2[c] * P.N[2] + P.b[c] * P.pXY[0]);
+        Gy[c] = W * (P.a1[c] * P.N[2] + P.a2[c] * P.N[1] + P.b[c] * P.pXY[1]);
+        Hxx[c] = -W * P.b[c] * P.M[0];
+        Hyy[c] = -W * P.b[c] * P.M[1];
+        Hxy[c] = -2.0 * W * P.b[c] * P.M[2];
+      }
+      if (n > 0) {
+#pragma unroll 2
+        for (int q = 0; q < n; ++q) {
+          const int64_t es = sb + q * stride;
+          const int64_t e = p0 + q;
+          const double2 d = reinterpret_cast<const double2*>(Dp)[es];
+          const double dxx = Ddp[3 * es], dyy = Ddp[3 * es + 1], dxy = Ddp[3 * es + 2];
+          double f[3];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) f[c] = Gx[c] * d.x + Gy[c] * d.y + Hxx[c] * dxx + Hyy[c] * dyy + Hxy[c] * dxy;
+          if (DET) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) a.Fc[3 * e + c] = f[c];
+          } else {
+            const int64_t node = Ix[es];
+            if (CHECK && (node < 0 || node >= a.n_nodes)) continue;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) atomicAdd(a.F + 3 * node + c, f[c]);
+          }
+        }
       }
     }
 }
@@ -1043,9 +1052,10 @@ __device__ __forceinline__ StageWin stage_window(int64_t q0, int64_t q1, int es)
 }
 
 // The block of the local pair (i, j) of one point from the frame (fr[0..1]: a1 | b.v,
-// a2), the I-side record (ri[0..1]) and the J-side record (rj), as in phase2_group. The
-// unit normal b = a1 x a2 / |a1 x a2| and g_I = a1 c0_I + a2 c1_I are rebuilt from the
-// frame here rather than read: the kernel is bound by shared-memory wavefronts, not FMAs.
+// a2), the I-side record (ri[0..1]) and the J-side record (rj), as in phase2_group, added
+// to v (the three rank-1 terms of each entry as one FMA chain onto it). The unit normal
+// b = a1 x a2 / |a1 x a2| and g_I = a1 c0_I + a2 c1_I are rebuilt from the frame here
+// rather than read: the kernel is bound by shared-memory wavefronts, not FMAs.
 template <bool BZERO>
 __device__ __forceinline__ void merged_pair(const float4* fr, const float4* ri, const float4* rj, float v[9]) {
   const float4 f0 = fr[0], f1 = fr[1];
@@ -1093,9 +1103,12 @@ __device__ __forceinline__ void merged_pair(const float4* fr, const float4* ri, 
     }
   }
 #pragma unroll
-  for (int r = 0; r < 3; ++r)
+  for (int r = 0; r < 3; ++r) {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) v[3 * r + c] = a1t[r] * Y1[c] + a2t[r] * Y2[c] + bt[r] * Y3[c] + (r == c ? geo : 0.0f);
+    for (int c = 0; c < 3; ++c)
+      v[3 * r + c] = fmaf(bt[r], Y3[c], fmaf(a2t[r], Y2[c], fmaf(a1t[r], Y1[c], v[3 * r + c])));
+    v[4 * r] += geo;
+  }
 }
 
 // DET: every entry's sum is stored (9 floats at unit e0 + e of a.Kc) for the ordered
@@ -1259,7 +1272,7 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
           int i = 0, off = p;
           while (off >= n - i) { off -= n - i; ++i; }
           const int j = i + off;
-          float v[9];
+          float v[9] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
           merged_pair<BZERO>(fr + FW * k, rec + RW * (k * nmax + i), rec + RW * (k * nmax + j) + 2, v);
           scatter_atomic<float>(a.Kacc, a.map_slot[m0 + p], a.idx[p0k + i] > a.idx[p0k + j], v);
         }
@@ -1281,10 +1294,7 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
           const unsigned code = next;
           if (c + 1 < cnt) next = codes[c + 1];
           const int k = code >> 12, i = (code >> 6) & 63, j = code & 63;
-          float v[9];
-          merged_pair<BZERO>(fr + FW * k, rec + RW * (k * nmax + i), rec + RW * (k * nmax + j) + 2, v);
-#pragma unroll
-          for (int q = 0; q < 9; ++q) acc[q] += v[q];
+          merged_pair<BZERO>(fr + FW * k, rec + RW * (k * nmax + i), rec + RW * (k * nmax + j) + 2, acc);
         }
         if constexpr (DET) {
           float* d = static_cast<float*>(a.Kc) + 9 * (e0 + e);
