@@ -1280,28 +1280,42 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
     } else {
       const int64_t e0 = mg.ent_ptr[G];
       const int ne = static_cast<int>(mg.ent_ptr[G + 1] - e0);
-      for (int e = threadIdx.x; e < ne; e += blockDim.x) {
-        const int cs = mg.ent_cstart[e0 + e];
+      // Each thread's entries are software-pipelined: the next entry's (count, first) word
+      // and its first code are fetched while this entry's contributions are summed, so that
+      // no entry starts on two dependent global loads.
+      const int step = static_cast<int>(blockDim.x);
+      const uint16_t* gcodes = mg.code + cbase;
+      int e = threadIdx.x;
+      int cs = e < ne ? mg.ent_cstart[e0 + e] : 0;
+      unsigned first = (e < ne && (cs >> 16) > 0) ? gcodes[cs & 0xffff] : 0u;
+      for (; e < ne; e += step) {
         const int cnt = cs >> 16, c0 = cs & 0xffff;
+        const int en = e + step;
+        const int cs_n = en < ne ? mg.ent_cstart[e0 + en] : 0;
+        const int32_t slot = DET ? 0 : mg.ent_slot[e0 + e];
         float acc[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) acc[q] = 0.0f;
-        // Codes are in the block's stored orientation (row node first); the next code is
-        // fetched while the current contribution is computed.
-        const uint16_t* codes = mg.code + cbase + c0;
-        unsigned next = cnt > 0 ? codes[0] : 0u;
+        // Codes are in the block's stored orientation (row node first); the next code (after
+        // the last one, the next entry's first) is fetched while the current contribution is
+        // computed.
+        const uint16_t* codes = gcodes + c0;
+        unsigned next = first;
         for (int c = 0; c < cnt; ++c) {
           const unsigned code = next;
           if (c + 1 < cnt) next = codes[c + 1];
+          else next = (cs_n >> 16) > 0 ? gcodes[cs_n & 0xffff] : 0u;
           const int k = code >> 12, i = (code >> 6) & 63, j = code & 63;
           merged_pair<BZERO>(fr + FW * k, rec + RW * (k * nmax + i), rec + RW * (k * nmax + j) + 2, acc);
         }
+        first = cnt > 0 ? next : ((cs_n >> 16) > 0 ? gcodes[cs_n & 0xffff] : 0u);
+        cs = cs_n;
         if constexpr (DET) {
           float* d = static_cast<float*>(a.Kc) + 9 * (e0 + e);
 #pragma unroll
           for (int q = 0; q < 9; ++q) d[q] = acc[q];
         } else {
-          float4* d = acc4 + 3 * static_cast<int64_t>(mg.ent_slot[e0 + e]);
+          float4* d = acc4 + 3 * static_cast<int64_t>(slot);
           atomicAdd(d, make_float4(acc[0], acc[1], acc[2], acc[3]));
           atomicAdd(d + 1, make_float4(acc[4], acc[5], acc[6], acc[7]));
           atomicAdd(d + 2, make_float4(acc[8], 0.0f, 0.0f, 0.0f));
