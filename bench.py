@@ -67,6 +67,10 @@ def parse():
     ap.add_argument("--plates", type=int, default=64, help="plates of the batched workload")
     ap.add_argument("--no-shape-stage", action="store_true",
                     help="skip the shape-function stage object (shorter runs under a profiler)")
+    ap.add_argument("--profile-mixed", default=None, metavar="CHUNKS,THREADS,CTAS,KIND",
+                    help="a short run for profilers: only W + K mixed steps of the assembly workload with this "
+                         "fixed launch shape (cgb_tuning fields), no autotuner and no other arm; prints one "
+                         "JSON line with the step time")
     ap.add_argument("--cpu-rows", type=int, default=None,
                     help="only the first CPU_ROWS cell rows on the CPU (a quick check; default: the whole plate)")
     return ap.parse_args()
@@ -346,6 +350,16 @@ def run_gpu(args):
         torch.cuda.synchronize()
         barrier()
         return max_over_ranks(e0.elapsed_time(e1) / steps)
+
+    if args.profile_mixed:
+        tuning = [int(v) for v in args.profile_mixed.split(",")]
+        asm.set_tuning(*tuning)
+        ms = timed(MIX, args.steps, args.warmup)
+        if rank == 0:
+            print(json.dumps({"profile_mixed": tuning, "workload": WORKLOAD, "n_side": args.n_side,
+                              "n_gauss_points": n_gp, "steps": args.steps, "warmup": args.warmup,
+                              "ms_per_step": ms, "value": n_gp / (ms * 1e-3), "unit": UNIT}))
+        return
 
     # Accuracy of the mixed assembly against the FP64 one on the same input.
     step(F64)
