@@ -38,6 +38,18 @@ def smoke_fixture():
         return json.load(f)
 
 
+# Paper A (examples/paperA_centre_crease/CB_n80_t0.5_xi10.json): the smoke case's run on the
+# 80 x 80 mesh CB_n80.msh with hinge stiffness Kt = xi D / L, xi = 10, L = 1.
+PAPER_A_KT = 10.0 * 1.098901098901099
+
+
+def paper_a_case(path, log_file=None):
+    xy = np.load(os.path.join(GOLDEN, "paper_a_cb_n80_nodes.npy"))
+    c = PC.centre_crease_case(path, 80, node_xy=xy, log_file=log_file)
+    c.plate.folds[0].Kt = PAPER_A_KT
+    return c
+
+
 def point_bcs():
     return smoke_case("/tmp/_smoke_bcs.msh", ideal=True).point_bcs
 
@@ -59,8 +71,12 @@ class OracleCreasingPlate:
     """The creasing-plate methods over the CPU oracle: FRNN once, RKPM again at every
     rebuild, updateStiffness + the (exact-tangent) hinge for the LineSearch problem."""
 
-    def __init__(self, o, p, spec, bcs, exact_tangent=True):
+    def __init__(self, o, p, spec, bcs, exact_tangent=True, static_schedule=False):
+        """static_schedule: the oracle's assembly splits the Gauss points statically over its
+        threads, so its sums round the same way on every run (the reference's guided schedule
+        otherwise)."""
         self.o, self.plate, self.specs = o, p, [spec]
+        self.static_schedule = bool(static_schedule)
         self.n = len(p.node_xy)
         self.exact = exact_tangent
         self._nb = {}
@@ -114,7 +130,7 @@ class OracleCreasingPlate:
         f = self.faces
         K, F = self.o.update_stiffness(self.n, self.plate.faces.weight, f["ptr"], f["idx"], f["dpsi"], f["ddpsi"],
                                        self.outer, self.mp, x, self.A, self.B, self.D, want_K=want_K,
-                                       n_threads=self.threads)
+                                       n_threads=self.threads, static_schedule=self.static_schedule)
         if hinge:
             K, F = self.o.hinge(self.n, x, [self.fold_dict], self.outer, self.col_ptr, self.col_nodes, K, F,
                                 exact_tangent=self.exact and want_K)

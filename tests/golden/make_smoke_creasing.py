@@ -30,16 +30,17 @@ from curvami_gb300 import creasing as PC  # noqa: E402
 from curvami_gb300 import mesh  # noqa: E402
 
 
-def main(ref_root):
-    src = os.path.join(ref_root, "examples", "smoke_centre_crease", "CB_n20.msh")
-    rxy, _ = mesh.read_msh41(src)
-    ideal, _ = mesh.centre_crease_sheet()
-    # Crease-line nodes and sheet nodes coincide in position; match each kind separately
-    # (the last 11 generator nodes are the crease line's own nodes).
+def reference_sheet_nodes(msh_path, n_cells):
+    """The node coordinates of one of the reference's centre-crease meshes (written by gmsh), in
+    the node order of curvami_gb300.mesh.centre_crease_sheet(n_cells)."""
     from scipy.spatial import cKDTree
 
+    rxy, _ = mesh.read_msh41(msh_path)
+    ideal, _ = mesh.centre_crease_sheet(n_cells=n_cells, crease_segments=n_cells // 2)
+    # Crease-line nodes and sheet nodes coincide in position; match each kind separately
+    # (the last n_cells / 2 + 1 generator nodes are the crease line's own nodes).
     out = np.empty_like(ideal)
-    n_sheet = len(ideal) - 11
+    n_sheet = len(ideal) - (n_cells // 2 + 1)
     used = set()
     tree = cKDTree(rxy)
     for i, p in enumerate(ideal):
@@ -48,11 +49,17 @@ def main(ref_root):
         if not cand:
             raise SystemExit(f"no reference node near {p}")
         # sheet nodes come first in the generator; gmsh lists the crease curve's nodes
-        # (points 10, 11 and the curve's interior) before the surface's interior nodes, so
-        # for a position shared by both take the later gmsh node for the sheet.
+        # (its end points and interior) before the surface's interior nodes, so for a
+        # position shared by both take the later gmsh node for the sheet.
         c = max(cand) if i < n_sheet else min(cand)
         used.add(c)
         out[i] = rxy[c]
+    return out
+
+
+def main(ref_root):
+    src = os.path.join(ref_root, "examples", "smoke_centre_crease", "CB_n20.msh")
+    out = reference_sheet_nodes(src, 20)
     np.save(os.path.join(HERE, "smoke_centre_crease_nodes.npy"), out)
 
     import creasing_helpers as H
