@@ -454,6 +454,7 @@ class _KKT:
     The two device modes stand in for the reference's symmetric MUMPS as direct solvers."""
 
     stats = {"solves": 0, "refine_steps": 0, "fallbacks": 0}   # refine_steps: GMRES steps
+    _last_rows = None   # size of the last device factorisation
 
     def __init__(self, K_upper, J, kkt="host", device="cuda"):
         """device: where the two dense modes run (a torch device; "cuda" for the GPU)."""
@@ -466,6 +467,12 @@ class _KKT:
         if self.device:
             import torch
 
+            # A KKT of another size (the constraint rows change as a crease grows) cannot reuse
+            # the blocks torch's allocator cached for the last one; give those back, or the cache
+            # grows with every size until it holds the whole device.
+            if _KKT._last_rows is not None and _KKT._last_rows != self.ns + self.nc:
+                torch.cuda.empty_cache()
+            _KKT._last_rows = self.ns + self.nc
             # Only the nonzeros cross to the GPU and the dense symmetric matrix is formed
             # there: K's stored upper triangle into both triangles, J into its two blocks
             # (no sparse symmetrisation or block assembly on the host).
