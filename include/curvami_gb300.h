@@ -240,8 +240,9 @@ int cgb_point_state_device(cgb_context* ctx, const cgb_shape* pts, const double*
  * allocates nothing.
  *
  * It runs the mixed-precision face assembly (FP64 residual, FP32 tangent, atomic
- * scatter; the same arithmetic as cgb_assemble_device with CGB_TANGENT | CGB_MIXED,
- * faces only, no hinge) on caller-owned arrays in the reference's own formats: the
+ * scatter, faces only, no hinge; the formulas of cgb_assemble_device with CGB_TANGENT |
+ * CGB_MIXED, but one warp per Gauss point and one scatter per pair, so K agrees with it to
+ * FP32 summation order, not bitwise) on caller-owned arrays in the reference's own formats: the
  * neighbour lists and shape derivatives of the face Gauss points, the K column starts
  * (Eigen outerIndexPtr) and the concatenated NonLinearAssembler::csrMapping positions.
  * Its FP32 block accumulator lives in a fixed array inside the library (every GPU that
