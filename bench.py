@@ -39,12 +39,13 @@ METRIC = "Gauss-pt residual+tangent evals/s, mixed vs FP64 GPU at stated error"
 UNIT = "GP evals/s"
 SEED = 1003
 # DRAM bytes (read + write) per Gauss point of the merged FP32 tangent, from one ncu capture
-# of one 40,000-point launch on a 101 x 101 plate (the traffic per point does not depend on
-# the plate size, so it scales to the full launch by its points).
-TANGENT_DRAM_BYTES_PER_GP = 2082.0
-TANGENT_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one 40,000-point "
-                          "face_tangent_merged_kernel launch (101 x 101 plate), per Gauss point, times the "
-                          "points of one launch")
+# of the whole 101 x 101 plate in one launch (160,000 points: 318.7 MB read + 20.9 MB
+# written); the traffic per point does not depend on the plate size, so it scales to the
+# full launch by its points.
+TANGENT_DRAM_BYTES_PER_GP = 2122.0
+TANGENT_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of face_tangent_merged_kernel over "
+                          "the 101 x 101 plate in one launch (bench.py --n-side 101 --profile-mixed 1,128,0,0), "
+                          "per Gauss point, times the points of one launch")
 WORKLOAD = ("single-plate assembly at scale: 201x201 jittered nodes, 4x4 Gauss rule (640,000 "
             "Gauss points), quadratic RKPM, quartic window, rho = 3h, circular-arc crease R = 60 "
             "with elastic hinge Kt = 1e-3, seeded 8-mode Fourier displacement (rotations up to 60 "
