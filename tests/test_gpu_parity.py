@@ -270,6 +270,13 @@ def test_assembly_with_coupling(ctx, arc_case):
     K1, F1 = asm.assemble(c.x, cg.TANGENT | cg.HINGE | cg.MIXED | cg.DETERMINISTIC)
     K2, F2 = asm.assemble(c.x, cg.TANGENT | cg.HINGE | cg.MIXED | cg.DETERMINISTIC)
     assert np.array_equal(K1, K2) and np.array_equal(F1, F2)
+    # The tensor-core tangent's general (B != 0) records: the same bars (Frobenius 3e-6).
+    asm.set_tuning(0, 0, 0, cg.TANGENT_TENSOR)
+    assert asm.tensor_stats()["tensor_groups"] > 0
+    for fl in (cg.MIXED, cg.MIXED | cg.DETERMINISTIC):
+        K, F = asm.assemble(c.x, cg.TANGENT | cg.HINGE | fl)
+        assert rel(F, Fo) < 1e-12, fl
+        assert rel(K, Ko) < 1e-5 and np.linalg.norm(K - Ko) / np.linalg.norm(Ko) < 3e-6, fl
 
 
 def test_assembler_stats(arc_case):
