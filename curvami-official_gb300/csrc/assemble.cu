@@ -1039,6 +1039,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return true;
 }
 
+// L2 prefetch of the bytes [lo, hi) of a global array whose base is 16-byte aligned: a
+// hint, so the window shrinks to the whole 16-byte units inside it (the bulk prefetch's
+// rule) and nothing outside the range is touched.
+__device__ __forceinline__ void l2_prefetch(const void* base, int64_t lo, int64_t hi) {
+  const int64_t b = (lo + 15) & ~static_cast<int64_t>(15), e = hi & ~static_cast<int64_t>(15);
+  if (e > b)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;"
+                 :: "l"(static_cast<const char*>(base) + b), "r"(static_cast<uint32_t>(e - b)) : "memory");
+}
+
 // Byte window [lo, lo + len) of the element range [q0, q1) of an array with `es`-byte
 // elements, widened to 16-byte boundaries (the bulk copy's alignment rule).
 struct StageWin { int64_t lo; uint32_t len, skip; };
@@ -1151,6 +1161,12 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
     mbar_expect(&stage_bar, wd.len + wdd.len + mg.extra_tx);
     if (wd.len) bulk_load(s_d, dpsi_b + wd.lo, wd.len, &stage_bar);
     if (wdd.len) bulk_load(s_dd, ddpsi_b + wdd.lo, wdd.len, &stage_bar);
+    // The group's pair codes and entry tables are read once per step from DRAM, one code per
+    // contribution: bring them into L2 now, a group ahead of their use.
+    l2_prefetch(mg.code, 2 * a.map_ptr[g0], 2 * a.map_ptr[g1]);
+    const int64_t e0 = mg.ent_ptr[G], e1 = mg.ent_ptr[G + 1];
+    l2_prefetch(mg.ent_cstart, 4 * e0, 4 * e1);
+    l2_prefetch(mg.ent_slot, 4 * e0, 4 * e1);
   };
   if (threadIdx.x == 0) {
     mbar_init(&stage_bar);
