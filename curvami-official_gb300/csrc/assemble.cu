@@ -1296,17 +1296,26 @@ __global__ void __launch_bounds__(kMrgThreads, 4) face_tangent_merged_kernel(Fac
     } else {
       const int64_t e0 = mg.ent_ptr[G];
       const int ne = static_cast<int>(mg.ent_ptr[G + 1] - e0);
-      // Each thread's entries are software-pipelined: the next entry's (count, first) word
-      // and its first code are fetched while this entry's contributions are summed, so that
-      // no entry starts on two dependent global loads.
+      // Entries are count-descending; thread t takes one entry per round of blockDim.x, in
+      // ascending order on even rounds and descending on odd ones, so that every warp's
+      // rounds add up to about the same work before the group's closing barrier. Each
+      // thread's entries are software-pipelined: the next entry's (count, first) word and its
+      // first code are fetched while this entry's contributions are summed, so that no entry
+      // starts on two dependent global loads.
       const int step = static_cast<int>(blockDim.x);
+      const int t = threadIdx.x;
+      auto entry_of = [&](int r) {
+        const int base = r * step, rem = min(step, ne - base);
+        return t < rem ? base + ((r & 1) ? rem - 1 - t : t) : ne;
+      };
       const uint16_t* gcodes = mg.code + cbase;
-      int e = threadIdx.x;
+      int r = 0;
+      int e = entry_of(0);
       int cs = e < ne ? mg.ent_cstart[e0 + e] : 0;
       unsigned first = (e < ne && (cs >> 16) > 0) ? gcodes[cs & 0xffff] : 0u;
-      for (; e < ne; e += step) {
+      for (; e < ne; e = entry_of(++r)) {
         const int cnt = cs >> 16, c0 = cs & 0xffff;
-        const int en = e + step;
+        const int en = entry_of(r + 1);
         const int cs_n = en < ne ? mg.ent_cstart[e0 + en] : 0;
         const int32_t slot = DET ? 0 : mg.ent_slot[e0 + e];
         float acc[9];
