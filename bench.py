@@ -469,8 +469,8 @@ def run_gpu(args):
         "peak_source": "measured live on this GPU (cgb_measure_fma_peaks: dependent FP32 FMA chains on "
                        "every SM); MEASURED_PEAKS.json has no CUDA-core FP32 figure",
         "kernel": "face_tangent_merged_kernel (FP32 CUDA cores, merged contributions)",
-        "binding_unit": ("the L1 / shared-memory data pipe: 87 % of its peak in ncu with the kernel alone "
-                         "(1.43 shared wavefronts per pair contribution), FMA pipe 40 %; in the step the FP64 "
+        "binding_unit": ("the L1 / shared-memory data pipe: 90 % of its peak in ncu with the kernel alone "
+                         "(1.44 shared wavefronts per pair contribution), FMA pipe 42 %; in the step the FP64 "
                          "residual's loads share that pipe"),
         "achieved_what": "the reference's hand-counted tangent flops, F_B(n) - F_R(n) per Gauss point, per second",
         "launch_ms": tan_ms / tan_launches, "launches_per_step": tan_launches, "step_ms": tan_ms,
